@@ -1,0 +1,785 @@
+// capi.cu -- the C ABI of libhdog: contexts, stage entry points, the batched substack
+// pipeline and the HDoG3D_main-compatible parameter-file runner.
+//
+// Reference host code this replaces: src/3D/HDoG3D_main.cpp (initializeGPU :58-109,
+// processSubstack :134-257, main :260-319) and src/3D/utils.h (loadParamFile :95-157,
+// loadImage :160-173, saveFeatureVector :204-250).
+#include <algorithm>
+#include <cerrno>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <mutex>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "json_min.hpp"
+#include "kernels.cuh"
+
+using namespace hdog;
+
+// ------------------------------------------------------------------ errors
+static thread_local std::string g_last_error;
+
+static int fail(int code, const std::string &msg) {
+  g_last_error = msg;
+  return code;
+}
+
+extern "C" int hdog_set_cuda_error(cudaError_t e, const char *what) {
+  return fail(HDOG_ERR_CUDA, std::string("CUDA error ") + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) +
+                                 ") in " + what);
+}
+
+extern "C" const char *hdog_last_error(void) { return g_last_error.c_str(); }
+extern "C" int hdog_abi_version(void) { return HDOG_ABI_VERSION; }
+
+#define TRY(expr)                          \
+  do {                                     \
+    int rc__ = (expr);                     \
+    if (rc__ != HDOG_OK) return rc__;      \
+  } while (0)
+
+// ------------------------------------------------------------------ parameters
+// calcGaussianWeight (DoG3DFilter.cu:372-392), host side, same float/double steps.
+static int gauss_taps(float sigma, float *h) {
+  int lw = (int)(2.0 * sigma + 0.5);
+  int length = lw * 2 + 1;
+  float p, sum;
+  sum = 1.f;
+  h[lw] = 1.f;
+  sigma *= sigma;
+  for (int i = 1; i <= lw; i++) {
+    p = (float)std::exp(-0.5 * i * i / sigma);
+    h[lw - i] = p;
+    h[lw + i] = p;
+    sum += p * 2;
+  }
+  for (int i = 0; i < length; i++) h[i] /= sum;
+  for (int i = length; i < kMaxTaps; i++) h[i] = 0;
+  return lw;
+}
+
+extern "C" int hdog_gaussian_taps(float sigma, float *taps80, int *radius) {
+  if (!taps80 || !radius) return fail(HDOG_ERR_ARG, "hdog_gaussian_taps: null pointer");
+  if (!(sigma >= 0.0f) || (int)(2.0 * sigma + 0.5) * 2 + 1 > kMaxTaps)
+    return fail(HDOG_ERR_SHAPE, "hdog_gaussian_taps: sigma must be in [0, 19.75)");
+  *radius = gauss_taps(sigma, taps80);
+  return HDOG_OK;
+}
+
+extern "C" int hdog_depth_margin(const hdog_params *p, int *margin) {
+  if (!p || !margin) return fail(HDOG_ERR_ARG, "hdog_depth_margin: null pointer");
+  float t[kMaxTaps];
+  int r;
+  TRY(hdog_gaussian_taps(p->sigma_z_large, t, &r));
+  *margin = r + p->extra_depth_margin;
+  return HDOG_OK;
+}
+
+static int validate(const hdog_params *p) {
+  if (!p) return fail(HDOG_ERR_ARG, "null params");
+  if (p->width < 2 || p->height < 2 || p->depth < 1)
+    return fail(HDOG_ERR_SHAPE, "width and height must be >= 2 and depth >= 1");
+  if ((int64_t)p->width * p->height * p->depth >= (int64_t)1 << 31)
+    return fail(HDOG_ERR_SHAPE, "a substack must hold fewer than 2^31 voxels (labels are int32 voxel indices)");
+  if (p->radius_norm_xy < 0 || p->radius_norm_z < 0 || p->radius_norm_xy > kMaxRadiusXY || p->radius_norm_z > 1000)
+    return fail(HDOG_ERR_SHAPE, "radius_norm.xy_large must be in [0, 421] and z_large in [0, 1000]");
+  if (p->erosion_radius_xy < 0 || p->erosion_radius_z < 0 || p->erosion_radius_xy > kMaxRadiusXY ||
+      p->erosion_radius_z > 1000)
+    return fail(HDOG_ERR_SHAPE, "erosion radius must be in [0, 421] (xy) and [0, 1000] (z)");
+  float t[kMaxTaps];
+  int r;
+  const float sig[4] = {p->sigma_xy_small, p->sigma_z_small, p->sigma_xy_large, p->sigma_z_large};
+  for (int k = 0; k < 4; k++) TRY(hdog_gaussian_taps(sig[k], t, &r));
+  if (p->min_intensity < 0 || p->min_intensity > 65535) return fail(HDOG_ERR_ARG, "min_intensity must fit in uint16");
+  if (p->min_size < 0 || p->min_size > 65535) return fail(HDOG_ERR_ARG, "min_size must fit in uint16");
+  return HDOG_OK;
+}
+
+// ------------------------------------------------------------------ context
+struct hdog_ctx {
+  hdog_params p;
+  int dev = 0;
+  int max_sub = 0;
+  int W = 0, H = 0, D = 0;
+  int64_t nvox = 0;        // W*H*D
+  int64_t reg_cap = 0;     // region slots per substack (background included)
+  int64_t nblk = 0;        // per-substack block slots (voxel blocks and region blocks)
+  int64_t nchk = 0;        // per-substack chunk slots
+  int margin = 0;
+  DogTaps taps;
+  std::mutex mu;
+
+  void *arena = nullptr;
+  size_t arena_bytes = 0;
+  uint16_t *img = nullptr;       // [max_sub * nvox] staging of host substacks
+  float2 *fa = nullptr, *fb = nullptr;   // [max_sub * nvox] temps (min/max, box, DoG)
+  float *norm = nullptr, *dog = nullptr;
+  uint8_t *mask = nullptr;
+  int32_t *labels = nullptr;
+  uint32_t *root_bits = nullptr, *blk_counts = nullptr, *blk_offsets = nullptr, *chunk = nullptr;
+  RegionAcc acc{};
+  RegionOut out{};
+  hdog_record *records = nullptr;
+  int64_t slots = 0;
+  int64_t *num_regions = nullptr, *num_records = nullptr;
+  int *status = nullptr;
+  Sub *d_subs = nullptr;
+  int64_t *d_seg = nullptr;      // [6][max_sub]: vseg off,len,chk ; rseg off,len,chk
+
+  // pinned host staging
+  Sub *h_subs = nullptr;
+  int64_t *h_seg = nullptr;
+  int64_t *h_counts = nullptr;   // [2*max_sub + 1]: records per substack, regions per substack, status
+  // device copy of a whole stack for hdog_run_stack with host input
+  uint16_t *stack_buf = nullptr;
+  size_t stack_bytes = 0;
+};
+
+static size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+struct Layout {
+  size_t off[32];
+  int n = 0;
+  size_t total = 0;
+  size_t add(size_t bytes) {
+    size_t o = total;
+    off[n++] = o;
+    total += align256(bytes);
+    return o;
+  }
+};
+
+static void plan(const hdog_params *p, int max_sub, int64_t &nvox, int64_t &reg_cap, int64_t &nblk,
+                 int64_t &nchk, Layout &L) {
+  nvox = (int64_t)p->width * p->height * p->depth;
+  reg_cap = (int64_t)((p->width + 1) / 2) * ((p->height + 1) / 2) * ((p->depth + 1) / 2) + 1;
+  const int64_t vb = (nvox + kScanBlock - 1) / kScanBlock, rb = (reg_cap + kFinalizeBlock - 1) / kFinalizeBlock;
+  nblk = vb > rb ? vb : rb;
+  nchk = (nblk + 1023) / 1024 + 1;
+  const int64_t S = max_sub, slots = S * reg_cap;
+  L.add(S * nvox * sizeof(uint16_t));        // 0 img
+  L.add(S * nvox * sizeof(float2));          // 1 fa
+  L.add(S * nvox * sizeof(float2));          // 2 fb
+  L.add(S * nvox * sizeof(float));           // 3 norm
+  L.add(S * nvox * sizeof(float));           // 4 dog
+  L.add(S * nvox * sizeof(uint8_t));         // 5 mask
+  L.add(S * nvox * sizeof(int32_t));         // 6 labels
+  L.add(S * nblk * (kScanBlock / 32) * sizeof(uint32_t));   // 7 root bits
+  L.add(S * nblk * sizeof(uint32_t));        // 8 blk counts
+  L.add(S * nblk * sizeof(uint32_t));        // 9 blk offsets
+  L.add(S * nchk * sizeof(uint32_t));        // 10 chunk
+  L.add(slots * sizeof(int32_t));            // 11 acc.label
+  L.add(slots * sizeof(uint32_t));           // 12 acc.count
+  L.add(slots * sizeof(uint32_t));           // 13 acc.max_ord
+  L.add(3 * slots * sizeof(unsigned long long));  // 14 acc.sum_xyz
+  L.add(slots * sizeof(double));             // 15 acc.sum_norm
+  L.add(6 * slots * sizeof(double));         // 16 acc.hess
+  L.add(slots * sizeof(float));              // 17 out.intensity
+  L.add(3 * slots * sizeof(float));          // 18 out.centroid
+  L.add(6 * slots * sizeof(float));          // 19 out.hessian
+  L.add(2 * slots * sizeof(float));          // 20 out.eigen
+  L.add(slots * sizeof(uint8_t));            // 21 out.keep
+  L.add(slots * sizeof(hdog_record));        // 22 records
+  L.add(S * sizeof(int64_t));                // 23 num_regions
+  L.add(S * sizeof(int64_t));                // 24 num_records
+  L.add(sizeof(int));                        // 25 status
+  L.add(S * sizeof(Sub));                    // 26 subs
+  L.add(6 * S * sizeof(int64_t));            // 27 seg
+}
+
+extern "C" int hdog_ctx_bytes(const hdog_params *p, int max_substacks, size_t *bytes) {
+  TRY(validate(p));
+  if (max_substacks < 1 || !bytes) return fail(HDOG_ERR_ARG, "hdog_ctx_bytes: bad arguments");
+  int64_t nvox, reg_cap, nblk, nchk;
+  Layout L;
+  plan(p, max_substacks, nvox, reg_cap, nblk, nchk, L);
+  *bytes = L.total;
+  return HDOG_OK;
+}
+
+static int make_taps(const hdog_params *p, DogTaps &T) {
+  memset(&T, 0, sizeof(T));
+  const float sig[4] = {p->sigma_xy_small, p->sigma_z_small, p->sigma_xy_large, p->sigma_z_large};
+  for (int k = 0; k < 4; k++) T.r[k] = gauss_taps(sig[k], T.k[k]);
+  // DoG3DFilter.cu:432, host powf as in the reference
+  T.normalizer = powf(p->sigma_xy_small, p->gamma_n * 2) * powf(p->sigma_z_small, p->gamma_n);
+  return HDOG_OK;
+}
+
+extern "C" int hdog_ctx_destroy(hdog_ctx *ctx) {
+  if (!ctx) return HDOG_OK;
+  cudaSetDevice(ctx->dev);
+  if (ctx->arena) cudaFree(ctx->arena);
+  if (ctx->stack_buf) cudaFree(ctx->stack_buf);
+  if (ctx->h_subs) cudaFreeHost(ctx->h_subs);
+  delete ctx;
+  return HDOG_OK;
+}
+
+extern "C" int hdog_ctx_create(const hdog_params *p, int max_substacks, hdog_ctx **out) {
+  if (!out) return fail(HDOG_ERR_ARG, "hdog_ctx_create: null output pointer");
+  *out = nullptr;
+  TRY(validate(p));
+  if (max_substacks < 1 || max_substacks > 65535) return fail(HDOG_ERR_ARG, "max_substacks must be in [1, 65535]");
+  HDOG_CUDA_TRY(cudaSetDevice(p->dev_id));
+  hdog_ctx *c = new hdog_ctx();
+  c->p = *p;
+  c->dev = p->dev_id;
+  c->max_sub = max_substacks;
+  c->W = p->width; c->H = p->height; c->D = p->depth;
+  Layout L;
+  plan(p, max_substacks, c->nvox, c->reg_cap, c->nblk, c->nchk, L);
+  c->slots = (int64_t)max_substacks * c->reg_cap;
+  TRY(hdog_depth_margin(p, &c->margin));
+  make_taps(p, c->taps);
+  cudaError_t e = cudaMalloc(&c->arena, L.total);
+  if (e != cudaSuccess) {
+    delete c;
+    return fail(HDOG_ERR_NOMEM, "hdog_ctx_create: cudaMalloc of " + std::to_string(L.total) + " bytes failed");
+  }
+  c->arena_bytes = L.total;
+  char *a = (char *)c->arena;
+  auto at = [&](int i) { return (void *)(a + L.off[i]); };
+  c->img = (uint16_t *)at(0);
+  c->fa = (float2 *)at(1);
+  c->fb = (float2 *)at(2);
+  c->norm = (float *)at(3);
+  c->dog = (float *)at(4);
+  c->mask = (uint8_t *)at(5);
+  c->labels = (int32_t *)at(6);
+  c->root_bits = (uint32_t *)at(7);
+  c->blk_counts = (uint32_t *)at(8);
+  c->blk_offsets = (uint32_t *)at(9);
+  c->chunk = (uint32_t *)at(10);
+  c->acc.label = (int32_t *)at(11);
+  c->acc.count = (uint32_t *)at(12);
+  c->acc.max_ord = (uint32_t *)at(13);
+  c->acc.sum_xyz = (unsigned long long *)at(14);
+  c->acc.sum_norm = (double *)at(15);
+  c->acc.hess = (double *)at(16);
+  c->out.intensity = (float *)at(17);
+  c->out.centroid = (float *)at(18);
+  c->out.hessian = (float *)at(19);
+  c->out.eigen = (float *)at(20);
+  c->out.keep = (uint8_t *)at(21);
+  c->records = (hdog_record *)at(22);
+  c->num_regions = (int64_t *)at(23);
+  c->num_records = (int64_t *)at(24);
+  c->status = (int *)at(25);
+  c->d_subs = (Sub *)at(26);
+  c->d_seg = (int64_t *)at(27);
+  const size_t hb = (size_t)max_substacks * sizeof(Sub) + 6 * (size_t)max_substacks * sizeof(int64_t) +
+                    (2 * (size_t)max_substacks + 2) * sizeof(int64_t);
+  e = cudaMallocHost(&c->h_subs, hb);
+  if (e != cudaSuccess) {
+    cudaFree(c->arena);
+    delete c;
+    return fail(HDOG_ERR_NOMEM, "hdog_ctx_create: pinned host staging failed");
+  }
+  c->h_seg = (int64_t *)(c->h_subs + max_substacks);
+  c->h_counts = c->h_seg + 6 * max_substacks;
+  *out = c;
+  return HDOG_OK;
+}
+
+// ------------------------------------------------------------------ batch helpers
+static FilterParams filter_of(const hdog_params &p) {
+  FilterParams f;
+  f.left = p.left_margin; f.right = p.right_margin; f.top = p.top_margin; f.bottom = p.bottom_margin;
+  f.min_size = p.min_size;
+  f.is_ave_mode = p.is_ave_mode;
+  return f;
+}
+
+// Fills the host descriptors of substack s (not yet uploaded).
+static void set_sub(hdog_ctx *c, int s, const uint16_t *src, int depth_valid, int z0) {
+  Sub &S = c->h_subs[s];
+  S.W = c->W; S.H = c->H; S.D = c->D;
+  S.depth_valid = depth_valid;
+  S.z0 = z0;
+  S.margin = c->margin;
+  S.vox = (int64_t)s * c->nvox;
+  S.reg = (int64_t)s * c->reg_cap;
+  S.reg_cap = c->reg_cap;
+  S.blk = (int64_t)s * c->nblk;
+  S.src = src;
+  const int ms = c->max_sub;
+  c->h_seg[0 * ms + s] = S.blk;
+  c->h_seg[1 * ms + s] = (c->nvox + kScanBlock - 1) / kScanBlock;
+  c->h_seg[2 * ms + s] = (int64_t)s * c->nchk;
+  c->h_seg[3 * ms + s] = S.blk;
+  c->h_seg[4 * ms + s] = (c->reg_cap + kFinalizeBlock - 1) / kFinalizeBlock;
+  c->h_seg[5 * ms + s] = (int64_t)s * c->nchk;
+}
+
+static int upload_subs(hdog_ctx *c, int nsub, cudaStream_t st) {
+  const int ms = c->max_sub;
+  HDOG_CUDA_TRY(cudaMemcpyAsync(c->d_subs, c->h_subs, nsub * sizeof(Sub), cudaMemcpyHostToDevice, st));
+  HDOG_CUDA_TRY(cudaMemcpyAsync(c->d_seg, c->h_seg, 6 * ms * sizeof(int64_t), cudaMemcpyHostToDevice, st));
+  return HDOG_OK;
+}
+
+static ScanSeg vseg_of(hdog_ctx *c) {
+  const int ms = c->max_sub;
+  return ScanSeg{c->d_seg, c->d_seg + ms, c->d_seg + 2 * ms, (c->nvox + kScanBlock - 1) / kScanBlock};
+}
+static ScanSeg rseg_of(hdog_ctx *c) {
+  const int ms = c->max_sub;
+  return ScanSeg{c->d_seg + 3 * ms, c->d_seg + 4 * ms, c->d_seg + 5 * ms,
+                 (c->reg_cap + kFinalizeBlock - 1) / kFinalizeBlock};
+}
+
+// Normalization of nsub substacks (descriptors already uploaded): src -> out_norm.
+static void enqueue_normalize(hdog_ctx *c, int nsub, float *out_norm, cudaStream_t st) {
+  const hdog_params &p = c->p;
+  const int plane = c->W * c->H;
+  const int64_t rows = (int64_t)c->H * c->D;
+  if (p.radius_norm_xy == 0 || p.radius_norm_z == 0) {
+    launch_copy_norm(c->d_subs, nsub, c->nvox, (float)p.min_intensity, out_norm, st);
+    return;
+  }
+  // min/max (exact): z from the raw slices, then x, then y; packed u32 in fb's halves
+  uint32_t *ma = reinterpret_cast<uint32_t *>(c->fb);
+  uint32_t *mb = ma + (int64_t)c->max_sub * c->nvox;
+  launch_minmax_z(c->d_subs, nsub, plane, p.radius_norm_z, ma, st);
+  launch_minmax_x(c->d_subs, nsub, rows, c->W, p.radius_norm_xy, ma, mb, st);
+  launch_minmax_y(c->d_subs, nsub, c->W, c->H, c->D, p.radius_norm_xy, mb, ma, st);
+  // box means in the reference order x -> y -> z, then the normalization
+  launch_box_x(c->d_subs, nsub, rows, c->W, p.radius_norm_xy, ma, c->fa, st);
+  launch_box_y(c->d_subs, nsub, c->W, c->H, c->D, p.radius_norm_xy, c->fa, c->fb, st);
+  launch_box_z_norm(c->d_subs, nsub, plane, p.radius_norm_z, (float)p.min_intensity, c->fb, out_norm, st);
+}
+
+static void enqueue_dog(hdog_ctx *c, int nsub, const float *norm, float *dog, cudaStream_t st) {
+  launch_dog(c->d_subs, nsub, c->W, c->H, c->D, (int64_t)c->H * c->D, c->taps, norm, c->fa, c->fb, dog, st);
+}
+
+// Whole chain for nsub substacks whose descriptors are set (host side).  Leaves record
+// counts, region counts and the status word in c->h_counts after a stream sync.
+static int run_batch(hdog_ctx *c, int nsub, cudaStream_t st) {
+  TRY(upload_subs(c, nsub, st));
+  HDOG_CUDA_TRY(cudaMemsetAsync(c->status, 0, sizeof(int), st));
+  if (c->p.erosion_radius_xy > 0 || c->p.erosion_radius_z > 0) {
+    // opt-in regional erosion of the input (the reference compiles Erosion3DFilter but
+    // never calls it); the eroded substacks replace the inputs in c->img
+    launch_erosion(c->d_subs, nsub, c->W, c->H, c->D, (int64_t)c->H * c->D, c->p.erosion_radius_xy,
+                   c->p.erosion_radius_z, nullptr, reinterpret_cast<uint16_t *>(c->fa), c->img, st);
+    for (int s = 0; s < nsub; s++) {
+      c->h_subs[s].src = c->img + (int64_t)s * c->nvox;
+      c->h_subs[s].depth_valid = c->D;   // the eroded volume already carries the zero tail
+    }
+    TRY(upload_subs(c, nsub, st));
+  }
+  enqueue_normalize(c, nsub, c->norm, st);
+  enqueue_dog(c, nsub, c->norm, c->dog, st);
+  launch_hessian_pd(c->d_subs, nsub, c->W, c->H, c->D, c->dog, c->mask, nullptr, st);
+  launch_ccl(c->d_subs, nsub, c->nvox, c->mask, c->labels, c->root_bits, c->blk_counts, c->status, st);
+  int32_t *rank = reinterpret_cast<int32_t *>(c->fa);
+  launch_regions(c->d_subs, nsub, c->nvox, vseg_of(c), c->mask, c->labels, c->root_bits, c->norm, c->dog, rank,
+                 c->blk_counts, c->blk_offsets, c->chunk, c->num_regions, c->acc, c->slots, c->status, st);
+  launch_finalize(c->d_subs, nsub, c->reg_cap, rseg_of(c), c->num_regions, c->acc, c->slots, c->out,
+                  filter_of(c->p), c->blk_counts, c->blk_offsets, c->chunk, c->num_records, c->records, st);
+  HDOG_CUDA_TRY(cudaGetLastError());
+  HDOG_CUDA_TRY(cudaMemcpyAsync(c->h_counts, c->num_records, nsub * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  HDOG_CUDA_TRY(cudaMemcpyAsync(c->h_counts + c->max_sub, c->num_regions, nsub * sizeof(int64_t),
+                                cudaMemcpyDeviceToHost, st));
+  HDOG_CUDA_TRY(cudaMemcpyAsync(c->h_counts + 2 * c->max_sub, c->status, sizeof(int), cudaMemcpyDeviceToHost, st));
+  HDOG_CUDA_TRY(cudaStreamSynchronize(st));
+  const int status = *(int *)(c->h_counts + 2 * c->max_sub);
+  if (status == HDOG_ERR_CAPACITY) return fail(HDOG_ERR_CAPACITY, "region capacity exceeded");
+  if (status != 0) return fail(status, "device loop limit reached in connected-component labelling");
+  return HDOG_OK;
+}
+
+// Appends the records of substacks [0, nsub) to out, in substack order.
+static int collect_records(hdog_ctx *c, int nsub, std::vector<hdog_record> &out, cudaStream_t st) {
+  size_t n = out.size(), total = n;
+  for (int s = 0; s < nsub; s++) total += (size_t)c->h_counts[s];
+  out.resize(total);
+  for (int s = 0; s < nsub; s++) {
+    const int64_t k = c->h_counts[s];
+    if (k > 0)
+      HDOG_CUDA_TRY(cudaMemcpyAsync(out.data() + n, c->records + (int64_t)s * c->reg_cap, k * sizeof(hdog_record),
+                                    cudaMemcpyDeviceToHost, st));
+    n += (size_t)k;
+  }
+  HDOG_CUDA_TRY(cudaStreamSynchronize(st));
+  return HDOG_OK;
+}
+
+static int copy_out(const std::vector<hdog_record> &v, hdog_record *out, int64_t cap, int64_t *n) {
+  *n = (int64_t)v.size();
+  if (*n > cap) return fail(HDOG_ERR_CAPACITY, "record buffer too small: " + std::to_string(*n) + " records");
+  if (*n > 0) memcpy(out, v.data(), v.size() * sizeof(hdog_record));
+  return HDOG_OK;
+}
+
+// ------------------------------------------------------------------ stage entry points
+static int single_sub(hdog_ctx *c, const uint16_t *src, cudaStream_t st) {
+  set_sub(c, 0, src, c->D, 0);
+  return upload_subs(c, 1, st);
+}
+
+#define CTX_GUARD(c)                                                   \
+  if (!(c)) return fail(HDOG_ERR_ARG, "null context");                 \
+  std::lock_guard<std::mutex> lock__((c)->mu);                         \
+  HDOG_CUDA_TRY(cudaSetDevice((c)->dev))
+
+extern "C" int hdog_normalize(hdog_ctx *c, const uint16_t *d_img, float *d_norm, void *stream) {
+  CTX_GUARD(c);
+  if (!d_img || !d_norm) return fail(HDOG_ERR_ARG, "hdog_normalize: null buffer");
+  cudaStream_t st = (cudaStream_t)stream;
+  TRY(single_sub(c, d_img, st));
+  enqueue_normalize(c, 1, d_norm, st);
+  HDOG_CUDA_TRY(cudaGetLastError());
+  return HDOG_OK;
+}
+
+extern "C" int hdog_dog(hdog_ctx *c, const float *d_norm, float *d_dog, void *stream) {
+  CTX_GUARD(c);
+  if (!d_norm || !d_dog) return fail(HDOG_ERR_ARG, "hdog_dog: null buffer");
+  cudaStream_t st = (cudaStream_t)stream;
+  TRY(single_sub(c, nullptr, st));
+  enqueue_dog(c, 1, d_norm, d_dog, st);
+  HDOG_CUDA_TRY(cudaGetLastError());
+  return HDOG_OK;
+}
+
+extern "C" int hdog_hessian_pd(hdog_ctx *c, const float *d_dog, uint8_t *d_mask, float *d_hessian, void *stream) {
+  CTX_GUARD(c);
+  if (!d_dog || !d_mask) return fail(HDOG_ERR_ARG, "hdog_hessian_pd: null buffer");
+  cudaStream_t st = (cudaStream_t)stream;
+  TRY(single_sub(c, nullptr, st));
+  launch_hessian_pd(c->d_subs, 1, c->W, c->H, c->D, d_dog, d_mask, d_hessian, st);
+  HDOG_CUDA_TRY(cudaGetLastError());
+  return HDOG_OK;
+}
+
+extern "C" int hdog_ccl(hdog_ctx *c, const uint8_t *d_mask, int32_t *d_labels, void *stream) {
+  CTX_GUARD(c);
+  if (!d_mask || !d_labels) return fail(HDOG_ERR_ARG, "hdog_ccl: null buffer");
+  cudaStream_t st = (cudaStream_t)stream;
+  TRY(single_sub(c, nullptr, st));
+  HDOG_CUDA_TRY(cudaMemsetAsync(c->status, 0, sizeof(int), st));
+  launch_ccl(c->d_subs, 1, c->nvox, d_mask, d_labels, c->root_bits, c->blk_counts, c->status, st);
+  HDOG_CUDA_TRY(cudaGetLastError());
+  int status = 0;
+  HDOG_CUDA_TRY(cudaMemcpyAsync(&status, c->status, sizeof(int), cudaMemcpyDeviceToHost, st));
+  HDOG_CUDA_TRY(cudaStreamSynchronize(st));
+  if (status) return fail(status, "device loop limit reached in connected-component labelling");
+  return HDOG_OK;
+}
+
+extern "C" int hdog_regional_features(hdog_ctx *c, const int32_t *d_labels, const float *d_norm,
+                                      const float *d_dog, hdog_regions *out, void *stream) {
+  CTX_GUARD(c);
+  if (!d_labels || !d_norm || !d_dog || !out) return fail(HDOG_ERR_ARG, "hdog_regional_features: null argument");
+  cudaStream_t st = (cudaStream_t)stream;
+  TRY(single_sub(c, nullptr, st));
+  HDOG_CUDA_TRY(cudaMemsetAsync(c->status, 0, sizeof(int), st));
+  // foreground = nonzero label; roots = voxels labelled with their own index
+  launch_roots_from_labels(c->d_subs, 1, c->nvox, d_labels, c->mask, c->root_bits, c->blk_counts, st);
+  int32_t *rank = reinterpret_cast<int32_t *>(c->fa);
+  launch_regions(c->d_subs, 1, c->nvox, vseg_of(c), c->mask, d_labels, c->root_bits, d_norm, d_dog, rank,
+                 c->blk_counts, c->blk_offsets, c->chunk, c->num_regions, c->acc, c->slots, c->status, st);
+  launch_finalize(c->d_subs, 1, c->reg_cap, rseg_of(c), c->num_regions, c->acc, c->slots, c->out, filter_of(c->p),
+                  c->blk_counts, c->blk_offsets, c->chunk, c->num_records, c->records, st);
+  HDOG_CUDA_TRY(cudaGetLastError());
+  int64_t nr = 0;
+  int status = 0;
+  HDOG_CUDA_TRY(cudaMemcpyAsync(&nr, c->num_regions, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  HDOG_CUDA_TRY(cudaMemcpyAsync(&status, c->status, sizeof(int), cudaMemcpyDeviceToHost, st));
+  HDOG_CUDA_TRY(cudaStreamSynchronize(st));
+  if (status == HDOG_ERR_CAPACITY) return fail(HDOG_ERR_CAPACITY, "region capacity exceeded");
+  if (status) return fail(status, "regional features failed");
+  out->num_regions = nr;
+  out->label = c->acc.label;
+  out->count = c->acc.count;
+  out->intensity = c->out.intensity;
+  out->centroid = c->out.centroid;
+  out->hessian = c->out.hessian;
+  out->eigen = c->out.eigen;
+  return HDOG_OK;
+}
+
+extern "C" int hdog_erosion(hdog_ctx *c, const uint16_t *d_src, uint16_t *d_dst, int rxy, int rz, void *stream) {
+  CTX_GUARD(c);
+  if (!d_src || !d_dst) return fail(HDOG_ERR_ARG, "hdog_erosion: null buffer");
+  if (rxy < 0 || rz < 0 || rxy > kMaxRadiusXY || rz > 1000)
+    return fail(HDOG_ERR_SHAPE, "hdog_erosion: radius out of range");
+  cudaStream_t st = (cudaStream_t)stream;
+  TRY(single_sub(c, d_src, st));
+  // the erosion writes dst at S.vox = 0; its scratch is fa (two packed volumes)
+  launch_erosion(c->d_subs, 1, c->W, c->H, c->D, (int64_t)c->H * c->D, rxy, rz, nullptr,
+                 reinterpret_cast<uint16_t *>(c->fa), d_dst, st);
+  HDOG_CUDA_TRY(cudaGetLastError());
+  return HDOG_OK;
+}
+
+// ------------------------------------------------------------------ whole chain
+extern "C" int hdog_run_substack(hdog_ctx *c, const uint16_t *img, int img_on_device, int depth_valid, int z0,
+                                 hdog_record *out, int64_t cap, int64_t *n_records, void *stream) {
+  CTX_GUARD(c);
+  if (!img || !n_records || (cap > 0 && !out)) return fail(HDOG_ERR_ARG, "hdog_run_substack: null argument");
+  if (depth_valid < 1 || depth_valid > c->D) return fail(HDOG_ERR_ARG, "depth_valid must be in [1, depth]");
+  cudaStream_t st = (cudaStream_t)stream;
+  const uint16_t *src = img;
+  if (!img_on_device) {
+    HDOG_CUDA_TRY(cudaMemcpyAsync(c->img, img, (size_t)depth_valid * c->W * c->H * sizeof(uint16_t),
+                                  cudaMemcpyHostToDevice, st));
+    src = c->img;
+  }
+  set_sub(c, 0, src, depth_valid, z0);
+  TRY(run_batch(c, 1, st));
+  std::vector<hdog_record> v;
+  TRY(collect_records(c, 1, v, st));
+  return copy_out(v, out, cap, n_records);
+}
+
+// z0 schedule of HDoG3D_main.cpp:309-314.
+static int schedule(int length, int D, int m, std::vector<int> &z0s) {
+  z0s.clear();
+  if (length - m <= 0) return HDOG_OK;
+  const int stride = D - 2 * m;
+  if (stride <= 0) return fail(HDOG_ERR_PARAM, "depth must exceed twice the depth margin");
+  for (int z0 = 0; z0 < length - m; z0 += stride) z0s.push_back(z0);
+  return HDOG_OK;
+}
+
+static int run_stack_locked(hdog_ctx *c, const uint16_t *stack, int on_device, int length,
+                            std::vector<hdog_record> &out, cudaStream_t st) {
+  std::vector<int> z0s;
+  TRY(schedule(length, c->D, c->margin, z0s));
+  if (z0s.empty()) return HDOG_OK;
+  const size_t plane = (size_t)c->W * c->H;
+  const uint16_t *dev = stack;
+  if (!on_device) {
+    const size_t bytes = (size_t)length * plane * sizeof(uint16_t);
+    if (bytes > c->stack_bytes) {
+      if (c->stack_buf) cudaFree(c->stack_buf);
+      c->stack_buf = nullptr;
+      c->stack_bytes = 0;
+      if (cudaMalloc(&c->stack_buf, bytes) != cudaSuccess)
+        return fail(HDOG_ERR_NOMEM, "hdog_run_stack: no device memory for the stack");
+      c->stack_bytes = bytes;
+    }
+    HDOG_CUDA_TRY(cudaMemcpyAsync(c->stack_buf, stack, bytes, cudaMemcpyHostToDevice, st));
+    dev = c->stack_buf;
+  }
+  for (size_t b = 0; b < z0s.size(); b += (size_t)c->max_sub) {
+    const int nsub = (int)std::min<size_t>((size_t)c->max_sub, z0s.size() - b);
+    for (int s = 0; s < nsub; s++) {
+      const int z0 = z0s[b + s];
+      set_sub(c, s, dev + (size_t)z0 * plane, std::min(c->D, length - z0), z0);
+    }
+    TRY(run_batch(c, nsub, st));
+    TRY(collect_records(c, nsub, out, st));
+  }
+  return HDOG_OK;
+}
+
+extern "C" int hdog_run_stack(hdog_ctx *c, const uint16_t *stack, int stack_on_device, int length,
+                              hdog_record *out, int64_t cap, int64_t *n_records, void *stream) {
+  CTX_GUARD(c);
+  if (!stack || !n_records || length < 0 || (cap > 0 && !out)) return fail(HDOG_ERR_ARG, "hdog_run_stack: bad argument");
+  std::vector<hdog_record> v;
+  TRY(run_stack_locked(c, stack, stack_on_device, length, v, (cudaStream_t)stream));
+  return copy_out(v, out, cap, n_records);
+}
+
+// ------------------------------------------------------------------ parameter file
+static int jnum(const json::Value *o, const char *key, double &v, bool required, const std::string &where) {
+  const json::Value *x = o ? o->get(key) : nullptr;
+  if (!x) return required ? fail(HDOG_ERR_PARAM, "parameter file: missing " + where + key) : 1;
+  if (x->kind == json::Value::Number) v = x->num;
+  else if (x->kind == json::Value::Bool) v = x->b ? 1 : 0;
+  else return fail(HDOG_ERR_PARAM, "parameter file: " + where + key + " is not a number");
+  return HDOG_OK;
+}
+
+struct StackSpec {
+  std::vector<std::string> src;
+  std::string dst;
+};
+
+static int load_param_file(const char *path, hdog_params *p, std::vector<StackSpec> *stacks, int *verbose) {
+  if (!path || !p) return fail(HDOG_ERR_ARG, "null argument");
+  std::ifstream f(path, std::ios::binary);
+  if (!f.is_open()) return fail(HDOG_ERR_IO, std::string("Unable to open file ") + path);
+  std::stringstream ss;
+  ss << f.rdbuf();
+  const std::string text = ss.str();
+  json::Value root;
+  std::string err;
+  if (!json::Parser(text).parse(root, err)) return fail(HDOG_ERR_PARAM, std::string("parameter file: ") + err);
+  if (root.kind != json::Value::Object) return fail(HDOG_ERR_PARAM, "parameter file: top level is not an object");
+  memset(p, 0, sizeof(*p));
+  double v;
+  TRY(jnum(&root, "devID", v, true, ""));
+  p->dev_id = (int)v;
+  if (verbose) {
+    *verbose = 0;
+    if (jnum(&root, "verbose", v, false, "") == HDOG_OK) *verbose = v != 0;
+  }
+  const json::Value *img = root.get("input_image_info");
+  if (!img) return fail(HDOG_ERR_PARAM, "parameter file: missing input_image_info");
+  TRY(jnum(img, "width", v, true, "input_image_info.")); p->width = (int)v;
+  TRY(jnum(img, "height", v, true, "input_image_info.")); p->height = (int)v;
+  TRY(jnum(img, "left_margin", v, true, "input_image_info.")); p->left_margin = (int)v;
+  TRY(jnum(img, "right_margin", v, true, "input_image_info.")); p->right_margin = (int)v;
+  TRY(jnum(img, "top_margin", v, true, "input_image_info.")); p->top_margin = (int)v;
+  TRY(jnum(img, "bottom_margin", v, true, "input_image_info.")); p->bottom_margin = (int)v;
+  const json::Value *co = root.get("coordinate_info");
+  if (!co) return fail(HDOG_ERR_PARAM, "parameter file: missing coordinate_info");
+  TRY(jnum(co, "scale_x", v, true, "coordinate_info."));
+  TRY(jnum(co, "scale_y", v, true, "coordinate_info."));
+  TRY(jnum(co, "scale_z", v, true, "coordinate_info."));
+  const json::Value *hp = root.get("HDoG_param");
+  if (!hp) return fail(HDOG_ERR_PARAM, "parameter file: missing HDoG_param");
+  const std::string w = "HDoG_param.";
+  TRY(jnum(hp, "depth", v, true, w)); p->depth = (int)v;
+  TRY(jnum(hp, "extra_depth_margin", v, true, w)); p->extra_depth_margin = (int)v;
+  const json::Value *rn = hp->get("radius_norm");
+  if (!rn) return fail(HDOG_ERR_PARAM, "parameter file: missing HDoG_param.radius_norm");
+  TRY(jnum(rn, "xy_large", v, true, w + "radius_norm.")); p->radius_norm_xy = (int)v;
+  TRY(jnum(rn, "z_large", v, true, w + "radius_norm.")); p->radius_norm_z = (int)v;
+  TRY(jnum(hp, "min_intensity", v, true, w)); p->min_intensity = (int)(uint16_t)(int64_t)v;
+  TRY(jnum(hp, "gamma_n", v, true, w)); p->gamma_n = (float)v;
+  const json::Value *sd = hp->get("sigma_dog");
+  if (!sd) return fail(HDOG_ERR_PARAM, "parameter file: missing HDoG_param.sigma_dog");
+  TRY(jnum(sd, "xy_small", v, true, w + "sigma_dog.")); p->sigma_xy_small = (float)v;
+  TRY(jnum(sd, "z_small", v, true, w + "sigma_dog.")); p->sigma_z_small = (float)v;
+  TRY(jnum(sd, "xy_large", v, true, w + "sigma_dog.")); p->sigma_xy_large = (float)v;
+  TRY(jnum(sd, "z_large", v, true, w + "sigma_dog.")); p->sigma_z_large = (float)v;
+  TRY(jnum(hp, "min_size", v, true, w)); p->min_size = (int)(uint16_t)(int64_t)v;
+  if (const json::Value *er = hp->get("erosion_radius")) {
+    if (jnum(er, "xy", v, false, w) == HDOG_OK) p->erosion_radius_xy = (int)v;
+    if (jnum(er, "z", v, false, w) == HDOG_OK) p->erosion_radius_z = (int)v;
+  }
+  if (jnum(&root, "is_ave_mode", v, false, "") == HDOG_OK) p->is_ave_mode = v != 0;
+  if (stacks) {
+    stacks->clear();
+    const json::Value *st = root.get("stacks");
+    if (!st || st->kind != json::Value::Array) return fail(HDOG_ERR_PARAM, "parameter file: missing stacks array");
+    for (const json::Value &s : st->arr) {
+      StackSpec sp;
+      const json::Value *src = s.get("src_paths");
+      const json::Value *dst = s.get("dst_path");
+      if (!src || src->kind != json::Value::Array || !dst || dst->kind != json::Value::String)
+        return fail(HDOG_ERR_PARAM, "parameter file: each stack needs src_paths[] and dst_path");
+      for (const json::Value &q : src->arr) {
+        if (q.kind != json::Value::String) return fail(HDOG_ERR_PARAM, "parameter file: src_paths must be strings");
+        sp.src.push_back(q.str);
+      }
+      sp.dst = dst->str;
+      stacks->push_back(std::move(sp));
+    }
+  }
+  return HDOG_OK;
+}
+
+extern "C" int hdog_params_load_json(const char *path, hdog_params *p) {
+  return load_param_file(path, p, nullptr, nullptr);
+}
+
+// loadImage (utils.h:160-173): the first W*H uint16 values of the file.  A file with
+// no data is an error; a short file leaves the rest of the slice zero.
+static int load_slice(const std::string &path, uint16_t *dst, size_t n) {
+  FILE *f = fopen(path.c_str(), "rb");
+  if (!f) return fail(HDOG_ERR_IO, "Unable to open " + path);
+  size_t got = fread(dst, sizeof(uint16_t), n, f);
+  fclose(f);
+  if (got == 0) return fail(HDOG_ERR_IO, "Unable to read " + path);
+  if (got < n) memset(dst + got, 0, (n - got) * sizeof(uint16_t));
+  return HDOG_OK;
+}
+
+extern "C" int hdog_run_param_file(const char *param_path, int verbose) {
+  hdog_params p;
+  std::vector<StackSpec> stacks;
+  int file_verbose = 0;
+  TRY(load_param_file(param_path, &p, &stacks, &file_verbose));
+  verbose = verbose || file_verbose;
+  int margin = 0;
+  TRY(validate(&p));
+  TRY(hdog_depth_margin(&p, &margin));
+  // as many substacks per batch as the longest stack needs, capped to keep memory modest
+  int max_len = 0;
+  for (auto &s : stacks) max_len = std::max(max_len, (int)s.src.size());
+  std::vector<int> z0s;
+  TRY(schedule(max_len, p.depth, margin, z0s));
+  int max_sub = std::max(1, std::min((int)z0s.size(), 8));
+  hdog_ctx *ctx = nullptr;
+  TRY(hdog_ctx_create(&p, max_sub, &ctx));
+  const size_t plane = (size_t)p.width * p.height;
+  uint16_t *h_stack = nullptr;
+  size_t h_cap = 0;
+  std::vector<hdog_record> recs;
+  int rc = HDOG_OK;
+  for (size_t i = 0; i < stacks.size() && rc == HDOG_OK; i++) {
+    const StackSpec &sp = stacks[i];
+    remove(sp.dst.c_str());   // the result is written in append mode (HDoG3D_main.cpp:295-300)
+    const int length = (int)sp.src.size();
+    TRY(schedule(length, p.depth, margin, z0s));
+    if (z0s.empty()) continue;
+    const size_t need = (size_t)length * plane;
+    if (need > h_cap) {
+      if (h_stack) cudaFreeHost(h_stack);
+      h_stack = nullptr;
+      if (cudaMallocHost(&h_stack, need * sizeof(uint16_t)) != cudaSuccess) {
+        rc = fail(HDOG_ERR_NOMEM, "pinned host buffer for the stack failed");
+        break;
+      }
+      h_cap = need;
+    }
+    // only the slices some substack reads
+    const int last = std::min(length, z0s.back() + p.depth);
+    for (int z = 0; z < last && rc == HDOG_OK; z++) rc = load_slice(sp.src[z], h_stack + (size_t)z * plane, plane);
+    if (rc != HDOG_OK) break;
+    recs.clear();
+    {
+      std::lock_guard<std::mutex> lock(ctx->mu);
+      rc = run_stack_locked(ctx, h_stack, 0, last, recs, nullptr);
+    }
+    if (rc != HDOG_OK) break;
+    const int64_t n = (int64_t)recs.size();
+    FILE *f = fopen(sp.dst.c_str(), "ab");
+    if (!f) { rc = fail(HDOG_ERR_IO, "Unable to open " + sp.dst); break; }
+    if (n > 0 && fwrite(recs.data(), sizeof(hdog_record), (size_t)n, f) != (size_t)n) {
+      fclose(f);
+      rc = fail(HDOG_ERR_IO, "Unable to write " + sp.dst);
+      break;
+    }
+    fclose(f);
+    if (verbose) printf("stack %zu: %d slices, %zu substacks, saved count:%lld\n", i, length, z0s.size(), (long long)n);
+  }
+  if (h_stack) cudaFreeHost(h_stack);
+  hdog_ctx_destroy(ctx);
+  return rc;
+}
+
+// ------------------------------------------------------------------ helpers
+extern "C" int hdog_memcpy(void *dst, const void *src, size_t bytes, void *stream) {
+  if (bytes == 0) return HDOG_OK;
+  if (!dst || !src) return fail(HDOG_ERR_ARG, "hdog_memcpy: null pointer");
+  HDOG_CUDA_TRY(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, (cudaStream_t)stream));
+  HDOG_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+  return HDOG_OK;
+}
+extern "C" int hdog_stream_sync(void *stream) {
+  HDOG_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+  return HDOG_OK;
+}
+extern "C" int hdog_device_alloc(void **ptr, size_t bytes) {
+  if (!ptr) return fail(HDOG_ERR_ARG, "hdog_device_alloc: null pointer");
+  HDOG_CUDA_TRY(cudaMalloc(ptr, bytes));
+  return HDOG_OK;
+}
+extern "C" int hdog_device_free(void *ptr) {
+  HDOG_CUDA_TRY(cudaFree(ptr));
+  return HDOG_OK;
+}

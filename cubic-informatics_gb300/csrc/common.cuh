@@ -1,0 +1,132 @@
+// common.cuh -- shared helpers for the HDoG sm_103a kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+
+#include "../../include/hdog.h"
+
+namespace hdog {
+
+// Volume geometry of one substack: x fastest, then y, then z (linear index
+// (z*H + y)*W + x, the layout of the reference's device buffers).
+struct Geom {
+  int W, H, D;
+  __host__ __device__ int64_t n() const { return (int64_t)W * H * D; }
+  __host__ __device__ int64_t plane() const { return (int64_t)W * H; }
+};
+
+__device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+// Packed u16 pair: low half = running min (erosion), high half = running max (dilation).
+__device__ __forceinline__ uint32_t pack_mm(uint32_t lo, uint32_t hi) { return lo | (hi << 16); }
+__device__ __forceinline__ uint32_t mm_combine(uint32_t a, uint32_t b) {
+  uint32_t lo = min(a & 0xFFFFu, b & 0xFFFFu);
+  uint32_t hi = max(a >> 16, b >> 16);
+  return lo | (hi << 16);
+}
+
+// Two IEEE round-to-nearest float adds / FMAs in one instruction (sm_100+ f32x2).  Each
+// lane rounds exactly like a scalar FADD / FFMA, so results equal the scalar chain.
+__device__ __forceinline__ float2 add2(float2 a, float2 b) {
+  unsigned long long ra = *reinterpret_cast<unsigned long long *>(&a);
+  unsigned long long rb = *reinterpret_cast<unsigned long long *>(&b);
+  unsigned long long rd;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(rd) : "l"(ra), "l"(rb));
+  return *reinterpret_cast<float2 *>(&rd);
+}
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
+  unsigned long long ra = *reinterpret_cast<unsigned long long *>(&a);
+  unsigned long long rb = *reinterpret_cast<unsigned long long *>(&b);
+  unsigned long long rc = *reinterpret_cast<unsigned long long *>(&c);
+  unsigned long long rd;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(rd) : "l"(ra), "l"(rb), "l"(rc));
+  return *reinterpret_cast<float2 *>(&rd);
+}
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) {
+  unsigned long long ra = *reinterpret_cast<unsigned long long *>(&a);
+  unsigned long long rb = *reinterpret_cast<unsigned long long *>(&b);
+  unsigned long long rd;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(rd) : "l"(ra), "l"(rb));
+  return *reinterpret_cast<float2 *>(&rd);
+}
+
+// Float max in a monotone unsigned encoding, for atomicMax on region maxima.
+__device__ __forceinline__ uint32_t f2ord(float f) {
+  uint32_t u = __float_as_uint(f);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__host__ __device__ __forceinline__ float ord2f(uint32_t o) {
+  uint32_t u = (o & 0x80000000u) ? (o & 0x7FFFFFFFu) : ~o;
+#ifdef __CUDA_ARCH__
+  return __uint_as_float(u);
+#else
+  float f;
+  memcpy(&f, &u, 4);
+  return f;
+#endif
+}
+
+// One central difference as gradientRowsKernel (:22-74) writes it:
+// sum = 0; sum += s[+1]; sum -= s[-1]; sum *= 0.5f.
+__device__ __forceinline__ float cdiff(float plus, float minus) {
+  return __fmul_rn(__fsub_rn(__fadd_rn(0.0f, plus), minus), 0.5f);
+}
+
+// Sylvester test of PositiveDefiniteKernel (:295-323) with each rounding written out:
+//   xx < 0,  fma(xx, yy, -(xy*xy)) > 0,
+//   det = fma(-(zz*xy), xy, fma(-(yy*xz), xz, fma(-(xx*yz), yz, fma(xx*yy, zz, (2xy*yz)*xz)))) < 0
+// This is the contraction nvcc applies to the reference's expression.
+__device__ __forceinline__ bool pd_test(float xx, float xy, float xz, float yy, float yz, float zz) {
+  if (!(xx < 0.0f)) return false;
+  const float m2 = __fmaf_rn(xx, yy, -__fmul_rn(xy, xy));
+  if (!(m2 > 0.0f)) return false;
+  const float p = __fmul_rn(xx, yy);
+  const float q = __fmul_rn(__fmul_rn(2.0f, xy), yz);
+  float t = __fmaf_rn(p, zz, __fmul_rn(q, xz));
+  t = __fmaf_rn(-__fmul_rn(xx, yz), yz, t);
+  t = __fmaf_rn(-__fmul_rn(yy, xz), xz, t);
+  const float det = __fmaf_rn(-__fmul_rn(zz, xy), xy, t);
+  return det < 0.0f;
+}
+
+// The six Hessian elements at voxel (x, y, z) straight from global memory, with the
+// same zero-halo rule as the tiled kernel: f outside the volume is 0 and a first
+// derivative at a position outside the volume is 0.  Order xx, xy, xz, yy, yz, zz.
+__device__ __forceinline__ float dog_ld(const float *f, int W, int H, int D, int x, int y, int z) {
+  return (x >= 0 && y >= 0 && z >= 0 && x < W && y < H && z < D) ? __ldg(f + ((int64_t)z * H + y) * W + x) : 0.0f;
+}
+__device__ __forceinline__ float grad1(const float *f, int W, int H, int D, int x, int y, int z, int dx,
+                                       int dy, int dz) {
+  if (x < 0 || y < 0 || z < 0 || x >= W || y >= H || z >= D) return 0.0f;
+  return cdiff(dog_ld(f, W, H, D, x + dx, y + dy, z + dz), dog_ld(f, W, H, D, x - dx, y - dy, z - dz));
+}
+__device__ __forceinline__ void hessian_at(const float *f, int W, int H, int D, int x, int y, int z,
+                                           float h[6]) {
+  h[0] = cdiff(grad1(f, W, H, D, x + 1, y, z, 1, 0, 0), grad1(f, W, H, D, x - 1, y, z, 1, 0, 0));
+  h[1] = cdiff(grad1(f, W, H, D, x, y + 1, z, 1, 0, 0), grad1(f, W, H, D, x, y - 1, z, 1, 0, 0));
+  h[2] = cdiff(grad1(f, W, H, D, x, y, z + 1, 1, 0, 0), grad1(f, W, H, D, x, y, z - 1, 1, 0, 0));
+  h[3] = cdiff(grad1(f, W, H, D, x, y + 1, z, 0, 1, 0), grad1(f, W, H, D, x, y - 1, z, 0, 1, 0));
+  h[4] = cdiff(grad1(f, W, H, D, x, y, z + 1, 0, 1, 0), grad1(f, W, H, D, x, y, z - 1, 0, 1, 0));
+  h[5] = cdiff(grad1(f, W, H, D, x, y, z + 1, 0, 0, 1), grad1(f, W, H, D, x, y, z - 1, 0, 0, 1));
+}
+
+constexpr int kMaxTaps = 80;   // MAX_KERNEL_LENGTH of the reference DoG taps
+
+// Gaussian taps of both DoG scales in constant memory: [0] small xy, [1] small z,
+// [2] large xy, [3] large z (the c_Kernel layout of the reference).
+struct DogTaps {
+  float k[4][kMaxTaps];
+  int r[4];
+  float normalizer;
+};
+
+}  // namespace hdog
+
+#define HDOG_CUDA_TRY(expr)                                 \
+  do {                                                      \
+    cudaError_t e__ = (expr);                               \
+    if (e__ != cudaSuccess) return hdog_set_cuda_error(e__, #expr); \
+  } while (0)
+
+extern "C" int hdog_set_cuda_error(cudaError_t e, const char *what);

@@ -1,0 +1,98 @@
+// kernels.cuh -- substack descriptors and the launchers each .cu file exports.
+#pragma once
+#include "common.cuh"
+
+namespace hdog {
+
+// One substack of a batch.  Volume arrays of a batch hold the substacks back to back;
+// substack s starts at voxel offset `vox`.  Kernels take the descriptor array in device
+// memory and use blockIdx.y as the substack index, blockIdx.x as the tile index inside
+// it (blocks past a smaller substack's tile count return at once).
+struct Sub {
+  int W, H, D;            // extent; D = HDoG_param.depth
+  int depth_valid;        // slices read from `src`; slices >= depth_valid are zero
+  int z0;                 // global z of slice 0, added to record centroid_z
+  int margin;             // depth margin m (records keep m <= cz < depth_valid - m)
+  int64_t vox;            // voxel offset of this substack in the batch volume arrays
+  int64_t reg;            // offset of its region slots in the region arrays
+  int64_t reg_cap;        // number of region slots (background included)
+  int64_t blk;            // offset of its per-block slots in block scratch arrays
+  const uint16_t *src;    // slice 0 of the raw input (device); slices are W*H apart
+};
+
+// Per-region accumulators (SoA over all region slots of a batch).
+struct RegionAcc {
+  int32_t *label;         // root voxel index (local to the substack)
+  uint32_t *count;
+  uint32_t *max_ord;      // f2ord(max normalized intensity)
+  unsigned long long *sum_xyz;   // [3][cap] exact coordinate sums
+  double *sum_norm;
+  double *hess;           // [6][cap]
+};
+
+struct RegionOut {
+  float *intensity;       // [cap]
+  float *centroid;        // [3][cap]
+  float *hessian;         // [6][cap]
+  float *eigen;           // [2][cap]
+  uint8_t *keep;          // [cap] record filter result
+};
+
+struct FilterParams {
+  int left, right, top, bottom;
+  int min_size;
+  int is_ave_mode;
+};
+
+inline unsigned ceil_div(int64_t a, int64_t b) { return (unsigned)((a + b - 1) / b); }
+
+// ---- norm.cu ----
+void launch_minmax_z(const Sub *d_subs, int nsub, int max_plane, int rz, uint32_t *mm, cudaStream_t s);
+void launch_minmax_x(const Sub *d_subs, int nsub, int64_t max_rows, int max_w, int r,
+                     const uint32_t *in, uint32_t *out, cudaStream_t s);
+void launch_minmax_y(const Sub *d_subs, int nsub, int max_w, int max_h, int max_d, int r,
+                     const uint32_t *in, uint32_t *out, cudaStream_t s);
+void launch_box_x(const Sub *d_subs, int nsub, int64_t max_rows, int max_w, int r,
+                  const uint32_t *in, float2 *out, cudaStream_t s);
+void launch_box_y(const Sub *d_subs, int nsub, int max_w, int max_h, int max_d, int r,
+                  const float2 *in, float2 *out, cudaStream_t s);
+void launch_box_z_norm(const Sub *d_subs, int nsub, int max_plane, int rz, float min_intensity,
+                       const float2 *in, float *norm, cudaStream_t s);
+void launch_copy_norm(const Sub *d_subs, int nsub, int64_t max_n, float min_intensity,
+                      float *norm, cudaStream_t s);
+void launch_erosion(const Sub *d_subs, int nsub, int max_w, int max_h, int max_d, int64_t max_rows,
+                    int rxy, int rz, const uint16_t *src_override, uint16_t *tmp, uint16_t *dst,
+                    cudaStream_t s);
+// ---- dog.cu ----
+void launch_dog(const Sub *d_subs, int nsub, int max_w, int max_h, int max_d, int64_t max_rows,
+                const DogTaps &T, const float *norm, float2 *t0, float2 *t1, float *dog, cudaStream_t s);
+void launch_hessian_pd(const Sub *d_subs, int nsub, int max_w, int max_h, int max_d,
+                       const float *dog, uint8_t *mask, float *hess6, cudaStream_t s);
+// ---- ccl.cu ----
+// Segments of a per-substack scan: substack s scans len[s] counts starting at off[s];
+// chk[s] is its offset in the chunk-sum scratch (one slot per 1024 counts).
+struct ScanSeg {
+  const int64_t *off, *len, *chk;
+  int64_t max_len;
+};
+void launch_scan(const ScanSeg &sg, int nsub, const uint32_t *in, uint32_t *out, uint32_t *chunk,
+                 int64_t *totals, int64_t add, cudaStream_t s);
+void launch_ccl(const Sub *d_subs, int nsub, int64_t max_n, const uint8_t *mask, int32_t *labels,
+                uint32_t *root_bits, uint32_t *blk_counts, int *d_status, cudaStream_t s);
+// Foreground mask (label != 0), root bitmap and per-block root counts from labels alone.
+void launch_roots_from_labels(const Sub *d_subs, int nsub, int64_t max_n, const int32_t *labels, uint8_t *mask,
+                              uint32_t *root_bits, uint32_t *blk_counts, cudaStream_t s);
+void launch_regions(const Sub *d_subs, int nsub, int64_t max_n, const ScanSeg &vseg, const uint8_t *mask,
+                    const int32_t *labels, const uint32_t *root_bits, const float *norm, const float *dog,
+                    int32_t *rank, uint32_t *blk_counts, uint32_t *blk_offsets, uint32_t *chunk,
+                    int64_t *d_num_regions, RegionAcc acc, int64_t slots, int *d_status, cudaStream_t s);
+void launch_finalize(const Sub *d_subs, int nsub, int64_t max_reg_cap, const ScanSeg &rseg,
+                     const int64_t *d_num_regions, RegionAcc acc, int64_t slots, RegionOut out,
+                     FilterParams fp, uint32_t *blk_counts, uint32_t *blk_offsets, uint32_t *chunk,
+                     int64_t *d_num_records, hdog_record *records, cudaStream_t s);
+
+constexpr int kMaxRadiusXY = 421;    // shared-memory bound of the min/max y pass
+constexpr int kScanBlock = 1024;     // voxels per block in the region scans
+constexpr int kFinalizeBlock = 256;  // regions per block in finalize / record compaction
+
+}  // namespace hdog

@@ -1,0 +1,358 @@
+"""Python host interface of the GB300 HDoG library (ctypes over include/hdog.h).
+
+Mirrors the reference's host functions for the HDoG path (CUBIC-informatics src/3D):
+Normalize3DFilter, DoG3DFilter, HessianPositiveDefiniteWithElement, CCL, the regional
+feature reductions, Erosion3DFilter, processSubstack and the HDoG3D_main executable.
+Device buffers are torch CUDA tensors; records come back as numpy arrays of the
+reference's ``dt_local`` layout (script/HalfBrainCells.py:11-15).
+
+The CUDA library must be built (``build()``); nothing here falls back to a CPU path.
+"""
+import ctypes
+import json
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_PKG = os.path.dirname(_HERE)
+BUILD_DIR = os.path.join(_PKG, "_build")
+LIB_PATH = os.path.join(BUILD_DIR, "libhdog.so")
+SYNTH_PATH = os.path.join(BUILD_DIR, "libhdog_synth.so")
+MAIN_PATH = os.path.join(BUILD_DIR, "hdog_main")
+
+HDOG_OK, HDOG_ERR_ARG, HDOG_ERR_SHAPE, HDOG_ERR_CUDA, HDOG_ERR_IO = 0, 1, 2, 3, 4
+HDOG_ERR_PARAM, HDOG_ERR_CAPACITY, HDOG_ERR_TIMEOUT, HDOG_ERR_NOMEM = 5, 6, 7, 8
+
+# The 28-byte candidate record (FeatureVector, src/3D/utils.h:188-197).
+DT_LOCAL = np.dtype([
+    ("local_x", "<f4"), ("local_y", "<f4"), ("local_z", "<f4"),
+    ("structureness", "<f4"), ("blobness", "<f4"), ("intensity", "<f4"),
+    ("size", "<u2"), ("padding", "<u2"),
+])
+
+
+class HDoGError(RuntimeError):
+    def __init__(self, code, message):
+        super().__init__("hdog error %d: %s" % (code, message))
+        self.code = code
+
+
+class hdog_params(ctypes.Structure):
+    _fields_ = [
+        ("width", ctypes.c_int), ("height", ctypes.c_int), ("depth", ctypes.c_int),
+        ("left_margin", ctypes.c_int), ("right_margin", ctypes.c_int),
+        ("top_margin", ctypes.c_int), ("bottom_margin", ctypes.c_int),
+        ("extra_depth_margin", ctypes.c_int),
+        ("radius_norm_xy", ctypes.c_int), ("radius_norm_z", ctypes.c_int),
+        ("min_intensity", ctypes.c_int),
+        ("gamma_n", ctypes.c_float),
+        ("sigma_xy_small", ctypes.c_float), ("sigma_z_small", ctypes.c_float),
+        ("sigma_xy_large", ctypes.c_float), ("sigma_z_large", ctypes.c_float),
+        ("min_size", ctypes.c_int), ("is_ave_mode", ctypes.c_int),
+        ("erosion_radius_xy", ctypes.c_int), ("erosion_radius_z", ctypes.c_int),
+        ("dev_id", ctypes.c_int),
+    ]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class hdog_regions(ctypes.Structure):
+    _fields_ = [
+        ("num_regions", ctypes.c_int64),
+        ("label", ctypes.c_void_p), ("count", ctypes.c_void_p), ("intensity", ctypes.c_void_p),
+        ("centroid", ctypes.c_void_p), ("hessian", ctypes.c_void_p), ("eigen", ctypes.c_void_p),
+    ]
+
+
+_P = ctypes.c_void_p
+_SIGNATURES = {
+    "hdog_last_error": (ctypes.c_char_p, []),
+    "hdog_abi_version": (ctypes.c_int, []),
+    "hdog_params_load_json": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(hdog_params)]),
+    "hdog_gaussian_taps": (ctypes.c_int, [ctypes.c_float, _P, ctypes.POINTER(ctypes.c_int)]),
+    "hdog_depth_margin": (ctypes.c_int, [ctypes.POINTER(hdog_params), ctypes.POINTER(ctypes.c_int)]),
+    "hdog_ctx_create": (ctypes.c_int, [ctypes.POINTER(hdog_params), ctypes.c_int, ctypes.POINTER(_P)]),
+    "hdog_ctx_destroy": (ctypes.c_int, [_P]),
+    "hdog_ctx_bytes": (ctypes.c_int, [ctypes.POINTER(hdog_params), ctypes.c_int, ctypes.POINTER(ctypes.c_size_t)]),
+    "hdog_normalize": (ctypes.c_int, [_P, _P, _P, _P]),
+    "hdog_dog": (ctypes.c_int, [_P, _P, _P, _P]),
+    "hdog_hessian_pd": (ctypes.c_int, [_P, _P, _P, _P, _P]),
+    "hdog_ccl": (ctypes.c_int, [_P, _P, _P, _P]),
+    "hdog_regional_features": (ctypes.c_int, [_P, _P, _P, _P, ctypes.POINTER(hdog_regions), _P]),
+    "hdog_erosion": (ctypes.c_int, [_P, _P, _P, ctypes.c_int, ctypes.c_int, _P]),
+    "hdog_run_substack": (ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P, ctypes.c_int64,
+                                         ctypes.POINTER(ctypes.c_int64), _P]),
+    "hdog_run_stack": (ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.c_int, _P, ctypes.c_int64,
+                                      ctypes.POINTER(ctypes.c_int64), _P]),
+    "hdog_run_param_file": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int]),
+    "hdog_memcpy": (ctypes.c_int, [_P, _P, ctypes.c_size_t, _P]),
+    "hdog_stream_sync": (ctypes.c_int, [_P]),
+    "hdog_device_alloc": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.c_size_t]),
+    "hdog_device_free": (ctypes.c_int, [_P]),
+}
+
+_lib = None
+
+
+def lib():
+    """The loaded libhdog.so; raises when the CUDA library has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise HDoGError(HDOG_ERR_ARG, "libhdog.so is not built (%s); run build()" % LIB_PATH)
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def build(verbose=False):
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("_hdog_build", os.path.join(_PKG, "build.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.build(verbose=verbose)
+
+
+def check(rc):
+    if rc != HDOG_OK:
+        raise HDoGError(rc, lib().hdog_last_error().decode("utf-8", "replace"))
+
+
+# ---------------------------------------------------------------- parameters
+PARAM_DEFAULTS = dict(width=2560, height=2160, depth=32, left_margin=100, right_margin=100, top_margin=100,
+                      bottom_margin=100, extra_depth_margin=3, radius_norm_xy=100, radius_norm_z=5,
+                      min_intensity=1000, gamma_n=1.0, sigma_xy_small=4.0, sigma_z_small=1.8,
+                      sigma_xy_large=6.0, sigma_z_large=2.7, min_size=10, is_ave_mode=0,
+                      erosion_radius_xy=0, erosion_radius_z=0, dev_id=0)
+
+
+def make_params(**kw):
+    p = hdog_params()
+    d = dict(PARAM_DEFAULTS)
+    d.update(kw)
+    for k, v in d.items():
+        setattr(p, k, v)
+    return p
+
+
+def load_param_file(path):
+    """loadParamFile (src/3D/utils.h:95-157): the HDoG keys of a parameter JSON."""
+    p = hdog_params()
+    check(lib().hdog_params_load_json(os.fsencode(path), ctypes.byref(p)))
+    return p
+
+
+def write_param_file(path, p, stacks, gpus=(0,)):
+    """Writes a parameter JSON in the reference's layout (param/param_example_HDoG_FW.json)
+    with `stacks` = [(dst_path, [src_path, ...]), ...]."""
+    d = {
+        "devID": int(p.dev_id), "gpus": list(gpus),
+        "input_image_info": {"width": p.width, "height": p.height, "left_margin": p.left_margin,
+                             "right_margin": p.right_margin, "top_margin": p.top_margin,
+                             "bottom_margin": p.bottom_margin},
+        "coordinate_info": {"scale_x": 1.0, "scale_y": 1.0, "scale_z": 1.0},
+        "HDoG_param": {"depth": p.depth, "extra_depth_margin": p.extra_depth_margin,
+                       "radius_norm": {"xy_large": p.radius_norm_xy, "z_large": p.radius_norm_z},
+                       "min_intensity": p.min_intensity, "gamma_n": p.gamma_n,
+                       "sigma_dog": {"xy_small": p.sigma_xy_small, "z_small": p.sigma_z_small,
+                                     "xy_large": p.sigma_xy_large, "z_large": p.sigma_z_large},
+                       "min_size": p.min_size},
+        "is_ave_mode": bool(p.is_ave_mode),
+        "stacks": [{"dst_path": dst, "src_paths": list(src)} for dst, src in stacks],
+    }
+    if p.erosion_radius_xy or p.erosion_radius_z:
+        d["HDoG_param"]["erosion_radius"] = {"xy": p.erosion_radius_xy, "z": p.erosion_radius_z}
+    with open(path, "w") as f:
+        json.dump(d, f, indent=2)
+
+
+def gaussian_taps(sigma):
+    """calcGaussianWeight (src/3D/DoG3DFilter.cu:372-392) -> (taps[80] float32, radius)."""
+    taps = np.zeros(80, np.float32)
+    r = ctypes.c_int()
+    check(lib().hdog_gaussian_taps(ctypes.c_float(sigma), taps.ctypes.data, ctypes.byref(r)))
+    return taps, r.value
+
+
+def depth_margin(p):
+    m = ctypes.c_int()
+    check(lib().hdog_depth_margin(ctypes.byref(p), ctypes.byref(m)))
+    return m.value
+
+
+def substack_schedule(length, depth, margin):
+    """z0 of each substack (src/3D/HDoG3D_main.cpp:309-314)."""
+    if length - margin <= 0:
+        return []
+    stride = depth - 2 * margin
+    if stride <= 0:
+        raise HDoGError(HDOG_ERR_PARAM, "depth must exceed twice the depth margin")
+    return list(range(0, length - margin, stride))
+
+
+def run_param_file(path, verbose=False):
+    """The HDoG3D_main executable as a call (src/3D/HDoG3D_main.cpp:260-319)."""
+    check(lib().hdog_run_param_file(os.fsencode(path), int(bool(verbose))))
+
+
+# ---------------------------------------------------------------- device context
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def _stream(stream):
+    import torch
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+class Context:
+    """Device scratch for up to `max_substacks` substacks of width x height x depth.
+
+    Stage methods take and return torch CUDA tensors shaped (depth, height, width),
+    x fastest, as the reference's device buffers."""
+
+    def __init__(self, params, max_substacks=1):
+        self.params = params
+        h = ctypes.c_void_p()
+        check(lib().hdog_ctx_create(ctypes.byref(params), int(max_substacks), ctypes.byref(h)))
+        self._h = h
+        self.max_substacks = max_substacks
+
+    def close(self):
+        if self._h:
+            lib().hdog_ctx_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def shape(self):
+        p = self.params
+        return (p.depth, p.height, p.width)
+
+    def _empty(self, dtype):
+        import torch
+        return torch.empty(self.shape, dtype=dtype, device="cuda:%d" % self.params.dev_id)
+
+    # Normalize3DFilter (src/3D/NormalizeFilter.cu:603-654)
+    def normalize(self, img, out=None, stream=None):
+        import torch
+        assert img.dtype == torch.uint16 and img.is_cuda and img.is_contiguous()
+        out = self._empty(torch.float32) if out is None else out
+        check(lib().hdog_normalize(self._h, _ptr(img), _ptr(out), _stream(stream)))
+        return out
+
+    # DoG3DFilter (src/3D/DoG3DFilter.cu:431-437)
+    def dog(self, norm, out=None, stream=None):
+        import torch
+        out = self._empty(torch.float32) if out is None else out
+        check(lib().hdog_dog(self._h, _ptr(norm), _ptr(out), _stream(stream)))
+        return out
+
+    # HessianPositiveDefiniteWithElement (src/3D/Hessian3DFilter_element.cu:355-388)
+    def hessian_pd(self, dog, want_hessian=False, stream=None):
+        import torch
+        mask = self._empty(torch.uint8)
+        hess = None
+        if want_hessian:
+            hess = torch.empty((6,) + self.shape, dtype=torch.float32, device=dog.device)
+        check(lib().hdog_hessian_pd(self._h, _ptr(dog), _ptr(mask), _ptr(hess) if hess is not None else None,
+                                    _stream(stream)))
+        return mask, hess
+
+    # CCL (src/3D/CCL3D.cu:81-117)
+    def ccl(self, mask, stream=None):
+        import torch
+        labels = self._empty(torch.int32)
+        check(lib().hdog_ccl(self._h, _ptr(mask), _ptr(labels), _stream(stream)))
+        return labels
+
+    # HessianFeatures + Eigenvalues + MaxNormalized/SumNormalized + RegionalSizeAndCentroid
+    def regional_features(self, labels, norm, dog, stream=None):
+        """Per-region arrays (region 0 = background), ordered by label, as numpy."""
+        r = hdog_regions()
+        check(lib().hdog_regional_features(self._h, _ptr(labels), _ptr(norm), _ptr(dog), ctypes.byref(r),
+                                           _stream(stream)))
+        n = int(r.num_regions)
+        cap = self._slots_stride()
+
+        def fetch(ptr, dtype, rows=1):
+            out = np.empty((rows, n), dtype)
+            for k in range(rows):
+                src = ptr + k * cap * np.dtype(dtype).itemsize
+                check(lib().hdog_memcpy(out[k].ctypes.data, ctypes.c_void_p(src), n * np.dtype(dtype).itemsize, None))
+            return out if rows > 1 else out[0]
+
+        return {
+            "num_regions": n,
+            "label": fetch(r.label, np.int32),
+            "count": fetch(r.count, np.uint32),
+            "intensity": fetch(r.intensity, np.float32),
+            "centroid": fetch(r.centroid, np.float32, 3),
+            "hessian": fetch(r.hessian, np.float32, 6),
+            "eigen": fetch(r.eigen, np.float32, 2),
+        }
+
+    def _slots_stride(self):
+        p = self.params
+        reg_cap = ((p.width + 1) // 2) * ((p.height + 1) // 2) * ((p.depth + 1) // 2) + 1
+        return reg_cap * self.max_substacks
+
+    # Erosion3DFilter (src/3D/Erosion3DFilter.cu:260-268)
+    def erosion(self, src, radius_xy, radius_z, stream=None):
+        import torch
+        out = self._empty(torch.uint16)
+        check(lib().hdog_erosion(self._h, _ptr(src), _ptr(out), int(radius_xy), int(radius_z), _stream(stream)))
+        return out
+
+    # processSubstack + saveFeatureVector
+    def run_substack(self, img, depth_valid, z0, cap=None, stream=None):
+        """img: host numpy uint16 (depth_valid, H, W) or a CUDA tensor; -> dt_local records."""
+        on_dev, ptr = _buffer(img)
+        cap = cap if cap is not None else 1 << 20
+        out = np.empty(cap, DT_LOCAL)
+        n = ctypes.c_int64()
+        rc = lib().hdog_run_substack(self._h, ptr, on_dev, int(depth_valid), int(z0), out.ctypes.data, cap,
+                                     ctypes.byref(n), _stream(stream) if on_dev else None)
+        if rc == HDOG_ERR_CAPACITY:
+            return self.run_substack(img, depth_valid, z0, cap=int(n.value), stream=stream)
+        check(rc)
+        return out[: n.value].copy()
+
+    def run_stack(self, stack, cap=None, stream=None):
+        """All substacks of one stack (length, H, W) in the reference's schedule."""
+        on_dev, ptr = _buffer(stack)
+        length = int(stack.shape[0])
+        cap = cap if cap is not None else 1 << 20
+        out = np.empty(cap, DT_LOCAL)
+        n = ctypes.c_int64()
+        rc = lib().hdog_run_stack(self._h, ptr, on_dev, length, out.ctypes.data, cap, ctypes.byref(n),
+                                  _stream(stream) if on_dev else None)
+        if rc == HDOG_ERR_CAPACITY:
+            return self.run_stack(stack, cap=int(n.value), stream=stream)
+        check(rc)
+        return out[: n.value].copy()
+
+
+def _buffer(a):
+    if isinstance(a, np.ndarray):
+        assert a.dtype == np.uint16 and a.flags["C_CONTIGUOUS"]
+        return 0, ctypes.c_void_p(a.ctypes.data)
+    assert a.is_cuda and a.is_contiguous()
+    return 1, ctypes.c_void_p(a.data_ptr())
+
+
+from . import synth  # noqa: E402,F401

@@ -1,0 +1,152 @@
+/*
+ * hdog.h -- C ABI of the GB300 HDoG cell-candidate detection library (libhdog.so).
+ *
+ * Drop-in for the HDoG hot path of CUBIC-informatics (src/3D).  Plain C types only:
+ * device buffers are `void *`/typed pointers, CUDA streams are passed as `void *`
+ * (a cudaStream_t; NULL = the legacy default stream).  Every function returns an
+ * HDOG_* status; none calls exit() (the reference exits through helper_cuda.h:595-612
+ * and utils.h:97-100).  hdog_last_error() gives the message of the last failure on the
+ * calling thread.
+ *
+ * Reference interfaces replaced (file:line within the reference project):
+ *   hdog_run_param_file     HDoG3D_main executable           src/3D/HDoG3D_main.cpp:260-319
+ *   hdog_params_load_json   loadParamFile                    src/3D/utils.h:95-157
+ *   hdog_gaussian_taps      calcGaussianWeight               src/3D/DoG3DFilter.cu:372-392
+ *   hdog_depth_margin       initGaussian3DKernel + margin    src/3D/DoG3DFilter.cu:394-415,
+ *                                                            src/3D/HDoG3D_main.cpp:280-284
+ *   hdog_normalize          Normalize3DFilter                src/3D/NormalizeFilter.cu:603-654
+ *   hdog_dog                DoG3DFilter                      src/3D/DoG3DFilter.cu:431-437
+ *   hdog_hessian_pd         HessianPositiveDefiniteWithElement
+ *                                                            src/3D/Hessian3DFilter_element.cu:355-388
+ *   hdog_ccl                CCL                              src/3D/CCL3D.cu:81-117
+ *   hdog_regional_features  HessianFeatures + Eigenvalues + MaxNormalized / SumNormalized +
+ *                           RegionalSizeAndCentroid          src/3D/RegionalFeatures.cu:65-87,
+ *                                                            114-137,214-255,295-329;
+ *                                                            src/3D/Eigenvalues.cu:99-112
+ *   hdog_erosion            Erosion3DFilter                  src/3D/Erosion3DFilter.cu:260-268
+ *   hdog_run_substack       processSubstack + saveFeatureVector
+ *                                                            src/3D/HDoG3D_main.cpp:134-257,
+ *                                                            src/3D/utils.h:204-250
+ *   hdog_run_stack          the substack loop of main        src/3D/HDoG3D_main.cpp:294-315
+ */
+#ifndef HDOG_H
+#define HDOG_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HDOG_ABI_VERSION 1
+
+enum {
+  HDOG_OK = 0,
+  HDOG_ERR_ARG = 1,       /* null pointer, negative or inconsistent size */
+  HDOG_ERR_SHAPE = 2,     /* geometry or radius outside what the kernels support */
+  HDOG_ERR_CUDA = 3,      /* CUDA runtime error (message has the detail) */
+  HDOG_ERR_IO = 4,        /* file could not be opened, read or written */
+  HDOG_ERR_PARAM = 5,     /* parameter file malformed or missing a required key */
+  HDOG_ERR_CAPACITY = 6,  /* caller's output buffer (or region capacity) too small */
+  HDOG_ERR_TIMEOUT = 7,   /* a bounded device loop hit its iteration limit */
+  HDOG_ERR_NOMEM = 8
+};
+
+/* HDoG parameters, the keys HDoG3D_main reads (src/3D/utils.h:48-93). */
+typedef struct hdog_params {
+  int width, height;            /* input_image_info.width / height */
+  int depth;                    /* HDoG_param.depth: slices per substack */
+  int left_margin, right_margin, top_margin, bottom_margin;
+  int extra_depth_margin;       /* HDoG_param.extra_depth_margin */
+  int radius_norm_xy, radius_norm_z;   /* HDoG_param.radius_norm.{xy_large,z_large} */
+  int min_intensity;            /* HDoG_param.min_intensity (unsigned short) */
+  float gamma_n;                /* HDoG_param.gamma_n */
+  float sigma_xy_small, sigma_z_small, sigma_xy_large, sigma_z_large;  /* sigma_dog */
+  int min_size;                 /* HDoG_param.min_size (unsigned short) */
+  int is_ave_mode;              /* top-level is_ave_mode: intensity = sum instead of max */
+  int erosion_radius_xy, erosion_radius_z;  /* opt-in regional erosion of the input before
+                                               normalization; 0,0 = off, as the reference */
+  int dev_id;                   /* devID */
+} hdog_params;
+
+/* 28-byte candidate record == FeatureVector (src/3D/utils.h:188-197) == dt_local
+   (script/HalfBrainCells.py:11-15). */
+typedef struct hdog_record {
+  float centroid_x, centroid_y, centroid_z;
+  float structureness, blobness, intensity;
+  uint16_t size, padding;
+} hdog_record;
+
+/* Per-region results of hdog_regional_features: DEVICE arrays owned by the context, valid
+   until the next call on it.  Region 0 is the background; regions are ordered by label,
+   i.e. by the minimum linear voxel index of the component. */
+typedef struct hdog_regions {
+  int64_t num_regions;          /* background included */
+  const int32_t *label;         /* [num_regions] */
+  const uint32_t *count;        /* [num_regions] exact voxel count (records keep count & 0xFFFF) */
+  const float *intensity;       /* [num_regions] max (or sum, is_ave_mode) of normalized intensity */
+  const float *centroid;        /* [3][num_regions] x, y, z (sum / (float)(uint16)count) */
+  const float *hessian;         /* [6][num_regions] sums of xx, xy, xz, yy, yz, zz */
+  const float *eigen;           /* [2][num_regions] structureness, blobness */
+} hdog_regions;
+
+typedef struct hdog_ctx hdog_ctx;
+
+/* ---- errors, version ---- */
+const char *hdog_last_error(void);
+int hdog_abi_version(void);
+
+/* ---- parameters ---- */
+/* Fills *p from an HDoG parameter JSON file (loadParamFile semantics; '#' keys ignored). */
+int hdog_params_load_json(const char *path, hdog_params *p);
+/* Gaussian taps of calcGaussianWeight: taps[80], *radius = (int)(2*sigma + 0.5). */
+int hdog_gaussian_taps(float sigma, float *taps80, int *radius);
+/* depth_margin = radius of the large-z Gaussian + extra_depth_margin. */
+int hdog_depth_margin(const hdog_params *p, int *margin);
+
+/* ---- context: device scratch for up to max_substacks substacks of width x height x depth ---- */
+int hdog_ctx_create(const hdog_params *p, int max_substacks, hdog_ctx **out);
+int hdog_ctx_destroy(hdog_ctx *ctx);
+/* Device scratch bytes hdog_ctx_create allocates for these parameters. */
+int hdog_ctx_bytes(const hdog_params *p, int max_substacks, size_t *bytes);
+
+/* ---- stages (device pointers, one substack of width x height x depth, on `stream`) ---- */
+int hdog_normalize(hdog_ctx *ctx, const uint16_t *d_img, float *d_norm, void *stream);
+int hdog_dog(hdog_ctx *ctx, const float *d_norm, float *d_dog, void *stream);
+/* d_hessian may be NULL; when given it receives the six planes xx,xy,xz,yy,yz,zz (pitch N). */
+int hdog_hessian_pd(hdog_ctx *ctx, const float *d_dog, uint8_t *d_mask, float *d_hessian,
+                    void *stream);
+int hdog_ccl(hdog_ctx *ctx, const uint8_t *d_mask, int32_t *d_labels, void *stream);
+/* Synchronizes `stream` to read the region count. */
+int hdog_regional_features(hdog_ctx *ctx, const int32_t *d_labels, const float *d_norm,
+                           const float *d_dog, hdog_regions *out, void *stream);
+/* Regional erosion: min over a (2rxy+1)^2 (2rz+1) box with a zero border, x -> y -> z. */
+int hdog_erosion(hdog_ctx *ctx, const uint16_t *d_src, uint16_t *d_dst, int radius_xy,
+                 int radius_z, void *stream);
+
+/* ---- whole chain ---- */
+/* One substack: img holds depth_valid slices (host memory, or device memory when
+   img_on_device != 0); slices depth_valid..depth-1 are taken as zero.  Records of
+   regions that pass the margin/size/intensity filter go to out (host), at most cap of
+   them; *n_records receives the number kept (HDOG_ERR_CAPACITY when it exceeds cap). */
+int hdog_run_substack(hdog_ctx *ctx, const uint16_t *img, int img_on_device, int depth_valid,
+                      int z0, hdog_record *out, int64_t cap, int64_t *n_records, void *stream);
+/* One stack of `length` slices: the overlapping substack schedule of HDoG3D_main
+   (z0 = 0, D-2m, ... while z0 < length - m), the substacks run as one batch when the
+   context has room, records appended in substack order. */
+int hdog_run_stack(hdog_ctx *ctx, const uint16_t *stack, int stack_on_device, int length,
+                   hdog_record *out, int64_t cap, int64_t *n_records, void *stream);
+/* The HDoG3D_main executable as a call: reads the parameter file, processes every stack,
+   writes each dst_path (removed first, then appended per substack). */
+int hdog_run_param_file(const char *param_path, int verbose);
+
+/* ---- small helpers for bindings without a CUDA runtime of their own ---- */
+int hdog_memcpy(void *dst, const void *src, size_t bytes, void *stream);  /* cudaMemcpyDefault */
+int hdog_stream_sync(void *stream);
+int hdog_device_alloc(void **ptr, size_t bytes);
+int hdog_device_free(void *ptr);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

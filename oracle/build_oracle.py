@@ -1,0 +1,65 @@
+"""TEST INFRASTRUCTURE: builds the checker, never the product.
+
+1. oracle/_build/liboracle.so from hdog_oracle.c (the CPU restatement), with
+   -ffp-contract=off so no host compiler adds contractions of its own.
+2. oracle/_ref/*.cubin: the reference's own CUDA kernels (CUBIC-informatics src/3D),
+   compiled unmodified for sm_103a straight from where they lie under the read-only
+   reference checkout, when that checkout is present.  Only device code is built; the
+   launcher in oracle/ref_cubin.py restates the reference's host-side launch geometry
+   and drives the kernels through the CUDA driver API on a GPU host.
+"""
+import os
+import platform
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+REF_OUT = os.path.join(HERE, "_ref")
+LIB = os.path.join(BUILD, "liboracle.so")
+REFERENCE = "/root/reference"
+REF_KERNEL_FILES = ["NormalizeFilter", "DoG3DFilter", "Hessian3DFilter_element", "CCL3D", "Eigenvalues",
+                    "Erosion3DFilter"]
+
+
+def _stale(t, deps):
+    return not os.path.exists(t) or any(os.path.getmtime(d) > os.path.getmtime(t) for d in deps)
+
+
+def build_oracle():
+    os.makedirs(BUILD, exist_ok=True)
+    src = os.path.join(HERE, "hdog_oracle.c")
+    hdr = os.path.join(HERE, "hdog_oracle.h")
+    if _stale(LIB, [src, hdr]):
+        flags = ["-O3", "-std=c11", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-fPIC", "-shared"]
+        if platform.machine() in ("x86_64", "AMD64"):
+            flags.append("-mfma")   # hardware fmaf; results are IEEE fma either way
+        subprocess.run(["gcc"] + flags + ["-o", LIB, src, "-lm"], check=True)
+    return LIB
+
+
+def build_reference_cubins():
+    """Returns the list of cubins built, [] when the reference checkout is absent."""
+    src_dir = os.path.join(REFERENCE, "src", "3D")
+    if not os.path.isdir(src_dir):
+        return []
+    os.makedirs(REF_OUT, exist_ok=True)
+    inc = ["-I" + os.path.join(REFERENCE, "deps", "cuda-samples", "Common"), "-I" + src_dir]
+    out = []
+    procs = []
+    for name in REF_KERNEL_FILES:
+        src = os.path.join(src_dir, name + ".cu")
+        dst = os.path.join(REF_OUT, name + ".cubin")
+        out.append(dst)
+        if _stale(dst, [src]):
+            procs.append(subprocess.Popen(["nvcc", "-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-O3",
+                                           "-w"] + inc + [src, "-o", dst]))
+    for p in procs:
+        if p.wait() != 0:
+            raise RuntimeError("reference cubin build failed")
+    return out
+
+
+if __name__ == "__main__":
+    print(build_oracle())
+    print(build_reference_cubins())

@@ -1,0 +1,124 @@
+"""Whole-chain parity: candidate records of the GPU path against the oracle.
+
+Exact fields: centroid x/y/z, intensity (max mode), size, padding, record count and
+order.  structureness / blobness come from region Hessian sums whose summation order
+differs (double accumulation here, the reference's CUB order there): they are checked
+within a relative tolerance stated below, against the oracle's sequential float sums.
+"""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+import torch
+
+import hdog
+from helpers import params, volume, padded
+from oracle import oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+EIGEN_RTOL = 1e-4      # structureness / blobness vs the float-sum oracle
+
+
+def assert_records_match(got, ref, what, sum_intensity=False):
+    assert len(got) == len(ref), "%s: %d records vs %d" % (what, len(got), len(ref))
+    if len(ref) == 0:
+        return
+    exact = ["local_x", "local_y", "local_z", "size", "padding"] + ([] if sum_intensity else ["intensity"])
+    for f in exact:
+        a, b = got[f], ref[f]
+        if a.dtype == np.float32:
+            a, b = a.view(np.uint32), b.view(np.uint32)
+        bad = np.count_nonzero(a != b)
+        assert bad == 0, "%s: field %s differs in %d records" % (what, f, bad)
+    tol_fields = ["structureness", "blobness"] + (["intensity"] if sum_intensity else [])
+    for f in tol_fields:
+        a = got[f].astype(np.float64)
+        b = ref[f].astype(np.float64)
+        fin = np.isfinite(b)
+        assert np.array_equal(np.isfinite(a), fin), (what, f)
+        rel = np.abs(a[fin] - b[fin]) / np.maximum(np.abs(b[fin]), 1e-30)
+        assert rel.max(initial=0) <= EIGEN_RTOL, (what, f, float(rel.max()))
+
+
+@pytest.mark.parametrize("depth_valid", [32, 21])
+def test_run_substack_matches_oracle(depth_valid):
+    W, H, D = 256, 192, 32
+    vol = volume(W, H, D, n_nuclei=160)
+    p = params(W, H, D, margins=10)
+    sub = padded(vol, D, depth_valid)
+    with hdog.Context(p) as ctx:
+        got = ctx.run_substack(np.ascontiguousarray(vol[:depth_valid]), depth_valid, 40)
+    ref = orc.substack(orc.params_from(p), sub, depth_valid, 40)[0]
+    assert len(ref) > 20
+    assert_records_match(got, ref, "substack dv=%d" % depth_valid)
+
+
+def test_run_substack_device_input_and_ave_mode():
+    W, H, D = 160, 128, 16
+    vol = volume(W, H, D, n_nuclei=60)
+    p = params(W, H, D, is_ave_mode=1, sigma_z_large=1.6, extra_depth_margin=1)
+    with hdog.Context(p) as ctx:
+        got = ctx.run_substack(torch.from_numpy(vol).cuda(), D, 0)
+    ref = orc.substack(orc.params_from(p), vol, D, 0)[0]
+    assert_records_match(got, ref, "ave mode", sum_intensity=True)
+
+
+@pytest.mark.parametrize("max_sub", [1, 4])
+def test_run_stack_matches_substack_loop(max_sub):
+    W, H, L, D = 192, 160, 100, 32
+    vol = volume(W, H, L, n_nuclei=250, seed=99)
+    p = params(W, H, D, margins=5)
+    with hdog.Context(p, max_substacks=max_sub) as ctx:
+        got = ctx.run_stack(vol)
+        got_dev = ctx.run_stack(torch.from_numpy(vol).cuda())
+    ref = orc.stack(orc.params_from(p), vol)
+    assert len(ref) > 50
+    assert_records_match(got, ref, "stack")
+    assert got.tobytes() == got_dev.tobytes()
+
+
+def test_hdog_main_executable_writes_reference_records(tmp_path):
+    W, H, L, D = 128, 96, 40, 32
+    vol = volume(W, H, L, n_nuclei=60, seed=7)
+    p = params(W, H, D, margins=3)
+    src = []
+    for z in range(L):
+        f = tmp_path / ("%06d.bin" % z)
+        vol[z].tofile(f)
+        src.append(str(f))
+    dst = tmp_path / "out" / "100000_200000.bin"
+    dst.parent.mkdir()
+    dst.write_bytes(b"stale")        # removed before the first substack is appended
+    pf = tmp_path / "param_gpu00.json"
+    hdog.write_param_file(str(pf), p, [(str(dst), src)])
+    r = subprocess.run([hdog.MAIN_PATH, str(pf)], stdout=subprocess.PIPE, stderr=subprocess.PIPE)
+    assert r.returncode == 0, r.stderr.decode()
+    got = np.fromfile(dst, dtype=hdog.DT_LOCAL)
+    ref = orc.stack(orc.params_from(p), vol)
+    assert_records_match(got, ref, "hdog_main")
+
+
+def test_erosion_opt_in_pipeline():
+    W, H, D = 128, 128, 16
+    vol = volume(W, H, D, n_nuclei=40, seed=5)
+    p = params(W, H, D, erosion_radius_xy=1, erosion_radius_z=1, sigma_z_large=1.6, extra_depth_margin=1)
+    with hdog.Context(p) as ctx:
+        got = ctx.run_substack(vol, D, 0)
+    ref = orc.substack(orc.params_from(p), orc.erosion(vol, 1, 1), D, 0)[0]
+    assert_records_match(got, ref, "eroded input")
+
+
+def test_capacity_error_is_reported():
+    W, H, D = 128, 128, 16
+    vol = volume(W, H, D, n_nuclei=40, seed=5)
+    p = params(W, H, D, sigma_z_large=1.6, extra_depth_margin=1)
+    with hdog.Context(p) as ctx:
+        n = len(ctx.run_substack(vol, D, 0))
+        assert n > 2
+        out = np.empty(1, hdog.DT_LOCAL)
+        cnt = __import__("ctypes").c_int64()
+        rc = hdog.lib().hdog_run_substack(ctx._h, vol.ctypes.data, 0, D, 0, out.ctypes.data, 1,
+                                          __import__("ctypes").byref(cnt), None)
+        assert rc == hdog.HDOG_ERR_CAPACITY and cnt.value == n
