@@ -37,8 +37,22 @@ def _run(cmd):
     return r.stdout
 
 
+def _arch_guard():
+    """Drops build products made on another host architecture (the tree is shared
+    between an x86-64 build host and aarch64 GPU hosts)."""
+    stamp = os.path.join(OUT, "ARCH")
+    here = platform.machine()
+    if os.path.exists(stamp) and open(stamp).read().strip() == here:
+        return
+    for f in os.listdir(OUT):
+        os.remove(os.path.join(OUT, f))
+    with open(stamp, "w") as fh:
+        fh.write(here + "\n")
+
+
 def build(verbose=False):
     os.makedirs(OUT, exist_ok=True)
+    _arch_guard()
     hdrs = [h if os.path.isabs(h) else os.path.join(CSRC, h) for h in HEADERS]
     objs = []
     jobs = []

@@ -28,6 +28,12 @@ def _stale(t, deps):
 
 def build_oracle():
     os.makedirs(BUILD, exist_ok=True)
+    stamp = os.path.join(BUILD, "ARCH")
+    if not os.path.exists(stamp) or open(stamp).read().strip() != platform.machine():
+        if os.path.exists(LIB):
+            os.remove(LIB)
+        with open(stamp, "w") as fh:
+            fh.write(platform.machine() + "\n")
     src = os.path.join(HERE, "hdog_oracle.c")
     hdr = os.path.join(HERE, "hdog_oracle.h")
     if _stale(LIB, [src, hdr]):
