@@ -1,0 +1,55 @@
+"""The CPU oracle replayed against digests of the reference's own kernels.
+
+tests/golden/ref_stages.json was written by oracle/ref_golden.py on a GB300, running
+the reference's src/3D kernels (compiled unmodified for sm_103a) on seeded synthetic
+volumes.  Here the oracle recomputes each case from the same seed and must reproduce
+every stage digest bit for bit: normalized volume, DoG, the six Hessian planes, the
+negative-definite mask and the CCL labels; and the erosion operator.
+"""
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+from hdog import synth
+from oracle import oracle as orc
+
+GOLDEN = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "ref_stages.json")))
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def case_volume(c):
+    return synth.volume(synth.spec(c["W"], c["H"], c["D"], c["n_nuclei"], c["seed"], **c["synth"]))
+
+
+@pytest.mark.parametrize("case", GOLDEN["cases"], ids=[c["name"] for c in GOLDEN["cases"]])
+def test_oracle_reproduces_reference_digests(case):
+    vol = case_volume(case)
+    assert sha(vol) == case["sha256_input"], "synthetic generator drifted"
+    sx1, sz1, sx2, sz2 = case["sigma"]
+    rxy, rz = case["radius_norm"]
+    norm = orc.normalize(vol, rxy, rz, case["min_intensity"])
+    assert sha(norm) == case["sha256"]["norm"]
+    dog = orc.dog(norm, sx1, sz1, sx2, sz2, case["gamma"])
+    assert sha(dog) == case["sha256"]["dog"]
+    mask, hess = orc.hessian_pd(dog, want_hessian=True)
+    assert sha(hess) == case["sha256"]["hessian"]
+    assert sha(mask) == case["sha256"]["pd"]
+    labels, n = orc.ccl(mask)
+    assert sha(labels) == case["sha256"]["labels"]
+    assert n == case["num_regions"]
+    # and on the GPU host the oracle matched the reference with zero differing values
+    assert all(v == 0 for v in case["oracle_mismatch"].values()), case["oracle_mismatch"]
+    assert case["eigen_bit_mismatch"] == {"structureness": 0, "blobness": 0}
+
+
+def test_oracle_erosion_reproduces_reference_digest():
+    e = GOLDEN["erosion"]
+    c = [c for c in GOLDEN["cases"] if c["name"] == e["case"]][0]
+    out = orc.erosion(case_volume(c), *e["radius"])
+    assert sha(out) == e["sha256"] and e["oracle_mismatch"] == 0
