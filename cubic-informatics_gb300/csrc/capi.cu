@@ -20,6 +20,66 @@
 
 using namespace hdog;
 
+namespace hdog {
+thread_local KernelTimer *g_timer = nullptr;
+}
+
+// Per-kernel CUDA-event timing of a context (hdog_timing_enable / hdog_timing_read).
+struct EventTimer : KernelTimer {
+  struct Rec {
+    const char *name;
+    cudaEvent_t a, b;
+  };
+  std::vector<cudaEvent_t> pool;
+  std::vector<Rec> pending;
+  struct Acc {
+    int64_t count = 0;
+    double ms = 0.0;
+  };
+  std::vector<std::pair<std::string, Acc>> totals;
+  cudaEvent_t get() {
+    if (!pool.empty()) {
+      cudaEvent_t e = pool.back();
+      pool.pop_back();
+      return e;
+    }
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    return e;
+  }
+  void begin(const char *name, cudaStream_t s) override {
+    Rec r{name, get(), get()};
+    cudaEventRecord(r.a, s);
+    pending.push_back(r);
+  }
+  void end(cudaStream_t s) override {
+    if (!pending.empty()) cudaEventRecord(pending.back().b, s);
+  }
+  void collect() {
+    for (Rec &r : pending) {
+      cudaEventSynchronize(r.b);
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, r.a, r.b);
+      Acc *acc = nullptr;
+      for (auto &t : totals)
+        if (t.first == r.name) acc = &t.second;
+      if (!acc) {
+        totals.emplace_back(r.name, Acc());
+        acc = &totals.back().second;
+      }
+      acc->count++;
+      acc->ms += ms;
+      pool.push_back(r.a);
+      pool.push_back(r.b);
+    }
+    pending.clear();
+  }
+  ~EventTimer() override {
+    for (Rec &r : pending) { pool.push_back(r.a); pool.push_back(r.b); }
+    for (cudaEvent_t e : pool) cudaEventDestroy(e);
+  }
+};
+
 // ------------------------------------------------------------------ errors
 static thread_local std::string g_last_error;
 
@@ -137,6 +197,13 @@ struct hdog_ctx {
   // device copy of a whole stack for hdog_run_stack with host input
   uint16_t *stack_buf = nullptr;
   size_t stack_bytes = 0;
+  EventTimer *timer = nullptr;
+};
+
+// Makes the context's kernel timer (if any) current on this thread for one API call.
+struct TimerScope {
+  explicit TimerScope(hdog_ctx *c) { g_timer = c->timer; }
+  ~TimerScope() { g_timer = nullptr; }
 };
 
 static size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
@@ -216,6 +283,7 @@ extern "C" int hdog_ctx_destroy(hdog_ctx *ctx) {
   if (ctx->arena) cudaFree(ctx->arena);
   if (ctx->stack_buf) cudaFree(ctx->stack_buf);
   if (ctx->h_subs) cudaFreeHost(ctx->h_subs);
+  delete ctx->timer;
   delete ctx;
   return HDOG_OK;
 }
@@ -427,6 +495,7 @@ static int single_sub(hdog_ctx *c, const uint16_t *src, cudaStream_t st) {
 #define CTX_GUARD(c)                                                   \
   if (!(c)) return fail(HDOG_ERR_ARG, "null context");                 \
   std::lock_guard<std::mutex> lock__((c)->mu);                         \
+  TimerScope timer_scope__(c);                                         \
   HDOG_CUDA_TRY(cudaSetDevice((c)->dev))
 
 extern "C" int hdog_normalize(hdog_ctx *c, const uint16_t *d_img, float *d_norm, void *stream) {
@@ -760,6 +829,37 @@ extern "C" int hdog_run_param_file(const char *param_path, int verbose) {
   if (h_stack) cudaFreeHost(h_stack);
   hdog_ctx_destroy(ctx);
   return rc;
+}
+
+// ------------------------------------------------------------------ timing
+extern "C" int hdog_timing_enable(hdog_ctx *c, int on) {
+  if (!c) return fail(HDOG_ERR_ARG, "null context");
+  std::lock_guard<std::mutex> lock(c->mu);
+  if (on && !c->timer) c->timer = new EventTimer();
+  if (!on && c->timer) {
+    delete c->timer;
+    c->timer = nullptr;
+  }
+  return HDOG_OK;
+}
+
+extern "C" int hdog_timing_read(hdog_ctx *c, char *buf, size_t cap) {
+  if (!c || !buf || cap == 0) return fail(HDOG_ERR_ARG, "hdog_timing_read: bad argument");
+  std::lock_guard<std::mutex> lock(c->mu);
+  buf[0] = 0;
+  if (!c->timer) return HDOG_OK;
+  cudaSetDevice(c->dev);
+  c->timer->collect();
+  std::string out;
+  for (auto &t : c->timer->totals) {
+    char line[256];
+    snprintf(line, sizeof(line), "%s %lld %.6f\n", t.first.c_str(), (long long)t.second.count, t.second.ms);
+    out += line;
+  }
+  c->timer->totals.clear();
+  if (out.size() + 1 > cap) return fail(HDOG_ERR_CAPACITY, "timing buffer too small");
+  memcpy(buf, out.c_str(), out.size() + 1);
+  return HDOG_OK;
 }
 
 // ------------------------------------------------------------------ helpers

@@ -416,24 +416,24 @@ __global__ void __launch_bounds__(kFinalizeBlock) k_records(const Sub *subs, con
 void launch_scan(const ScanSeg &sg, int nsub, const uint32_t *in, uint32_t *out, uint32_t *chunk,
                  int64_t *totals, int64_t add, cudaStream_t s) {
   const unsigned nch = ceil_div(sg.max_len, 1024);
-  k_scan_p1<<<dim3(nch, nsub), 1024, 0, s>>>(sg.off, sg.len, sg.chk, in, chunk);
-  k_scan_p2<<<nsub, 1024, 0, s>>>(sg.len, sg.chk, chunk, totals, add);
-  k_scan_p3<<<dim3(nch, nsub), 1024, 0, s>>>(sg.off, sg.len, sg.chk, in, chunk, out);
+  KLAUNCH("k_scan_p1", s, (k_scan_p1<<<dim3(nch, nsub), 1024, 0, s>>>(sg.off, sg.len, sg.chk, in, chunk)));
+  KLAUNCH("k_scan_p2", s, (k_scan_p2<<<nsub, 1024, 0, s>>>(sg.len, sg.chk, chunk, totals, add)));
+  KLAUNCH("k_scan_p3", s, (k_scan_p3<<<dim3(nch, nsub), 1024, 0, s>>>(sg.off, sg.len, sg.chk, in, chunk, out)));
 }
 
 void launch_ccl(const Sub *d_subs, int nsub, int64_t max_n, const uint8_t *mask, int32_t *labels,
                 uint32_t *root_bits, uint32_t *blk_counts, int *d_status, cudaStream_t s) {
   const unsigned g256 = ceil_div(max_n, 256);
-  k_ccl_init<<<dim3(g256, nsub), 256, 0, s>>>(d_subs, mask, labels);
-  k_ccl_merge<<<dim3(g256, nsub), 256, 0, s>>>(d_subs, mask, labels, d_status);
-  k_ccl_flatten<<<dim3(ceil_div(max_n, kScanBlock), nsub), kScanBlock, 0, s>>>(d_subs, mask, labels, root_bits,
-                                                                              blk_counts, d_status);
+  KLAUNCH("k_ccl_init", s, (k_ccl_init<<<dim3(g256, nsub), 256, 0, s>>>(d_subs, mask, labels)));
+  KLAUNCH("k_ccl_merge", s, (k_ccl_merge<<<dim3(g256, nsub), 256, 0, s>>>(d_subs, mask, labels, d_status)));
+  KLAUNCH("k_ccl_flatten", s, (k_ccl_flatten<<<dim3(ceil_div(max_n, kScanBlock), nsub), kScanBlock, 0, s>>>(d_subs, mask, labels, root_bits,
+                                                                              blk_counts, d_status)));
 }
 
 void launch_roots_from_labels(const Sub *d_subs, int nsub, int64_t max_n, const int32_t *labels, uint8_t *mask,
                               uint32_t *root_bits, uint32_t *blk_counts, cudaStream_t s) {
-  k_roots_from_labels<<<dim3(ceil_div(max_n, kScanBlock), nsub), kScanBlock, 0, s>>>(d_subs, labels, mask, root_bits,
-                                                                                    blk_counts);
+  KLAUNCH("k_roots_from_labels", s, (k_roots_from_labels<<<dim3(ceil_div(max_n, kScanBlock), nsub), kScanBlock, 0, s>>>(d_subs, labels, mask, root_bits,
+                                                                                    blk_counts)));
 }
 
 void launch_regions(const Sub *d_subs, int nsub, int64_t max_n, const ScanSeg &vseg, const uint8_t *mask,
@@ -441,10 +441,10 @@ void launch_regions(const Sub *d_subs, int nsub, int64_t max_n, const ScanSeg &v
                     int32_t *rank, uint32_t *blk_counts, uint32_t *blk_offsets, uint32_t *chunk,
                     int64_t *d_num_regions, RegionAcc acc, int64_t slots, int *d_status, cudaStream_t s) {
   launch_scan(vseg, nsub, blk_counts, blk_offsets, chunk, d_num_regions, 1, s);
-  k_rank<<<dim3(ceil_div(max_n, kScanBlock), nsub), kScanBlock, 0, s>>>(d_subs, root_bits, blk_offsets, rank,
-                                                                        acc, slots, d_status);
-  k_accumulate<<<dim3(ceil_div(max_n, 256), nsub), 256, 0, s>>>(d_subs, mask, labels, rank, norm, dog, acc,
-                                                                slots);
+  KLAUNCH("k_rank", s, (k_rank<<<dim3(ceil_div(max_n, kScanBlock), nsub), kScanBlock, 0, s>>>(d_subs, root_bits, blk_offsets, rank,
+                                                                        acc, slots, d_status)));
+  KLAUNCH("k_accumulate", s, (k_accumulate<<<dim3(ceil_div(max_n, 256), nsub), 256, 0, s>>>(d_subs, mask, labels, rank, norm, dog, acc,
+                                                                slots)));
 }
 
 void launch_finalize(const Sub *d_subs, int nsub, int64_t max_reg_cap, const ScanSeg &rseg,
@@ -452,10 +452,10 @@ void launch_finalize(const Sub *d_subs, int nsub, int64_t max_reg_cap, const Sca
                      FilterParams fp, uint32_t *blk_counts, uint32_t *blk_offsets, uint32_t *chunk,
                      int64_t *d_num_records, hdog_record *records, cudaStream_t s) {
   const unsigned nb = ceil_div(max_reg_cap, kFinalizeBlock);
-  k_finalize<<<dim3(nb, nsub), kFinalizeBlock, 0, s>>>(d_subs, d_num_regions, acc, slots, out, fp, blk_counts);
+  KLAUNCH("k_finalize", s, (k_finalize<<<dim3(nb, nsub), kFinalizeBlock, 0, s>>>(d_subs, d_num_regions, acc, slots, out, fp, blk_counts)));
   launch_scan(rseg, nsub, blk_counts, blk_offsets, chunk, d_num_records, 0, s);
-  k_records<<<dim3(nb, nsub), kFinalizeBlock, 0, s>>>(d_subs, d_num_regions, out, acc.count, slots, blk_offsets,
-                                                      records);
+  KLAUNCH("k_records", s, (k_records<<<dim3(nb, nsub), kFinalizeBlock, 0, s>>>(d_subs, d_num_regions, out, acc.count, slots, blk_offsets,
+                                                      records)));
 }
 
 }  // namespace hdog

@@ -121,7 +121,32 @@ struct DogTaps {
   float normalizer;
 };
 
+// Optional per-kernel timing: when a context enables it, each kernel launch is
+// bracketed by CUDA events recorded on the launching stream.
+struct KernelTimer {
+  virtual void begin(const char *name, cudaStream_t s) = 0;
+  virtual void end(cudaStream_t s) = 0;
+  virtual ~KernelTimer() {}
+};
+extern thread_local KernelTimer *g_timer;
+
 }  // namespace hdog
+
+#define KT_BEGIN(name, s)                            \
+  do {                                               \
+    if (::hdog::g_timer) ::hdog::g_timer->begin(name, s); \
+  } while (0)
+#define KT_END(s)                                    \
+  do {                                               \
+    if (::hdog::g_timer) ::hdog::g_timer->end(s);    \
+  } while (0)
+// Launch `kernel<<<args>>>(...)` between timing events named after the kernel.
+#define KLAUNCH(name, s, launch) \
+  do {                           \
+    KT_BEGIN(name, s);           \
+    launch;                      \
+    KT_END(s);                   \
+  } while (0)
 
 #define HDOG_CUDA_TRY(expr)                                 \
   do {                                                      \

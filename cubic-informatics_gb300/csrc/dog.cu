@@ -199,11 +199,11 @@ void launch_dog(const Sub *d_subs, int nsub, int max_w, int max_h, int max_d, in
                 const DogTaps &T, const float *norm, float2 *t0, float2 *t1, float *dog, cudaStream_t s) {
   const int rm = max(T.r[0], T.r[2]);
   size_t smx = (size_t)(kConvSeg + 2 * rm) * sizeof(float);
-  k_conv_x<<<dim3((unsigned)(max_rows * ceil_div(max_w, kConvSeg)), nsub), kConvSeg, smx, s>>>(d_subs, T, norm, t0);
+  KLAUNCH("k_conv_x", s, (k_conv_x<<<dim3((unsigned)(max_rows * ceil_div(max_w, kConvSeg)), nsub), kConvSeg, smx, s>>>(d_subs, T, norm, t0)));
   const int by = 4;
-  k_conv_y<<<dim3((unsigned)((int64_t)ceil_div(max_w, 32) * ceil_div(max_h, by * kConvK) * max_d), nsub),
-             dim3(32, by), 0, s>>>(d_subs, T, t0, t1);
-  k_conv_z_dog<<<dim3(ceil_div((int64_t)max_w * max_h, 128), nsub), 128, 0, s>>>(d_subs, T, t1, dog);
+  KLAUNCH("k_conv_y", s, (k_conv_y<<<dim3((unsigned)((int64_t)ceil_div(max_w, 32) * ceil_div(max_h, by * kConvK) * max_d), nsub),
+             dim3(32, by), 0, s>>>(d_subs, T, t0, t1)));
+  KLAUNCH("k_conv_z_dog", s, (k_conv_z_dog<<<dim3(ceil_div((int64_t)max_w * max_h, 128), nsub), 128, 0, s>>>(d_subs, T, t1, dog)));
 }
 
 void launch_hessian_pd(const Sub *d_subs, int nsub, int max_w, int max_h, int max_d, const float *dog,
@@ -211,7 +211,7 @@ void launch_hessian_pd(const Sub *d_subs, int nsub, int max_w, int max_h, int ma
   const size_t smem = (size_t)(kDZ * kDY * kDX + 3 * kGZ * kGY * kGX) * sizeof(float);
   cudaFuncSetAttribute(k_hessian_pd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   const int64_t tiles = (int64_t)ceil_div(max_w, kHX) * ceil_div(max_h, kHY) * ceil_div(max_d, kHZ);
-  k_hessian_pd<<<dim3((unsigned)tiles, nsub), dim3(kHX, kHY), smem, s>>>(d_subs, dog, mask, hess6);
+  KLAUNCH("k_hessian_pd", s, (k_hessian_pd<<<dim3((unsigned)tiles, nsub), dim3(kHX, kHY), smem, s>>>(d_subs, dog, mask, hess6)));
 }
 
 }  // namespace hdog

@@ -318,14 +318,14 @@ static size_t minmax_y_smem(int r) { return (size_t)2 * (kColTileY + 2 * r) * kC
 
 void launch_minmax_z(const Sub *d_subs, int nsub, int max_plane, int rz, uint32_t *mm, cudaStream_t s) {
   dim3 grid(ceil_div(max_plane, 256), nsub);
-  k_minmax_z<0><<<grid, 256, 0, s>>>(d_subs, rz, mm);
+  KLAUNCH("k_minmax_z", s, (k_minmax_z<0><<<grid, 256, 0, s>>>(d_subs, rz, mm)));
 }
 
 void launch_minmax_x(const Sub *d_subs, int nsub, int64_t max_rows, int max_w, int r,
                      const uint32_t *in, uint32_t *out, cudaStream_t s) {
   dim3 grid((unsigned)(max_rows * ceil_div(max_w, kRowSeg)), nsub);
   size_t smem = (size_t)2 * (kRowSeg + 2 * r) * sizeof(uint32_t);
-  k_minmax_x<0><<<grid, kRowSeg, smem, s>>>(d_subs, r, in, out);
+  KLAUNCH("k_minmax_x", s, (k_minmax_x<0><<<grid, kRowSeg, smem, s>>>(d_subs, r, in, out)));
 }
 
 void launch_minmax_y(const Sub *d_subs, int nsub, int max_w, int max_h, int max_d, int r,
@@ -333,7 +333,7 @@ void launch_minmax_y(const Sub *d_subs, int nsub, int max_w, int max_h, int max_
   dim3 grid((unsigned)((int64_t)ceil_div(max_w, kColTileX) * ceil_div(max_h, kColTileY) * max_d), nsub);
   size_t smem = minmax_y_smem(r);
   if (smem > 48 * 1024) cudaFuncSetAttribute(k_minmax_y<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  k_minmax_y<0><<<grid, dim3(kColTileX, 8), smem, s>>>(d_subs, r, in, out);
+  KLAUNCH("k_minmax_y", s, (k_minmax_y<0><<<grid, dim3(kColTileX, 8), smem, s>>>(d_subs, r, in, out)));
 }
 
 void launch_box_x(const Sub *d_subs, int nsub, int64_t max_rows, int max_w, int r,
@@ -341,26 +341,26 @@ void launch_box_x(const Sub *d_subs, int nsub, int64_t max_rows, int max_w, int 
   dim3 grid((unsigned)(max_rows * ceil_div(max_w, kRowSeg)), nsub);
   size_t smem = (size_t)(kRowSeg + 2 * r + 1) * sizeof(unsigned long long);
   if (smem > 48 * 1024) cudaFuncSetAttribute(k_box_x, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  k_box_x<<<grid, kRowSeg, smem, s>>>(d_subs, r, in, out);
+  KLAUNCH("k_box_x", s, (k_box_x<<<grid, kRowSeg, smem, s>>>(d_subs, r, in, out)));
 }
 
 void launch_box_y(const Sub *d_subs, int nsub, int max_w, int max_h, int max_d, int r,
                   const float2 *in, float2 *out, cudaStream_t s) {
   const int by = 4;
   dim3 grid((unsigned)((int64_t)ceil_div(max_w, 32) * ceil_div(max_h, by * kBoxK) * max_d), nsub);
-  k_box_y<<<grid, dim3(32, by), 0, s>>>(d_subs, r, in, out);
+  KLAUNCH("k_box_y", s, (k_box_y<<<grid, dim3(32, by), 0, s>>>(d_subs, r, in, out)));
 }
 
 void launch_box_z_norm(const Sub *d_subs, int nsub, int max_plane, int rz, float min_intensity,
                        const float2 *in, float *norm, cudaStream_t s) {
   dim3 grid(ceil_div(max_plane, 128), nsub);
-  k_box_z_norm<<<grid, 128, 0, s>>>(d_subs, rz, min_intensity, in, norm);
+  KLAUNCH("k_box_z_norm", s, (k_box_z_norm<<<grid, 128, 0, s>>>(d_subs, rz, min_intensity, in, norm)));
 }
 
 void launch_copy_norm(const Sub *d_subs, int nsub, int64_t max_n, float min_intensity, float *norm,
                       cudaStream_t s) {
   dim3 grid(ceil_div(max_n, 256), nsub);
-  k_copy_norm<<<grid, 256, 0, s>>>(d_subs, min_intensity, norm);
+  KLAUNCH("k_copy_norm", s, (k_copy_norm<<<grid, 256, 0, s>>>(d_subs, min_intensity, norm)));
 }
 
 // Erosion3DFilter: min with a zero border.  Min is separable and exact, so z -> x -> y
@@ -373,14 +373,14 @@ void launch_erosion(const Sub *d_subs, int nsub, int max_w, int max_h, int max_d
   const int64_t max_n = max_rows * max_w;
   uint32_t *b = a + max_n * nsub;
   const int max_plane = max_w * max_h;
-  k_minmax_z<1><<<dim3(ceil_div(max_plane, 256), nsub), 256, 0, s>>>(d_subs, rz, a);
+  KLAUNCH("k_minmax_z", s, (k_minmax_z<1><<<dim3(ceil_div(max_plane, 256), nsub), 256, 0, s>>>(d_subs, rz, a)));
   size_t smx = (size_t)2 * (kRowSeg + 2 * rxy) * sizeof(uint32_t);
-  k_minmax_x<1><<<dim3((unsigned)(max_rows * ceil_div(max_w, kRowSeg)), nsub), kRowSeg, smx, s>>>(d_subs, rxy, a, b);
+  KLAUNCH("k_minmax_x", s, (k_minmax_x<1><<<dim3((unsigned)(max_rows * ceil_div(max_w, kRowSeg)), nsub), kRowSeg, smx, s>>>(d_subs, rxy, a, b)));
   size_t smy = minmax_y_smem(rxy);
   if (smy > 48 * 1024) cudaFuncSetAttribute(k_minmax_y<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smy);
-  k_minmax_y<1><<<dim3((unsigned)((int64_t)ceil_div(max_w, kColTileX) * ceil_div(max_h, kColTileY) * max_d), nsub),
-                  dim3(kColTileX, 8), smy, s>>>(d_subs, rxy, b, a);
-  k_unpack_lo<<<dim3(ceil_div(max_n, 256), nsub), 256, 0, s>>>(d_subs, a, dst);
+  KLAUNCH("k_minmax_y", s, (k_minmax_y<1><<<dim3((unsigned)((int64_t)ceil_div(max_w, kColTileX) * ceil_div(max_h, kColTileY) * max_d), nsub),
+                  dim3(kColTileX, 8), smy, s>>>(d_subs, rxy, b, a)));
+  KLAUNCH("k_unpack_lo", s, (k_unpack_lo<<<dim3(ceil_div(max_n, 256), nsub), 256, 0, s>>>(d_subs, a, dst)));
 }
 
 }  // namespace hdog

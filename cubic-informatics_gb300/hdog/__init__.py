@@ -87,6 +87,8 @@ _SIGNATURES = {
     "hdog_run_stack": (ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.c_int, _P, ctypes.c_int64,
                                       ctypes.POINTER(ctypes.c_int64), _P]),
     "hdog_run_param_file": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int]),
+    "hdog_timing_enable": (ctypes.c_int, [_P, ctypes.c_int]),
+    "hdog_timing_read": (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_size_t]),
     "hdog_memcpy": (ctypes.c_int, [_P, _P, ctypes.c_size_t, _P]),
     "hdog_stream_sync": (ctypes.c_int, [_P]),
     "hdog_device_alloc": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.c_size_t]),
@@ -246,6 +248,20 @@ class Context:
     def _empty(self, dtype):
         import torch
         return torch.empty(self.shape, dtype=dtype, device="cuda:%d" % self.params.dev_id)
+
+    def timing(self, on=True):
+        """Per-kernel CUDA-event timing of this context's launches."""
+        check(lib().hdog_timing_enable(self._h, int(bool(on))))
+
+    def timing_read(self):
+        """{kernel: (launches, total_ms)} since the last read."""
+        buf = ctypes.create_string_buffer(1 << 16)
+        check(lib().hdog_timing_read(self._h, buf, len(buf)))
+        out = {}
+        for line in buf.value.decode().splitlines():
+            name, cnt, ms = line.split()
+            out[name] = (int(cnt), float(ms))
+        return out
 
     # Normalize3DFilter (src/3D/NormalizeFilter.cu:603-654)
     def normalize(self, img, out=None, stream=None):

@@ -140,6 +140,13 @@ int hdog_run_stack(hdog_ctx *ctx, const uint16_t *stack, int stack_on_device, in
    writes each dst_path (removed first, then appended per substack). */
 int hdog_run_param_file(const char *param_path, int verbose);
 
+/* ---- per-kernel timing (CUDA events on the launching stream) ---- */
+/* When on, every kernel launch of the context's calls is bracketed by two events. */
+int hdog_timing_enable(hdog_ctx *ctx, int on);
+/* Writes "kernel_name launches total_ms\n" lines accumulated since the last read
+   (waiting for the recorded events), then resets the accumulators. */
+int hdog_timing_read(hdog_ctx *ctx, char *buf, size_t cap);
+
 /* ---- small helpers for bindings without a CUDA runtime of their own ---- */
 int hdog_memcpy(void *dst, const void *src, size_t bytes, void *stream);  /* cudaMemcpyDefault */
 int hdog_stream_sync(void *stream);

@@ -300,36 +300,45 @@ void orc_dog(const float *norm, float *dog, int W, int H, int D, float sxy1, flo
 /* Sylvester test of PositiveDefiniteKernel, src/3D/Hessian3DFilter_element.cu:295-323:
      xx < 0 && xx*yy - xy*xy > 0 &&
      xx*yy*zz + 2*xy*yz*xz - xx*yz*yz - yy*xz*xz - zz*xy*xy < 0
-   pd_variant selects how the products and sums are rounded: bits 0-1 the 2x2 minor
-   (0 separate roundings, 1 fma(xx,yy,-xy*xy), 2 fma(-xy,xy,xx*yy)); bits 2-3 the
-   determinant (0 separate roundings, 1 A fused into the first add and C, D, E fused
-   as negated FMAs, 2 B fused into the first add, C, D, E fused). */
+   The expression leaves the compiler free to contract products into FMAs and to fold
+   `a - b > 0` into `a > b`; pd_variant names one combination so the form the
+   reference binary uses can be pinned against it.
+     bits 0-1, 2x2 minor:  0  both products rounded, then compared / subtracted
+                           1  fma(xx, yy, -(xy*xy))
+                           2  fma(-xy, xy, xx*yy)
+     bits 2-4, determinant, with A = (xx*yy)*zz, B = ((2*xy)*yz)*xz, C = (xx*yz)*yz,
+               D = (yy*xz)*xz, E = (zz*xy)*xy:
+                           0  every product rounded, (((A + B) - C) - D) - E < 0
+                           1  t = fma(xx*yy, zz, B); t = fma(-(xx*yz), yz, t);
+                              t = fma(-(yy*xz), xz, t); fma(-(zz*xy), xy, t) < 0
+                           2  as 1 with B fused first: t = fma((2*xy)*yz, xz, A)
+                           3  as 1, the last subtraction folded into the compare: t < E
+                           4  as 2, the last subtraction folded into the compare: t < E */
 int orc_pd_test(float xx, float xy, float xz, float yy, float yz, float zz, int v) {
   if (!(xx < 0)) return 0;
-  const int vm = v & 3, vd = (v >> 2) & 3;
-  float m2;
-  if (vm == 1) m2 = fmaf(xx, yy, -(xy * xy));
-  else if (vm == 2) m2 = fmaf(-xy, xy, xx * yy);
-  else { float a = xx * yy, b = xy * xy; m2 = a - b; }
-  if (!(m2 > 0)) return 0;
-  float det;
+  const int vm = v & 3, vd = (v >> 2) & 7;
+  if (vm == 1) {
+    if (!(fmaf(xx, yy, -(xy * xy)) > 0)) return 0;
+  } else if (vm == 2) {
+    if (!(fmaf(-xy, xy, xx * yy) > 0)) return 0;
+  } else {
+    const float a = xx * yy, b = xy * xy;
+    if (!(a - b > 0)) return 0;
+  }
   const float p = xx * yy;
   const float q = (2.0f * xy) * yz;
-  if (vd == 1 || vd == 2) {
-    float t;
-    if (vd == 1) t = fmaf(p, zz, q * xz);
-    else t = fmaf(q, xz, p * zz);
-    t = fmaf(-(xx * yz), yz, t);
-    t = fmaf(-(yy * xz), xz, t);
-    det = fmaf(-(zz * xy), xy, t);
-  } else {
+  if (vd == 0) {
     float A = p * zz, B = q * xz, C = (xx * yz) * yz, Dd = (yy * xz) * xz, E = (zz * xy) * xy;
     float s = A + B;
     s = s - C;
     s = s - Dd;
-    det = s - E;
+    return (s - E) < 0;
   }
-  return det < 0;
+  float t = (vd == 2 || vd == 4) ? fmaf(q, xz, p * zz) : fmaf(p, zz, q * xz);
+  t = fmaf(-(xx * yz), yz, t);
+  t = fmaf(-(yy * xz), xz, t);
+  if (vd == 3 || vd == 4) return t < (zz * xy) * xy;
+  return fmaf(-(zz * xy), xy, t) < 0;
 }
 
 void orc_pd_test_planes(const float *planes, int64_t n, int v, uint8_t *out) {

@@ -41,7 +41,7 @@ CASES = [
     dict(name="example_radii_1280x720x16", W=1280, H=720, D=16, n=1400, seed=SEED + 13, synth={},
          sigma=(4.0, 1.8, 6.0, 2.7), rxy=100, rz=5, min_intensity=50.0, gamma=1.0),
 ]
-PD_VARIANTS = [v + 4 * d for v in range(3) for d in range(3)]
+PD_VARIANTS = [v + 4 * d for v in range(3) for d in range(5)]
 
 
 def sha(a):
@@ -98,7 +98,9 @@ def main(out_dir):
         m = orc.pd_test_planes(planes, v)
         counts[str(v)] = int(np.count_nonzero(m != pd_ref))
     result["pd_adversarial"] = {"voxels": int(D * H * W), "positives": int(pd_ref.sum()),
-                                "mismatches_by_variant": counts, "sha256_pd": sha(pd_ref)}
+                                "mismatches_by_variant": counts, "sha256_pd": sha(pd_ref),
+                                "sha256_planes": sha(planes), "seed": SEED + 99}
+    np.savez_compressed(os.path.join(out_dir, "pd_adversarial.npz"), planes=planes, pd=pd_ref)
     print("PD variants (mismatches):", counts, flush=True)
 
     for c in CASES:
