@@ -243,8 +243,8 @@ static void plan(const hdog_params *p, int max_sub, int64_t &nvox, int64_t &reg_
   L.add(slots * sizeof(uint32_t));           // 12 acc.count
   L.add(slots * sizeof(uint32_t));           // 13 acc.max_ord
   L.add(3 * slots * sizeof(unsigned long long));  // 14 acc.sum_xyz
-  L.add(slots * sizeof(double));             // 15 acc.sum_norm
-  L.add(6 * slots * sizeof(double));         // 16 acc.hess
+  L.add(slots * sizeof(unsigned long long));      // 15 acc.sum_norm (fixed point)
+  L.add(6 * slots * sizeof(unsigned long long));  // 16 acc.hess (fixed point)
   L.add(slots * sizeof(float));              // 17 out.intensity
   L.add(3 * slots * sizeof(float));          // 18 out.centroid
   L.add(6 * slots * sizeof(float));          // 19 out.hessian
@@ -327,8 +327,8 @@ extern "C" int hdog_ctx_create(const hdog_params *p, int max_substacks, hdog_ctx
   c->acc.count = (uint32_t *)at(12);
   c->acc.max_ord = (uint32_t *)at(13);
   c->acc.sum_xyz = (unsigned long long *)at(14);
-  c->acc.sum_norm = (double *)at(15);
-  c->acc.hess = (double *)at(16);
+  c->acc.sum_norm = (unsigned long long *)at(15);
+  c->acc.hess = (unsigned long long *)at(16);
   c->out.intensity = (float *)at(17);
   c->out.centroid = (float *)at(18);
   c->out.hessian = (float *)at(19);

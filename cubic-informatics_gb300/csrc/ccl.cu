@@ -19,7 +19,8 @@
 // by reduce-by-key.  Here regions are numbered by a scan over a root bitmap (ascending
 // root index = the reference's region order), and one pass over the foreground voxels
 // accumulates count, max intensity, exact integer coordinate sums and the six Hessian
-// sums (recomputed from the DoG instead of stored) with atomics.
+// sums (recomputed from the DoG instead of stored) with integer atomics: fixed point
+// for the float sums, so the result does not depend on the order threads arrive in.
 #include "kernels.cuh"
 
 namespace hdog {
@@ -225,11 +226,11 @@ __device__ __forceinline__ void init_slot(RegionAcc acc, int64_t slots, int64_t 
   acc.label[g] = label;
   acc.count[g] = 0u;
   acc.max_ord[g] = 0u;   // below f2ord of every float
-  acc.sum_norm[g] = 0.0;
+  acc.sum_norm[g] = 0ull;
 #pragma unroll
   for (int k = 0; k < 3; k++) acc.sum_xyz[k * slots + g] = 0ull;
 #pragma unroll
-  for (int k = 0; k < 6; k++) acc.hess[k * slots + g] = 0.0;
+  for (int k = 0; k < 6; k++) acc.hess[k * slots + g] = 0ull;
 }
 
 __global__ void __launch_bounds__(kScanBlock) k_rank(const Sub *subs, const uint32_t *root_bits,
@@ -280,14 +281,14 @@ __global__ void k_accumulate(const Sub *subs, const uint8_t *mask, const int32_t
   const float v = norm[S.vox + i];
   atomicAdd(&acc.count[g], 1u);
   atomicMax(&acc.max_ord[g], f2ord(v));
-  atomicAdd(&acc.sum_norm[g], (double)v);
+  atomicAdd(&acc.sum_norm[g], to_fix(v));
   atomicAdd(&acc.sum_xyz[g], (unsigned long long)x);
   atomicAdd(&acc.sum_xyz[slots + g], (unsigned long long)y);
   atomicAdd(&acc.sum_xyz[2 * slots + g], (unsigned long long)z);
   float h[6];
   hessian_at(dog + S.vox, S.W, S.H, S.D, x, y, z, h);
 #pragma unroll
-  for (int k = 0; k < 6; k++) atomicAdd(&acc.hess[k * slots + g], (double)h[k]);
+  for (int k = 0; k < 6; k++) atomicAdd(&acc.hess[k * slots + g], to_fix(h[k]));
 }
 
 // ------------------------------------------------------------------ eigen features
@@ -344,10 +345,10 @@ __global__ void __launch_bounds__(kFinalizeBlock) k_finalize(const Sub *subs, co
     const float cx = __fdiv_rn(__ull2float_rn(acc.sum_xyz[g]), c16);
     const float cy = __fdiv_rn(__ull2float_rn(acc.sum_xyz[slots + g]), c16);
     const float cz = __fdiv_rn(__ull2float_rn(acc.sum_xyz[2 * slots + g]), c16);
-    const float inten = fp.is_ave_mode ? __double2float_rn(acc.sum_norm[g]) : ord2f(acc.max_ord[g]);
+    const float inten = fp.is_ave_mode ? __double2float_rn(from_fix(acc.sum_norm[g])) : ord2f(acc.max_ord[g]);
     float hs[6];
 #pragma unroll
-    for (int k = 0; k < 6; k++) hs[k] = __double2float_rn(acc.hess[k * slots + g]);
+    for (int k = 0; k < 6; k++) hs[k] = __double2float_rn(from_fix(acc.hess[k * slots + g]));
     float st, bl;
     eigen_features(hs, &st, &bl);
     out.intensity[g] = inten;

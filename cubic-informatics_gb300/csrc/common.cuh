@@ -73,21 +73,22 @@ __device__ __forceinline__ float cdiff(float plus, float minus) {
   return __fmul_rn(__fsub_rn(__fadd_rn(0.0f, plus), minus), 0.5f);
 }
 
-// Sylvester test of PositiveDefiniteKernel (:295-323) with each rounding written out:
-//   xx < 0,  fma(xx, yy, -(xy*xy)) > 0,
-//   det = fma(-(zz*xy), xy, fma(-(yy*xz), xz, fma(-(xx*yz), yz, fma(xx*yy, zz, (2xy*yz)*xz)))) < 0
-// This is the contraction nvcc applies to the reference's expression.
+// Sylvester test of PositiveDefiniteKernel (Hessian3DFilter_element.cu:295-323) with
+// every rounding written out, in the form nvcc gives the reference's expression
+// (pinned against the reference binary on crafted near-singular matrices):
+//   xx < 0
+//   xx*yy > xy*xy              (`a - b > 0` folded to `a > b`, both products rounded)
+//   t = fma(xx*yy, zz, (2xy*yz)*xz); t = fma(-(xx*yz), yz, t); t = fma(-(yy*xz), xz, t)
+//   t < (zz*xy)*xy             (the last subtraction of the determinant folded into `< 0`)
 __device__ __forceinline__ bool pd_test(float xx, float xy, float xz, float yy, float yz, float zz) {
   if (!(xx < 0.0f)) return false;
-  const float m2 = __fmaf_rn(xx, yy, -__fmul_rn(xy, xy));
-  if (!(m2 > 0.0f)) return false;
   const float p = __fmul_rn(xx, yy);
+  if (!(p > __fmul_rn(xy, xy))) return false;
   const float q = __fmul_rn(__fmul_rn(2.0f, xy), yz);
   float t = __fmaf_rn(p, zz, __fmul_rn(q, xz));
   t = __fmaf_rn(-__fmul_rn(xx, yz), yz, t);
   t = __fmaf_rn(-__fmul_rn(yy, xz), xz, t);
-  const float det = __fmaf_rn(-__fmul_rn(zz, xy), xy, t);
-  return det < 0.0f;
+  return t < __fmul_rn(__fmul_rn(zz, xy), xy);
 }
 
 // The six Hessian elements at voxel (x, y, z) straight from global memory, with the
@@ -110,6 +111,15 @@ __device__ __forceinline__ void hessian_at(const float *f, int W, int H, int D, 
   h[4] = cdiff(grad1(f, W, H, D, x, y, z + 1, 0, 1, 0), grad1(f, W, H, D, x, y, z - 1, 0, 1, 0));
   h[5] = cdiff(grad1(f, W, H, D, x, y, z + 1, 0, 0, 1), grad1(f, W, H, D, x, y, z - 1, 0, 0, 1));
 }
+
+// Region float sums accumulate as 64-bit fixed point with 36 fractional bits: integer
+// atomics are associative, so the sums (and every record) are identical run to run.
+constexpr double kFixScale = 68719476736.0;          // 2^36
+constexpr double kFixInv = 1.0 / 68719476736.0;
+__device__ __forceinline__ unsigned long long to_fix(float v) {
+  return (unsigned long long)__double2ll_rn((double)v * kFixScale);
+}
+__host__ __device__ __forceinline__ double from_fix(unsigned long long v) { return (double)(long long)v * kFixInv; }
 
 constexpr int kMaxTaps = 80;   // MAX_KERNEL_LENGTH of the reference DoG taps
 

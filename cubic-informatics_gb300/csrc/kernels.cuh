@@ -26,8 +26,8 @@ struct RegionAcc {
   uint32_t *count;
   uint32_t *max_ord;      // f2ord(max normalized intensity)
   unsigned long long *sum_xyz;   // [3][cap] exact coordinate sums
-  double *sum_norm;
-  double *hess;           // [6][cap]
+  unsigned long long *sum_norm;  // fixed point (kFixScale)
+  unsigned long long *hess;      // [6][cap] fixed point (kFixScale)
 };
 
 struct RegionOut {

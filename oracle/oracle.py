@@ -18,8 +18,11 @@ DT_RECORD = np.dtype([
 ])
 
 # Contraction form of the Sylvester test that matches the reference binary
-# (pd_variant = minor form + 4 * determinant form, see orc_pd_test).
-PD_VARIANT_REFERENCE = 1 + 4 * 1
+# (pd_variant = minor form + 4 * determinant form, see orc_pd_test): both minor
+# products rounded and compared, the determinant as an FMA chain whose last
+# subtraction is folded into the compare.  Pinned by oracle/ref_golden.py: 0 of
+# 524,288 crafted near-singular matrices differ (tests/golden/ref_stages.json).
+PD_VARIANT_REFERENCE = 0 + 4 * 3
 
 
 class orc_params(ctypes.Structure):

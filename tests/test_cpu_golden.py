@@ -53,3 +53,21 @@ def test_oracle_erosion_reproduces_reference_digest():
     c = [c for c in GOLDEN["cases"] if c["name"] == e["case"]][0]
     out = orc.erosion(case_volume(c), *e["radius"])
     assert sha(out) == e["sha256"] and e["oracle_mismatch"] == 0
+
+
+def test_oracle_sylvester_form_matches_reference_on_near_singular_matrices():
+    """524,288 Hessians built so that the 2x2 minor or the determinant sits at float32
+    resolution; the reference's PositiveDefiniteKernel output digest was recorded on the
+    GPU.  Only the contraction form the oracle uses reproduces it; the others miss by
+    thousands of voxels (the recorded per-form counts)."""
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(__file__)), "oracle"))
+    from oracle import ref_golden
+    g = GOLDEN["pd_adversarial"]
+    planes = ref_golden.adversarial_hessians(g["voxels"], g["seed"]).reshape(6, 32, 128, 128)
+    assert sha(planes) == g["sha256_planes"]
+    m = orc.pd_test_planes(planes, orc.PD_VARIANT_REFERENCE)
+    assert sha(m) == g["sha256_pd"]
+    counts = g["mismatches_by_variant"]
+    assert counts[str(orc.PD_VARIANT_REFERENCE)] == 0
+    assert sorted(counts.values())[1] > 0
