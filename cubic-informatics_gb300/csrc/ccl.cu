@@ -11,8 +11,8 @@
 // component the minimum linear index of its voxels, over a graph whose edges are the
 // 26 LINEAR offsets dz*W*H + dy*W + dx kept inside [0, N) -- so rows and slices wrap --
 // and where voxel 0 is background.  Here the same labels come from a lock-free
-// union-find: one pass links every foreground voxel to its 13 backward neighbours with
-// atomicMin (the larger root always hangs under the smaller, so roots are component
+// union-find: one pass links every foreground voxel to its 13 backward neighbours (a
+// compare-and-swap hangs the larger root under the smaller, so roots are component
 // minima), one pass flattens.  No host round trip, no iteration count.
 //
 // Features.  The reference runs ten full-volume radix sorts (label -> value) followed
@@ -26,12 +26,25 @@
 namespace hdog {
 
 // ------------------------------------------------------------------ union-find
+// Invariants: a parent pointer only ever points to a smaller index in the same tree;
+// a root is linked only by a compare-and-swap that requires it to still be a root, so
+// trees merge but never split.  Under those two rules a stale read (the L1 cache is not
+// coherent across SMs) can only show an older pointer of the same tree: a find may stop
+// early at a former root, but two finds that meet at one node are truly in one tree,
+// and a link attempted on a former root fails and retries from its current parent.
+// Path halving writes only an ancestor of the node's parent, which keeps both rules.
+template <bool L2_ONLY>
+__device__ __forceinline__ int32_t lab_ld(const int32_t *p) {
+  return L2_ONLY ? __ldcg(p) : *p;
+}
+
+template <bool L2_ONLY>
 __device__ __forceinline__ int32_t uf_find(int32_t *L, int32_t a, int64_t limit, int *status) {
-  int32_t p = L[a];
+  int32_t p = lab_ld<L2_ONLY>(L + a);
   int64_t steps = 0;
   while (p != a) {
-    const int32_t gp = L[p];
-    if (gp != p) L[a] = gp;   // path halving; gp is an ancestor of a in the same tree
+    const int32_t gp = lab_ld<L2_ONLY>(L + p);
+    if (gp != p) L[a] = gp;   // path halving: gp is an ancestor of a's parent
     a = p;
     p = gp;
     if (++steps > limit) { atomicExch(status, HDOG_ERR_TIMEOUT); break; }
@@ -41,13 +54,13 @@ __device__ __forceinline__ int32_t uf_find(int32_t *L, int32_t a, int64_t limit,
 
 __device__ __forceinline__ void uf_union(int32_t *L, int32_t a, int32_t b, int64_t limit, int *status) {
   for (int64_t it = 0; it <= limit; it++) {
-    a = uf_find(L, a, limit, status);
-    b = uf_find(L, b, limit, status);
+    a = uf_find<true>(L, a, limit, status);
+    b = uf_find<true>(L, b, limit, status);
     if (a == b) return;
     if (a > b) { const int32_t t = a; a = b; b = t; }
-    const int32_t old = atomicMin(&L[b], a);
-    if (old == b) return;   // b was a root and now hangs under a
-    b = old;                // b was re-parented meanwhile: merge its new parent instead
+    const int32_t cur = atomicCAS(&L[b], b, a);
+    if (cur == b) return;   // b was still a root: it now hangs under the smaller root a
+    b = cur;                // b had been linked meanwhile: continue from its parent
   }
   atomicExch(status, HDOG_ERR_TIMEOUT);
 }
@@ -95,7 +108,7 @@ __global__ void __launch_bounds__(kScanBlock) k_ccl_flatten(const Sub *subs, con
   bool root = false;
   if (i > 0 && i < n && mask[S.vox + i]) {
     int32_t *L = labels + S.vox;
-    const int32_t r = uf_find(L, (int32_t)i, n, status);
+    const int32_t r = uf_find<true>(L, (int32_t)i, n, status);
     L[i] = r;
     root = (r == (int32_t)i);
   }
