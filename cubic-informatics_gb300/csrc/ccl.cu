@@ -52,6 +52,19 @@ __device__ __forceinline__ int32_t uf_find(int32_t *L, int32_t a, int64_t limit,
   return a;
 }
 
+// Read-only walk to the root, for the flatten pass: there every store must be a final
+// root, so no thread may leave an intermediate ancestor behind with a halving store.
+__device__ __forceinline__ int32_t uf_root(const int32_t *L, int32_t a, int64_t limit, int *status) {
+  int32_t p = __ldcg(L + a);
+  int64_t steps = 0;
+  while (p != a) {
+    a = p;
+    p = __ldcg(L + a);
+    if (++steps > limit) { atomicExch(status, HDOG_ERR_TIMEOUT); break; }
+  }
+  return a;
+}
+
 __device__ __forceinline__ void uf_union(int32_t *L, int32_t a, int32_t b, int64_t limit, int *status) {
   for (int64_t it = 0; it <= limit; it++) {
     a = uf_find<true>(L, a, limit, status);
@@ -108,7 +121,7 @@ __global__ void __launch_bounds__(kScanBlock) k_ccl_flatten(const Sub *subs, con
   bool root = false;
   if (i > 0 && i < n && mask[S.vox + i]) {
     int32_t *L = labels + S.vox;
-    const int32_t r = uf_find<true>(L, (int32_t)i, n, status);
+    const int32_t r = uf_root(L, (int32_t)i, n, status);
     L[i] = r;
     root = (r == (int32_t)i);
   }
