@@ -54,3 +54,15 @@ def test_fullframe_stack_records_are_deterministic(stack):
     assert a.tobytes() == b.tobytes()
     assert a.tobytes() == c.tobytes()
     assert a.tobytes() == d.tobytes()
+
+
+def test_fullframe_stack_records_match_oracle(stack):
+    """The whole 2560x2160x128 stack (8 substacks, ~1.3M records) against the oracle:
+    exact centroids, intensity and size; eigen features within 1e-4 relative."""
+    from test_gpu_pipeline import assert_records_match
+    p = hdog.make_params(**P)
+    with hdog.Context(p, max_substacks=8) as ctx:
+        got = ctx.run_stack(torch.from_numpy(stack).cuda())
+    ref = orc.stack(orc.params_from(p), stack)
+    assert len(ref) > 1000000
+    assert_records_match(got, ref, "camera stack")
