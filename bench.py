@@ -129,6 +129,7 @@ def time_steps(ctx, stack, steps, warmup, stream, dist=None):
     for _ in range(warmup):
         ctx.run_stack(stack, stream=stream)
     torch.cuda.synchronize()
+    ctx.timing_read()          # drop the warm-up launches from the per-kernel times
     if dist:
         dist.barrier()
     torch.cuda.synchronize()

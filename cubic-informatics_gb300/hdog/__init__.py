@@ -254,7 +254,7 @@ class Context:
         check(lib().hdog_timing_enable(self._h, int(bool(on))))
 
     def timing_read(self):
-        """{kernel: (launches, total_ms)} since the last read."""
+        """{kernel: (launches, total_ms)} since the last read ({} when timing is off)."""
         buf = ctypes.create_string_buffer(1 << 16)
         check(lib().hdog_timing_read(self._h, buf, len(buf)))
         out = {}
