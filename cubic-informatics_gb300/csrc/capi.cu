@@ -169,6 +169,8 @@ struct hdog_ctx {
   int64_t reg_cap = 0;     // region slots per substack (background included)
   int64_t nblk = 0;        // per-substack block slots (voxel blocks and region blocks)
   int64_t nchk = 0;        // per-substack chunk slots
+  int64_t edge_cap = 0;    // cross-tile CCL edges per substack
+  int num_sms = 152;
   int margin = 0;
   DogTaps taps;
   std::mutex mu;
@@ -181,6 +183,8 @@ struct hdog_ctx {
   uint8_t *mask = nullptr;
   int32_t *labels = nullptr;
   uint32_t *root_bits = nullptr, *blk_counts = nullptr, *blk_offsets = nullptr, *chunk = nullptr;
+  int2 *edges = nullptr;
+  unsigned long long *edge_count = nullptr;
   RegionAcc acc{};
   RegionOut out{};
   hdog_record *records = nullptr;
@@ -220,6 +224,8 @@ struct Layout {
   }
 };
 
+static int64_t edge_capacity(int64_t nvox) { return nvox / 8 + 1024; }
+
 static void plan(const hdog_params *p, int max_sub, int64_t &nvox, int64_t &reg_cap, int64_t &nblk,
                  int64_t &nchk, Layout &L) {
   nvox = (int64_t)p->width * p->height * p->depth;
@@ -256,6 +262,8 @@ static void plan(const hdog_params *p, int max_sub, int64_t &nvox, int64_t &reg_
   L.add(sizeof(int));                        // 25 status
   L.add(S * sizeof(Sub));                    // 26 subs
   L.add(6 * S * sizeof(int64_t));            // 27 seg
+  L.add(S * edge_capacity(nvox) * sizeof(int2));          // 28 cross-tile edges
+  L.add(S * sizeof(unsigned long long));     // 29 edge counts
 }
 
 extern "C" int hdog_ctx_bytes(const hdog_params *p, int max_substacks, size_t *bytes) {
@@ -340,6 +348,10 @@ extern "C" int hdog_ctx_create(const hdog_params *p, int max_substacks, hdog_ctx
   c->status = (int *)at(25);
   c->d_subs = (Sub *)at(26);
   c->d_seg = (int64_t *)at(27);
+  c->edges = (int2 *)at(28);
+  c->edge_count = (unsigned long long *)at(29);
+  c->edge_cap = edge_capacity(c->nvox);
+  cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->dev);
   const size_t hb = (size_t)max_substacks * sizeof(Sub) + 6 * (size_t)max_substacks * sizeof(int64_t) +
                     (2 * (size_t)max_substacks + 2) * sizeof(int64_t);
   e = cudaMallocHost(&c->h_subs, hb);
@@ -374,6 +386,8 @@ static void set_sub(hdog_ctx *c, int s, const uint16_t *src, int depth_valid, in
   S.reg = (int64_t)s * c->reg_cap;
   S.reg_cap = c->reg_cap;
   S.blk = (int64_t)s * c->nblk;
+  S.edge = (int64_t)s * c->edge_cap;
+  S.edge_cap = c->edge_cap;
   S.src = src;
   const int ms = c->max_sub;
   c->h_seg[0 * ms + s] = S.blk;
@@ -445,7 +459,8 @@ static int run_batch(hdog_ctx *c, int nsub, cudaStream_t st) {
   enqueue_normalize(c, nsub, c->norm, st);
   enqueue_dog(c, nsub, c->norm, c->dog, st);
   launch_hessian_pd(c->d_subs, nsub, c->W, c->H, c->D, c->dog, c->mask, nullptr, st);
-  launch_ccl(c->d_subs, nsub, c->nvox, c->mask, c->labels, c->root_bits, c->blk_counts, c->status, st);
+  launch_ccl(c->d_subs, nsub, c->W, c->H, c->D, c->nvox, c->mask, c->labels, c->edges, c->edge_count, c->root_bits,
+             c->blk_counts, c->status, c->num_sms, st);
   int32_t *rank = reinterpret_cast<int32_t *>(c->fa);
   launch_regions(c->d_subs, nsub, c->nvox, vseg_of(c), c->mask, c->labels, c->root_bits, c->norm, c->dog, rank,
                  c->blk_counts, c->blk_offsets, c->chunk, c->num_regions, c->acc, c->slots, c->status, st);
@@ -534,7 +549,8 @@ extern "C" int hdog_ccl(hdog_ctx *c, const uint8_t *d_mask, int32_t *d_labels, v
   cudaStream_t st = (cudaStream_t)stream;
   TRY(single_sub(c, nullptr, st));
   HDOG_CUDA_TRY(cudaMemsetAsync(c->status, 0, sizeof(int), st));
-  launch_ccl(c->d_subs, 1, c->nvox, d_mask, d_labels, c->root_bits, c->blk_counts, c->status, st);
+  launch_ccl(c->d_subs, 1, c->W, c->H, c->D, c->nvox, d_mask, d_labels, c->edges, c->edge_count, c->root_bits,
+             c->blk_counts, c->status, c->num_sms, st);
   HDOG_CUDA_TRY(cudaGetLastError());
   int status = 0;
   HDOG_CUDA_TRY(cudaMemcpyAsync(&status, c->status, sizeof(int), cudaMemcpyDeviceToHost, st));

@@ -1,50 +1,39 @@
-// ccl.cu -- connected components, regional features, eigen features and candidate
-// records, sm_103a.
+// ccl.cu -- 3D connected-component labelling with the reference's connectivity, sm_103a.
 //
-// Reference: src/3D/CCL3D.cu (CCL :81-117), src/3D/RegionalFeatures.cu (HessianFeatures
-// :295-329, MaxNormalized :65-87, SumNormalized :114-137, RegionalSizeAndCentroid
-// :214-255), src/3D/Eigenvalues.cu (:19-112) and src/3D/utils.h (saveFeatureVector
-// :204-250).
+// Reference: src/3D/CCL3D.cu (CCL :81-117).  The reference iterates neighbour-min scans
+// and pointer jumping, synchronising with the host twice per iteration.  Its fixed point
+// labels each component with the minimum linear index of its voxels, over a graph whose
+// edges are the 26 LINEAR offsets dz*W*H + dy*W + dx kept inside [0, N) -- so a row end
+// touches the next row's start and a slice's last row the next slice's first -- and in
+// which voxel 0 is background (label = index * mask).
 //
-// CCL.  The reference labels with iterated neighbour-min scans and pointer jumping,
-// synchronising with the host twice per iteration.  Its fixed point gives each
-// component the minimum linear index of its voxels, over a graph whose edges are the
-// 26 LINEAR offsets dz*W*H + dy*W + dx kept inside [0, N) -- so rows and slices wrap --
-// and where voxel 0 is background.  Here the same labels come from a lock-free
-// union-find: one pass links every foreground voxel to its 13 backward neighbours (a
-// compare-and-swap hangs the larger root under the smaller, so roots are component
-// minima), one pass flattens.  No host round trip, no iteration count.
-//
-// Features.  The reference runs ten full-volume radix sorts (label -> value) followed
-// by reduce-by-key.  Here regions are numbered by a scan over a root bitmap (ascending
-// root index = the reference's region order), and one pass over the foreground voxels
-// accumulates count, max intensity, exact integer coordinate sums and the six Hessian
-// sums (recomputed from the DoG instead of stored) with integer atomics: fixed point
-// for the float sums, so the result does not depend on the order threads arrive in.
+// Here the same labels come from union-find in three passes, with no host round trip:
+//   1. k_ccl_local: a 64 x 16 x 32 tile (a whole 32-slice substack column) is labelled in
+//      shared memory with 16-bit parents; the tile's foreground edges that leave the
+//      tile (its x and y faces, and the wrap-around offsets) go to a compact edge list.
+//   2. k_ccl_edges: a persistent pass merges those edges in the global label array.
+//      If the list overflowed, k_ccl_cross_direct merges the same edges from the mask.
+//   3. k_ccl_flatten: every foreground voxel gets its root (a read-only walk, so every
+//      store is final); roots are recorded in a bitmap and counted per 4096 voxels for
+//      the region numbering.
+// Linking always hangs the larger root under the smaller, so roots are component minima.
 #include "kernels.cuh"
 
 namespace hdog {
 
-// ------------------------------------------------------------------ union-find
-// Invariants: a parent pointer only ever points to a smaller index in the same tree;
-// a root is linked only by a compare-and-swap that requires it to still be a root, so
-// trees merge but never split.  Under those two rules a stale read (the L1 cache is not
-// coherent across SMs) can only show an older pointer of the same tree: a find may stop
-// early at a former root, but two finds that meet at one node are truly in one tree,
-// and a link attempted on a former root fails and retries from its current parent.
-// Path halving writes only an ancestor of the node's parent, which keeps both rules.
-template <bool L2_ONLY>
-__device__ __forceinline__ int32_t lab_ld(const int32_t *p) {
-  return L2_ONLY ? __ldcg(p) : *p;
-}
-
-template <bool L2_ONLY>
+// ------------------------------------------------------------------ global union-find
+// Invariants: a parent pointer only ever points to a smaller index in the same tree; a
+// root is linked only by a compare-and-swap that requires it to still be a root, so
+// trees merge but never split.  A stale read (the L1 cache is not coherent across SMs)
+// can then only show an older pointer of the same tree: two finds that meet at one node
+// are truly in one tree, and a link attempted on a former root fails and retries from
+// its current parent.  Path halving stores only an ancestor of the node's parent.
 __device__ __forceinline__ int32_t uf_find(int32_t *L, int32_t a, int64_t limit, int *status) {
-  int32_t p = lab_ld<L2_ONLY>(L + a);
+  int32_t p = __ldcg(L + a);
   int64_t steps = 0;
   while (p != a) {
-    const int32_t gp = lab_ld<L2_ONLY>(L + p);
-    if (gp != p) L[a] = gp;   // path halving: gp is an ancestor of a's parent
+    const int32_t gp = __ldcg(L + p);
+    if (gp != p) L[a] = gp;
     a = p;
     p = gp;
     if (++steps > limit) { atomicExch(status, HDOG_ERR_TIMEOUT); break; }
@@ -52,8 +41,7 @@ __device__ __forceinline__ int32_t uf_find(int32_t *L, int32_t a, int64_t limit,
   return a;
 }
 
-// Read-only walk to the root, for the flatten pass: there every store must be a final
-// root, so no thread may leave an intermediate ancestor behind with a halving store.
+// Read-only walk, for the flatten pass where every store must be a final root.
 __device__ __forceinline__ int32_t uf_root(const int32_t *L, int32_t a, int64_t limit, int *status) {
   int32_t p = __ldcg(L + a);
   int64_t steps = 0;
@@ -67,422 +55,305 @@ __device__ __forceinline__ int32_t uf_root(const int32_t *L, int32_t a, int64_t 
 
 __device__ __forceinline__ void uf_union(int32_t *L, int32_t a, int32_t b, int64_t limit, int *status) {
   for (int64_t it = 0; it <= limit; it++) {
-    a = uf_find<true>(L, a, limit, status);
-    b = uf_find<true>(L, b, limit, status);
+    a = uf_find(L, a, limit, status);
+    b = uf_find(L, b, limit, status);
     if (a == b) return;
     if (a > b) { const int32_t t = a; a = b; b = t; }
     const int32_t cur = atomicCAS(&L[b], b, a);
-    if (cur == b) return;   // b was still a root: it now hangs under the smaller root a
-    b = cur;                // b had been linked meanwhile: continue from its parent
+    if (cur == b) return;
+    b = cur;
   }
   atomicExch(status, HDOG_ERR_TIMEOUT);
 }
 
-// initLabels (CCL3D.cu:17-26): label = index * mask, so voxel 0 is always background.
-__global__ void k_ccl_init(const Sub *subs, const uint8_t *mask, int32_t *labels) {
-  const Sub S = subs[blockIdx.y];
-  const int64_t n = (int64_t)S.W * S.H * S.D;
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  labels[S.vox + i] = (i > 0 && mask[S.vox + i]) ? (int32_t)i : 0;
+// The 13 backward linear offsets (the other 13 of the 26 are their mirror images).
+__device__ __forceinline__ void back_offset(int k, int &dz, int &dy, int &dx) {
+  dz = k < 9 ? -1 : 0;
+  dy = k < 9 ? k / 3 - 1 : (k < 12 ? -1 : 0);
+  dx = k < 9 ? k % 3 - 1 : (k < 12 ? k - 10 : -1);
 }
 
-// Union with the 13 backward linear neighbours (the other 13 are their mirror images).
-__global__ void k_ccl_merge(const Sub *subs, const uint8_t *mask, int32_t *labels, int *status) {
+// ------------------------------------------------------------------ pass 1: tile-local
+constexpr int kTX = 64, kTY = 16, kTZ = 32;
+constexpr int kTileVox = kTX * kTY * kTZ;     // 32768: parents fit in 16 bits
+constexpr int kCclThreads = 256;              // thread = 4 x-consecutive voxels of one row, all kTZ slices
+constexpr uint16_t kBg = 0xFFFF;
+
+__device__ __forceinline__ int sfind(volatile uint16_t *lab, int t) {
+  int p = lab[t];
+  while (p != t) {
+    t = p;
+    p = lab[t];
+  }
+  return t;
+}
+
+__device__ __forceinline__ void sunion(uint16_t *lab, int a, int b) {
+  volatile uint16_t *v = lab;
+  for (int it = 0; it < 2 * kTileVox; it++) {
+    a = sfind(v, a);
+    b = sfind(v, b);
+    if (a == b) return;
+    if (a > b) { const int t = a; a = b; b = t; }
+    const unsigned short cur = atomicCAS(reinterpret_cast<unsigned short *>(&lab[b]), (unsigned short)b,
+                                         (unsigned short)a);
+    if (cur == b) return;
+    b = cur;
+  }
+}
+
+struct CclTile {
+  int x0, y0, z0, tz;     // origin, slices in this tile
+};
+
+__device__ __forceinline__ bool ccl_tile(const Sub &S, int64_t bid, CclTile &T) {
+  const int nx = (S.W + kTX - 1) / kTX, ny = (S.H + kTY - 1) / kTY, nz = (S.D + kTZ - 1) / kTZ;
+  if (bid >= (int64_t)nx * ny * nz) return false;
+  T.x0 = (int)(bid % nx) * kTX;
+  T.y0 = (int)((bid / nx) % ny) * kTY;
+  T.z0 = (int)(bid / ((int64_t)nx * ny)) * kTZ;
+  T.tz = min(kTZ, S.D - T.z0);
+  return true;
+}
+
+// Backward neighbour (dz, dy, dx) of voxel (x, y, z), tile coordinates (lx, ly, lz):
+// true when the edge is not a plain 3D step inside this tile (it leaves the tile, or
+// it wraps around a row or slice end).
+__device__ __forceinline__ bool leaves_tile(const Sub &S, const CclTile &T, int x, int y, int z, int lx, int ly,
+                                            int lz, int dz, int dy, int dx) {
+  const int nx = x + dx, ny = y + dy, nz = z + dz;
+  const bool in_vol = nx >= 0 && nx < S.W && ny >= 0 && ny < S.H && nz >= 0;
+  const bool in_tile = lx + dx >= 0 && lx + dx < kTX && ly + dy >= 0 && ly + dy < kTY && lz + dz >= 0 && lz + dz < T.tz;
+  return !(in_vol && in_tile);
+}
+
+__global__ void __launch_bounds__(kCclThreads) k_ccl_local(const Sub *subs, const uint8_t *mask, int32_t *labels,
+                                                          int2 *edges, unsigned long long *edge_count) {
+  extern __shared__ uint16_t lab[];   // kTileVox entries
   const Sub S = subs[blockIdx.y];
-  const int64_t n = (int64_t)S.W * S.H * S.D;
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i <= 0 || i >= n) return;
+  CclTile T;
+  if (!ccl_tile(S, blockIdx.x, T)) return;
+  const int t = threadIdx.x;
+  const int lx0 = (t % (kTX / 4)) * 4, ly = t / (kTX / 4);
+  const int x = T.x0 + lx0, y = T.y0 + ly;
+  const int64_t WH = (int64_t)S.W * S.H;
   const uint8_t *m = mask + S.vox;
-  if (!m[i]) return;
+  const bool row_ok = y < S.H;
+  const bool vec = row_ok && x + 3 < S.W && (S.W % 4 == 0) &&
+                   ((reinterpret_cast<uintptr_t>(m + (int64_t)y * S.W + x) & 3) == 0);
+  // 1. foreground -> own tile index, background -> kBg
+  for (int lz = 0; lz < kTZ; lz++) {
+    const int lt = (lz * kTY + ly) * kTX + lx0;
+    uint32_t w = 0;
+    if (lz < T.tz) {
+      const int64_t g = (T.z0 + lz) * WH + (int64_t)y * S.W + x;
+      if (vec) {
+        w = __ldg(reinterpret_cast<const uint32_t *>(m + g));
+      } else if (row_ok) {
+        for (int k = 0; k < 4; k++)
+          if (x + k < S.W && m[g + k]) w |= 0xFFu << (8 * k);
+      }
+      if (g == 0) w &= ~0xFFu;   // voxel 0 is background
+    }
+    ushort4 v;
+    v.x = (w & 0xFFu) ? (uint16_t)lt : kBg;
+    v.y = ((w >> 8) & 0xFFu) ? (uint16_t)(lt + 1) : kBg;
+    v.z = ((w >> 16) & 0xFFu) ? (uint16_t)(lt + 2) : kBg;
+    v.w = (w >> 24) ? (uint16_t)(lt + 3) : kBg;
+    *reinterpret_cast<ushort4 *>(&lab[lt]) = v;
+  }
+  __syncthreads();
+  // 2. unions along edges inside the tile; count the edges that leave it
+  int n_cross = 0;
+  for (int lz = 0; lz < T.tz; lz++) {
+    const int z = T.z0 + lz;
+    for (int k = 0; k < 4; k++) {
+      const int lt = (lz * kTY + ly) * kTX + lx0 + k;
+      if (lab[lt] == kBg) continue;
+      const int lx = lx0 + k;
+      for (int o = 0; o < 13; o++) {
+        int dz, dy, dx;
+        back_offset(o, dz, dy, dx);
+        if (!leaves_tile(S, T, x + k, y, z, lx, ly, lz, dz, dy, dx)) {
+          const int ln = lt + (dz * kTY + dy) * kTX + dx;
+          if (lab[ln] != kBg) sunion(lab, lt, ln);
+        } else {
+          const int64_t g = z * WH + (int64_t)y * S.W + x + k;
+          const int64_t gn = g + dz * WH + dy * (int64_t)S.W + dx;
+          if (gn >= 1 && m[gn]) n_cross++;
+        }
+      }
+    }
+  }
+  __syncthreads();
+  // 3. reserve edge slots (one atomic per warp), write labels and edges
+  const int lane = threadIdx.x & 31;
+  int incl = n_cross;
+  for (int d = 1; d < 32; d <<= 1) {
+    const int v = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+    if (lane >= d) incl += v;
+  }
+  const int warp_total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+  unsigned long long base = 0;
+  if (lane == 31 && warp_total) base = atomicAdd(&edge_count[blockIdx.y], (unsigned long long)warp_total);
+  base = __shfl_sync(0xFFFFFFFFu, base, 31) + (unsigned long long)(incl - n_cross);
+  if (!row_ok) return;
   int32_t *L = labels + S.vox;
-  const int64_t W = S.W, WH = (int64_t)S.W * S.H;
-#pragma unroll
-  for (int k = 0; k < 13; k++) {
-    const int dz = k < 9 ? -1 : 0;
-    const int dy = k < 9 ? (k / 3) - 1 : (k < 12 ? -1 : 0);
-    const int dx = k < 9 ? (k % 3) - 1 : (k < 12 ? (k - 9) - 1 : -1);
-    const int64_t j = i + dz * WH + dy * W + dx;
-    if (j <= 0) continue;
-    if (m[j]) uf_union(L, (int32_t)i, (int32_t)j, n, status);
-  }
-}
-
-// Flatten to roots; record roots in a bitmap and count them per 1024-voxel block.
-__global__ void __launch_bounds__(kScanBlock) k_ccl_flatten(const Sub *subs, const uint8_t *mask,
-                                                            int32_t *labels, uint32_t *root_bits,
-                                                            uint32_t *blk_counts, int *status) {
-  __shared__ uint32_t warp_cnt[kScanBlock / 32];
-  const Sub S = subs[blockIdx.y];
-  const int64_t n = (int64_t)S.W * S.H * S.D;
-  const int64_t base = (int64_t)blockIdx.x * kScanBlock;
-  if (base >= n) return;
-  const int64_t i = base + threadIdx.x;
-  bool root = false;
-  if (i > 0 && i < n && mask[S.vox + i]) {
-    int32_t *L = labels + S.vox;
-    const int32_t r = uf_root(L, (int32_t)i, n, status);
-    L[i] = r;
-    root = (r == (int32_t)i);
-  }
-  const uint32_t bits = __ballot_sync(0xFFFFFFFFu, root);
-  if ((threadIdx.x & 31) == 0) {
-    root_bits[(S.blk + blockIdx.x) * (kScanBlock / 32) + (threadIdx.x >> 5)] = bits;
-    warp_cnt[threadIdx.x >> 5] = __popc(bits);
-  }
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    uint32_t c = warp_cnt[threadIdx.x];
-    for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xFFFFFFFFu, c, o);
-    if (threadIdx.x == 0) blk_counts[S.blk + blockIdx.x] = c;
-  }
-}
-
-// Same outputs as k_ccl_flatten for labels produced elsewhere: foreground = label != 0.
-__global__ void __launch_bounds__(kScanBlock) k_roots_from_labels(const Sub *subs, const int32_t *labels,
-                                                                  uint8_t *mask, uint32_t *root_bits,
-                                                                  uint32_t *blk_counts) {
-  __shared__ uint32_t warp_cnt[kScanBlock / 32];
-  const Sub S = subs[blockIdx.y];
-  const int64_t n = (int64_t)S.W * S.H * S.D;
-  const int64_t base = (int64_t)blockIdx.x * kScanBlock;
-  if (base >= n) return;
-  const int64_t i = base + threadIdx.x;
-  bool root = false;
-  if (i < n) {
-    const int32_t l = labels[S.vox + i];
-    mask[S.vox + i] = l != 0;
-    root = i > 0 && l == (int32_t)i;
-  }
-  const uint32_t bits = __ballot_sync(0xFFFFFFFFu, root);
-  if ((threadIdx.x & 31) == 0) {
-    root_bits[(S.blk + blockIdx.x) * (kScanBlock / 32) + (threadIdx.x >> 5)] = bits;
-    warp_cnt[threadIdx.x >> 5] = __popc(bits);
-  }
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    uint32_t cnt = warp_cnt[threadIdx.x];
-    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_down_sync(0xFFFFFFFFu, cnt, o);
-    if (threadIdx.x == 0) blk_counts[S.blk + blockIdx.x] = cnt;
-  }
-}
-
-// ------------------------------------------------------------------ segmented scan
-// Exclusive scan of per-block counts, independently per substack.  seg_off/seg_len
-// locate each substack's count array; chunk scratch holds one sum per 1024 counts.
-__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t *total) {
-  __shared__ uint32_t wsum[33];   // [0, 32): exclusive warp offsets, [32]: block total
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  uint32_t inc = v;
-  for (int o = 1; o < 32; o <<= 1) {
-    const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, inc, o);
-    if (lane >= o) inc += y;
-  }
-  if (lane == 31) wsum[w] = inc;
-  __syncthreads();
-  if (w == 0) {
-    const int nw = blockDim.x >> 5;
-    uint32_t s = lane < nw ? wsum[lane] : 0u, si = s;
-    for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, si, o);
-      if (lane >= o) si += y;
+  for (int lz = 0; lz < T.tz; lz++) {
+    const int z = T.z0 + lz;
+    const int64_t g = z * WH + (int64_t)y * S.W + x;
+    int32_t out[4];
+    for (int k = 0; k < 4; k++) {
+      const int lt = (lz * kTY + ly) * kTX + lx0 + k;
+      out[k] = 0;
+      if (lab[lt] == kBg) continue;
+      const int r = sfind(lab, lt);
+      const int rx = r % kTX, ry = (r / kTX) % kTY, rz = r / (kTX * kTY);
+      out[k] = (int32_t)((T.z0 + rz) * WH + (int64_t)(T.y0 + ry) * S.W + T.x0 + rx);
+      if (n_cross == 0) continue;
+      for (int o = 0; o < 13; o++) {
+        int dz, dy, dx;
+        back_offset(o, dz, dy, dx);
+        if (!leaves_tile(S, T, x + k, y, z, lx0 + k, ly, lz, dz, dy, dx)) continue;
+        const int64_t gn = g + k + dz * WH + dy * (int64_t)S.W + dx;
+        if (gn >= 1 && m[gn]) {
+          if ((int64_t)base < S.edge_cap) edges[S.edge + base] = make_int2((int32_t)(g + k), (int32_t)gn);
+          base++;
+        }
+      }
     }
-    if (lane < nw) wsum[lane] = si - s;
-    if (lane == nw - 1) wsum[32] = si;
-  }
-  __syncthreads();
-  const uint32_t r = wsum[w] + inc - v;
-  if (total) *total = wsum[32];
-  __syncthreads();
-  return r;
-}
-
-__global__ void __launch_bounds__(1024) k_scan_p1(const int64_t *seg_off, const int64_t *seg_len,
-                                                  const int64_t *chk_off, const uint32_t *in,
-                                                  uint32_t *chunk) {
-  const int s = blockIdx.y;
-  const int64_t len = seg_len[s], c = blockIdx.x;
-  if (c * 1024 >= len) return;
-  const int64_t i = c * 1024 + threadIdx.x;
-  uint32_t v = i < len ? in[seg_off[s] + i] : 0u;
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xFFFFFFFFu, v, o);
-  __shared__ uint32_t ws[32];
-  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = v;
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    uint32_t t = ws[threadIdx.x];
-    for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xFFFFFFFFu, t, o);
-    if (threadIdx.x == 0) chunk[chk_off[s] + c] = t;
+    if (vec) {
+      *reinterpret_cast<int4 *>(L + g) = make_int4(out[0], out[1], out[2], out[3]);
+    } else {
+      for (int k = 0; k < 4; k++)
+        if (x + k < S.W) L[g + k] = out[k];
+    }
   }
 }
 
-// One block per substack: exclusive scan of its chunk sums; total -> totals[s].
-__global__ void __launch_bounds__(1024) k_scan_p2(const int64_t *seg_len, const int64_t *chk_off,
-                                                  uint32_t *chunk, int64_t *totals, int64_t add) {
-  const int s = blockIdx.x;
-  const int64_t nch = (seg_len[s] + 1023) / 1024;
-  uint32_t carry = 0;
-  for (int64_t b = 0; b < nch; b += 1024) {
-    const int64_t i = b + threadIdx.x;
-    const uint32_t v = i < nch ? chunk[chk_off[s] + i] : 0u;
-    uint32_t tot;
-    const uint32_t e = block_excl_scan(v, &tot);
-    if (i < nch) chunk[chk_off[s] + i] = carry + e;
-    carry += tot;
+// ------------------------------------------------------------------ pass 2: cross-tile edges
+__global__ void k_ccl_edges(const Sub *subs, const int2 *edges, const unsigned long long *edge_count,
+                            int32_t *labels, int *status) {
+  const Sub S = subs[blockIdx.y];
+  const unsigned long long cnt = edge_count[blockIdx.y];
+  if (cnt > (unsigned long long)S.edge_cap) return;   // overflowed: k_ccl_cross_direct merges instead
+  const int64_t n = (int64_t)S.W * S.H * S.D;
+  int32_t *L = labels + S.vox;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < (int64_t)cnt;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int2 ab = edges[S.edge + e];
+    uf_union(L, ab.x, ab.y, n, status);
   }
-  if (threadIdx.x == 0) totals[s] = (int64_t)carry + add;
 }
 
-__global__ void __launch_bounds__(1024) k_scan_p3(const int64_t *seg_off, const int64_t *seg_len,
-                                                  const int64_t *chk_off, const uint32_t *in,
-                                                  const uint32_t *chunk, uint32_t *out) {
-  const int s = blockIdx.y;
-  const int64_t len = seg_len[s], c = blockIdx.x;
-  if (c * 1024 >= len) return;
-  const int64_t i = c * 1024 + threadIdx.x;
-  const uint32_t v = i < len ? in[seg_off[s] + i] : 0u;
-  const uint32_t e = block_excl_scan(v, nullptr);
-  if (i < len) out[seg_off[s] + i] = chunk[chk_off[s] + c] + e;
+// The same cross-tile edges straight from the mask, for a substack whose list overflowed.
+__global__ void __launch_bounds__(kCclThreads) k_ccl_cross_direct(const Sub *subs, const uint8_t *mask,
+                                                                 const unsigned long long *edge_count,
+                                                                 int32_t *labels, int *status) {
+  const Sub S = subs[blockIdx.y];
+  if (edge_count[blockIdx.y] <= (unsigned long long)S.edge_cap) return;
+  CclTile T;
+  if (!ccl_tile(S, blockIdx.x, T)) return;
+  const int t = threadIdx.x;
+  const int lx0 = (t % (kTX / 4)) * 4, ly = t / (kTX / 4);
+  const int x = T.x0 + lx0, y = T.y0 + ly;
+  if (y >= S.H) return;
+  const int64_t WH = (int64_t)S.W * S.H, n = WH * S.D;
+  const uint8_t *m = mask + S.vox;
+  int32_t *L = labels + S.vox;
+  for (int lz = 0; lz < T.tz; lz++) {
+    const int z = T.z0 + lz;
+    for (int k = 0; k < 4 && x + k < S.W; k++) {
+      const int64_t g = z * WH + (int64_t)y * S.W + x + k;
+      if (g == 0 || !m[g]) continue;
+      for (int o = 0; o < 13; o++) {
+        int dz, dy, dx;
+        back_offset(o, dz, dy, dx);
+        if (!leaves_tile(S, T, x + k, y, z, lx0 + k, ly, lz, dz, dy, dx)) continue;
+        const int64_t gn = g + dz * WH + dy * (int64_t)S.W + dx;
+        if (gn >= 1 && m[gn]) uf_union(L, (int32_t)g, (int32_t)gn, n, status);
+      }
+    }
+  }
 }
 
-// ------------------------------------------------------------------ region numbering
-// Region r >= 1 is the r-th root in ascending voxel order (region 0 = background), the
-// order reduce-by-key over sorted labels produces.  Each root initialises its slot.
-__device__ __forceinline__ void init_slot(RegionAcc acc, int64_t slots, int64_t g, int32_t label) {
-  acc.label[g] = label;
-  acc.count[g] = 0u;
-  acc.max_ord[g] = 0u;   // below f2ord of every float
-  acc.sum_norm[g] = 0ull;
-#pragma unroll
-  for (int k = 0; k < 3; k++) acc.sum_xyz[k * slots + g] = 0ull;
-#pragma unroll
-  for (int k = 0; k < 6; k++) acc.hess[k * slots + g] = 0ull;
-}
-
-__global__ void __launch_bounds__(kScanBlock) k_rank(const Sub *subs, const uint32_t *root_bits,
-                                                     const uint32_t *blk_offsets, int32_t *rank,
-                                                     RegionAcc acc, int64_t slots, int *status) {
+// ------------------------------------------------------------------ pass 3: flatten
+// 4096 voxels per block, 16 consecutive voxels per thread.  Root bits of voxels
+// [32w, 32w+32) of block b go to word (S.blk + b) * 128 + w.
+template <bool FROM_LABELS>
+__global__ void __launch_bounds__(256) k_ccl_flatten(const Sub *subs, uint8_t *mask, int32_t *labels,
+                                                    uint32_t *root_bits, uint32_t *blk_counts, int *status) {
+  __shared__ uint32_t wcnt[8];
   const Sub S = subs[blockIdx.y];
   const int64_t n = (int64_t)S.W * S.H * S.D;
   const int64_t base = (int64_t)blockIdx.x * kScanBlock;
   if (base >= n) return;
-  __shared__ uint32_t wpre[kScanBlock / 32];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const uint32_t bits = root_bits[(S.blk + blockIdx.x) * (kScanBlock / 32) + w];
-  if (lane == 0) wpre[w] = __popc(bits);
-  __syncthreads();
-  if (w == 0) {
-    uint32_t v = wpre[lane], inc = v;
-    for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, inc, o);
-      if (lane >= o) inc += y;
+  const int64_t i0 = base + threadIdx.x * 16;
+  int32_t *L = labels + S.vox;
+  uint8_t *m = mask + S.vox;
+  uint32_t bits = 0;
+  if (!FROM_LABELS) {
+    uint8_t mk[16];
+    if (i0 + 16 <= n && ((reinterpret_cast<uintptr_t>(m + i0) & 15) == 0)) {
+      *reinterpret_cast<uint4 *>(mk) = __ldg(reinterpret_cast<const uint4 *>(m + i0));
+    } else {
+      for (int k = 0; k < 16; k++) mk[k] = (i0 + k < n) ? m[i0 + k] : 0;
     }
-    wpre[lane] = inc - v;
-  }
-  __syncthreads();
-  if (blockIdx.x == 0 && threadIdx.x == 0) init_slot(acc, slots, S.reg, 0);
-  if (!((bits >> lane) & 1u)) return;
-  const int64_t r = 1 + (int64_t)blk_offsets[S.blk + blockIdx.x] + wpre[w] + __popc(bits & ((1u << lane) - 1u));
-  if (r >= S.reg_cap) { atomicExch(status, HDOG_ERR_CAPACITY); return; }
-  const int64_t i = base + threadIdx.x;
-  rank[S.vox + i] = (int32_t)r;
-  init_slot(acc, slots, S.reg + r, (int32_t)i);
-}
-
-// One pass over the foreground: count, max / sum of normalized intensity, exact
-// coordinate sums, Hessian element sums.
-__global__ void k_accumulate(const Sub *subs, const uint8_t *mask, const int32_t *labels,
-                             const int32_t *rank, const float *norm, const float *dog, RegionAcc acc,
-                             int64_t slots) {
-  const Sub S = subs[blockIdx.y];
-  const int64_t n = (int64_t)S.W * S.H * S.D;
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i <= 0 || i >= n) return;
-  if (!mask[S.vox + i]) return;
-  const int32_t lab = labels[S.vox + i];
-  const int32_t r = rank[S.vox + lab];
-  if (r <= 0 || r >= S.reg_cap) return;
-  const int64_t g = S.reg + r;
-  const int x = (int)(i % S.W), y = (int)((i / S.W) % S.H), z = (int)(i / ((int64_t)S.W * S.H));
-  const float v = norm[S.vox + i];
-  atomicAdd(&acc.count[g], 1u);
-  atomicMax(&acc.max_ord[g], f2ord(v));
-  atomicAdd(&acc.sum_norm[g], to_fix(v));
-  atomicAdd(&acc.sum_xyz[g], (unsigned long long)x);
-  atomicAdd(&acc.sum_xyz[slots + g], (unsigned long long)y);
-  atomicAdd(&acc.sum_xyz[2 * slots + g], (unsigned long long)z);
-  float h[6];
-  hessian_at(dog + S.vox, S.W, S.H, S.D, x, y, z, h);
-#pragma unroll
-  for (int k = 0; k < 6; k++) atomicAdd(&acc.hess[k * slots + g], to_fix(h[k]));
-}
-
-// ------------------------------------------------------------------ eigen features
-// EigenvaluesKernel<float> (Eigenvalues.cu:19-96): Eberly's closed form in double on
-// the float region sums; structureness = l0^2 + l1^2 + l2^2, blobness = l2^2 / (l0*l1).
-__device__ void eigen_features(const float hs[6], float *structureness, float *blobness) {
-  const double xx = hs[0], xy = hs[1], xz = hs[2], yy = hs[3], yz = hs[4], zz = hs[5];
-  const double max0 = fmax(fabs(xx), fabs(xy));
-  const double max1 = fmax(fabs(xz), fabs(yy));
-  const double max2 = fmax(fabs(yz), fabs(zz));
-  const double maxAbs = fmax(fmax(max0, max1), max2);
-  if (maxAbs < 1e-30) { *structureness = 0.f; *blobness = 0.f; return; }
-  const double nrm = xy * xy + xz * xz + yz * yz;
-  double e0, e1, e2;
-  if (nrm > 1e-30) {
-    const double t = (xx + yy + zz) / 3.0;
-    const double b00 = xx - t, b11 = yy - t, b22 = zz - t;
-    const double den = sqrt((b00 * b00 + b11 * b11 + b22 * b22 + nrm * 2.0) / 6.0);
-    const double c00 = b11 * b22 - yz * yz;
-    const double c01 = xy * b22 - yz * xz;
-    const double c02 = xy * yz - b11 * xz;
-    const double det = (b00 * c00 - xy * c01 + xz * c02) / (den * den * den);
-    const double hd = fmin(fmax(det * 0.5, -1.0), 1.0);
-    const double ang = acos(hd) / 3.0;
-    const double twoThirdsPi = 2.094395102393195;
-    const double beta2 = cos(ang) * 2.0;
-    const double beta0 = cos(ang + twoThirdsPi) * 2.0;
-    const double beta1 = -(beta0 + beta2);
-    e0 = t + den * beta0;
-    e1 = t + den * beta1;
-    e2 = t + den * beta2;
+    for (int k = 0; k < 16; k++) {
+      const int64_t i = i0 + k;
+      if (i == 0 || !mk[k]) continue;
+      const int32_t l = __ldcg(L + i);
+      const int32_t r = uf_root(L, l, n, status);
+      if (r != l) L[i] = r;
+      if (r == (int32_t)i) bits |= 1u << k;
+    }
   } else {
-    e0 = xx; e1 = yy; e2 = zz;
-  }
-  *structureness = (float)(e0 * e0 + e1 * e1 + e2 * e2);
-  *blobness = (float)(e2 * e2 / (e0 * e1));
-}
-
-// Per region: float features, eigen features and the saveFeatureVector filter
-// (utils.h:222-232); keep counts per block of kFinalizeBlock regions.
-__global__ void __launch_bounds__(kFinalizeBlock) k_finalize(const Sub *subs, const int64_t *num_regions,
-                                                            RegionAcc acc, int64_t slots, RegionOut out,
-                                                            FilterParams fp, uint32_t *blk_counts) {
-  const Sub S = subs[blockIdx.y];
-  const int64_t nblk = (S.reg_cap + kFinalizeBlock - 1) / kFinalizeBlock;
-  if ((int64_t)blockIdx.x >= nblk) return;
-  const int64_t R = num_regions[blockIdx.y];
-  const int64_t r = (int64_t)blockIdx.x * kFinalizeBlock + threadIdx.x;
-  bool keep = false;
-  if (r < R) {
-    const int64_t g = S.reg + r;
-    const uint32_t cnt = acc.count[g];
-    const float c16 = (float)(uint16_t)(cnt & 0xFFFFu);
-    const float cx = __fdiv_rn(__ull2float_rn(acc.sum_xyz[g]), c16);
-    const float cy = __fdiv_rn(__ull2float_rn(acc.sum_xyz[slots + g]), c16);
-    const float cz = __fdiv_rn(__ull2float_rn(acc.sum_xyz[2 * slots + g]), c16);
-    const float inten = fp.is_ave_mode ? __double2float_rn(from_fix(acc.sum_norm[g])) : ord2f(acc.max_ord[g]);
-    float hs[6];
-#pragma unroll
-    for (int k = 0; k < 6; k++) hs[k] = __double2float_rn(from_fix(acc.hess[k * slots + g]));
-    float st, bl;
-    eigen_features(hs, &st, &bl);
-    out.intensity[g] = inten;
-    out.centroid[g] = cx; out.centroid[slots + g] = cy; out.centroid[2 * slots + g] = cz;
-#pragma unroll
-    for (int k = 0; k < 6; k++) out.hessian[k * slots + g] = hs[k];
-    out.eigen[g] = st; out.eigen[slots + g] = bl;
-    if (r >= 1) {
-      keep = true;
-      if (cz < (float)S.margin || cz >= (float)(S.depth_valid - S.margin)) keep = false;
-      if (cx < (float)fp.left || cx >= (float)(S.W - fp.right)) keep = false;
-      if (cy < (float)fp.top || cy >= (float)(S.H - fp.bottom)) keep = false;
-      if ((int)(cnt & 0xFFFFu) < fp.min_size || inten <= 0.0f) keep = false;
+    // labels produced elsewhere: foreground = nonzero label, roots label themselves
+    for (int k = 0; k < 16; k++) {
+      const int64_t i = i0 + k;
+      if (i >= n) break;
+      const int32_t l = L[i];
+      m[i] = l != 0;
+      if (i > 0 && l == (int32_t)i) bits |= 1u << k;
     }
-    out.keep[g] = keep ? 1 : 0;
   }
-  const uint32_t b = __ballot_sync(0xFFFFFFFFu, keep);
-  __shared__ uint32_t wc[kFinalizeBlock / 32];
-  if ((threadIdx.x & 31) == 0) wc[threadIdx.x >> 5] = __popc(b);
+  const uint32_t hi = __shfl_down_sync(0xFFFFFFFFu, bits, 1);
+  if ((threadIdx.x & 1) == 0) root_bits[(S.blk + blockIdx.x) * (kScanBlock / 32) + threadIdx.x / 2] = bits | (hi << 16);
+  uint32_t c = __popc(bits);
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xFFFFFFFFu, c, o);
+  if ((threadIdx.x & 31) == 0) wcnt[threadIdx.x >> 5] = c;
   __syncthreads();
   if (threadIdx.x == 0) {
-    uint32_t t = 0;
-    for (int k = 0; k < kFinalizeBlock / 32; k++) t += wc[k];
-    blk_counts[S.blk + blockIdx.x] = t;
+    uint32_t tot = 0;
+    for (int k = 0; k < 8; k++) tot += wcnt[k];
+    blk_counts[S.blk + blockIdx.x] = tot;
   }
 }
-
-// Write kept regions as 28-byte records in region order (FeatureVector, utils.h:235-246).
-__global__ void __launch_bounds__(kFinalizeBlock) k_records(const Sub *subs, const int64_t *num_regions,
-                                                           RegionOut out, const uint32_t *count,
-                                                           int64_t slots, const uint32_t *blk_offsets,
-                                                           hdog_record *rec) {
-  const Sub S = subs[blockIdx.y];
-  const int64_t nblk = (S.reg_cap + kFinalizeBlock - 1) / kFinalizeBlock;
-  if ((int64_t)blockIdx.x >= nblk) return;
-  const int64_t R = num_regions[blockIdx.y];
-  const int64_t r = (int64_t)blockIdx.x * kFinalizeBlock + threadIdx.x;
-  const int64_t g = S.reg + r;
-  const bool keep = r < R && out.keep[g];
-  const uint32_t b = __ballot_sync(0xFFFFFFFFu, keep);
-  __shared__ uint32_t wp[kFinalizeBlock / 32];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  if (lane == 0) wp[w] = __popc(b);
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    uint32_t t = 0;
-    for (int k = 0; k < kFinalizeBlock / 32; k++) { const uint32_t c = wp[k]; wp[k] = t; t += c; }
-  }
-  __syncthreads();
-  if (!keep) return;
-  const int64_t o = S.reg + blk_offsets[S.blk + blockIdx.x] + wp[w] + __popc(b & ((1u << lane) - 1u));
-  hdog_record q;
-  q.centroid_x = out.centroid[g];
-  q.centroid_y = out.centroid[slots + g];
-  q.centroid_z = __fadd_rn(out.centroid[2 * slots + g], (float)S.z0);
-  q.structureness = out.eigen[g];
-  q.blobness = out.eigen[slots + g];
-  q.intensity = out.intensity[g];
-  q.size = (uint16_t)(count[g] & 0xFFFFu);
-  q.padding = 0;
-  rec[o] = q;
-}
-
 
 // ------------------------------------------------------------------ launchers
-void launch_scan(const ScanSeg &sg, int nsub, const uint32_t *in, uint32_t *out, uint32_t *chunk,
-                 int64_t *totals, int64_t add, cudaStream_t s) {
-  const unsigned nch = ceil_div(sg.max_len, 1024);
-  KLAUNCH("k_scan_p1", s, (k_scan_p1<<<dim3(nch, nsub), 1024, 0, s>>>(sg.off, sg.len, sg.chk, in, chunk)));
-  KLAUNCH("k_scan_p2", s, (k_scan_p2<<<nsub, 1024, 0, s>>>(sg.len, sg.chk, chunk, totals, add)));
-  KLAUNCH("k_scan_p3", s, (k_scan_p3<<<dim3(nch, nsub), 1024, 0, s>>>(sg.off, sg.len, sg.chk, in, chunk, out)));
-}
-
-void launch_ccl(const Sub *d_subs, int nsub, int64_t max_n, const uint8_t *mask, int32_t *labels,
-                uint32_t *root_bits, uint32_t *blk_counts, int *d_status, cudaStream_t s) {
-  const unsigned g256 = ceil_div(max_n, 256);
-  KLAUNCH("k_ccl_init", s, (k_ccl_init<<<dim3(g256, nsub), 256, 0, s>>>(d_subs, mask, labels)));
-  KLAUNCH("k_ccl_merge", s, (k_ccl_merge<<<dim3(g256, nsub), 256, 0, s>>>(d_subs, mask, labels, d_status)));
-  KLAUNCH("k_ccl_flatten", s, (k_ccl_flatten<<<dim3(ceil_div(max_n, kScanBlock), nsub), kScanBlock, 0, s>>>(d_subs, mask, labels, root_bits,
-                                                                              blk_counts, d_status)));
+void launch_ccl(const Sub *d_subs, int nsub, int max_w, int max_h, int max_d, int64_t max_n, const uint8_t *mask,
+                int32_t *labels, int2 *edges, unsigned long long *edge_count, uint32_t *root_bits,
+                uint32_t *blk_counts, int *d_status, int num_sms, cudaStream_t s) {
+  const int64_t tiles = (int64_t)ceil_div(max_w, kTX) * ceil_div(max_h, kTY) * ceil_div(max_d, kTZ);
+  cudaMemsetAsync(edge_count, 0, nsub * sizeof(unsigned long long), s);
+  const int smem = kTileVox * (int)sizeof(uint16_t);
+  cudaFuncSetAttribute(k_ccl_local, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  KLAUNCH("k_ccl_local", s, (k_ccl_local<<<dim3((unsigned)tiles, nsub), kCclThreads, smem, s>>>(
+                                d_subs, mask, labels, edges, edge_count)));
+  const unsigned eb = (unsigned)max(1, (8 * num_sms + nsub - 1) / nsub);
+  KLAUNCH("k_ccl_edges", s, (k_ccl_edges<<<dim3(eb, nsub), 256, 0, s>>>(d_subs, edges, edge_count, labels,
+                                                                        d_status)));
+  KLAUNCH("k_ccl_cross_direct", s, (k_ccl_cross_direct<<<dim3((unsigned)tiles, nsub), kCclThreads, 0, s>>>(
+                                       d_subs, mask, edge_count, labels, d_status)));
+  KLAUNCH("k_ccl_flatten", s, (k_ccl_flatten<false><<<dim3(ceil_div(max_n, kScanBlock), nsub), 256, 0, s>>>(
+                                  d_subs, const_cast<uint8_t *>(mask), labels, root_bits, blk_counts, d_status)));
 }
 
 void launch_roots_from_labels(const Sub *d_subs, int nsub, int64_t max_n, const int32_t *labels, uint8_t *mask,
                               uint32_t *root_bits, uint32_t *blk_counts, cudaStream_t s) {
-  KLAUNCH("k_roots_from_labels", s, (k_roots_from_labels<<<dim3(ceil_div(max_n, kScanBlock), nsub), kScanBlock, 0, s>>>(d_subs, labels, mask, root_bits,
-                                                                                    blk_counts)));
-}
-
-void launch_regions(const Sub *d_subs, int nsub, int64_t max_n, const ScanSeg &vseg, const uint8_t *mask,
-                    const int32_t *labels, const uint32_t *root_bits, const float *norm, const float *dog,
-                    int32_t *rank, uint32_t *blk_counts, uint32_t *blk_offsets, uint32_t *chunk,
-                    int64_t *d_num_regions, RegionAcc acc, int64_t slots, int *d_status, cudaStream_t s) {
-  launch_scan(vseg, nsub, blk_counts, blk_offsets, chunk, d_num_regions, 1, s);
-  KLAUNCH("k_rank", s, (k_rank<<<dim3(ceil_div(max_n, kScanBlock), nsub), kScanBlock, 0, s>>>(d_subs, root_bits, blk_offsets, rank,
-                                                                        acc, slots, d_status)));
-  KLAUNCH("k_accumulate", s, (k_accumulate<<<dim3(ceil_div(max_n, 256), nsub), 256, 0, s>>>(d_subs, mask, labels, rank, norm, dog, acc,
-                                                                slots)));
-}
-
-void launch_finalize(const Sub *d_subs, int nsub, int64_t max_reg_cap, const ScanSeg &rseg,
-                     const int64_t *d_num_regions, RegionAcc acc, int64_t slots, RegionOut out,
-                     FilterParams fp, uint32_t *blk_counts, uint32_t *blk_offsets, uint32_t *chunk,
-                     int64_t *d_num_records, hdog_record *records, cudaStream_t s) {
-  const unsigned nb = ceil_div(max_reg_cap, kFinalizeBlock);
-  KLAUNCH("k_finalize", s, (k_finalize<<<dim3(nb, nsub), kFinalizeBlock, 0, s>>>(d_subs, d_num_regions, acc, slots, out, fp, blk_counts)));
-  launch_scan(rseg, nsub, blk_counts, blk_offsets, chunk, d_num_records, 0, s);
-  KLAUNCH("k_records", s, (k_records<<<dim3(nb, nsub), kFinalizeBlock, 0, s>>>(d_subs, d_num_regions, out, acc.count, slots, blk_offsets,
-                                                      records)));
+  KLAUNCH("k_roots_from_labels", s, (k_ccl_flatten<true><<<dim3(ceil_div(max_n, kScanBlock), nsub), 256, 0, s>>>(
+                                        d_subs, mask, const_cast<int32_t *>(labels), root_bits, blk_counts,
+                                        nullptr)));
 }
 
 }  // namespace hdog

@@ -17,6 +17,8 @@ struct Sub {
   int64_t reg;            // offset of its region slots in the region arrays
   int64_t reg_cap;        // number of region slots (background included)
   int64_t blk;            // offset of its per-block slots in block scratch arrays
+  int64_t edge;           // offset of its cross-tile edge list
+  int64_t edge_cap;       // edge list capacity
   const uint16_t *src;    // slice 0 of the raw input (device); slices are W*H apart
 };
 
@@ -77,8 +79,9 @@ struct ScanSeg {
 };
 void launch_scan(const ScanSeg &sg, int nsub, const uint32_t *in, uint32_t *out, uint32_t *chunk,
                  int64_t *totals, int64_t add, cudaStream_t s);
-void launch_ccl(const Sub *d_subs, int nsub, int64_t max_n, const uint8_t *mask, int32_t *labels,
-                uint32_t *root_bits, uint32_t *blk_counts, int *d_status, cudaStream_t s);
+void launch_ccl(const Sub *d_subs, int nsub, int max_w, int max_h, int max_d, int64_t max_n, const uint8_t *mask,
+                int32_t *labels, int2 *edges, unsigned long long *edge_count, uint32_t *root_bits,
+                uint32_t *blk_counts, int *d_status, int num_sms, cudaStream_t s);
 // Foreground mask (label != 0), root bitmap and per-block root counts from labels alone.
 void launch_roots_from_labels(const Sub *d_subs, int nsub, int64_t max_n, const int32_t *labels, uint8_t *mask,
                               uint32_t *root_bits, uint32_t *blk_counts, cudaStream_t s);
@@ -92,7 +95,7 @@ void launch_finalize(const Sub *d_subs, int nsub, int64_t max_reg_cap, const Sca
                      int64_t *d_num_records, hdog_record *records, cudaStream_t s);
 
 constexpr int kMaxRadiusXY = 421;    // shared-memory bound of the min/max y pass
-constexpr int kScanBlock = 1024;     // voxels per block in the region scans
+constexpr int kScanBlock = 4096;     // voxels per block in the region scans (16 per thread)
 constexpr int kFinalizeBlock = 256;  // regions per block in finalize / record compaction
 
 }  // namespace hdog
