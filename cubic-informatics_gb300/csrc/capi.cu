@@ -170,7 +170,10 @@ struct hdog_ctx {
   int64_t nblk = 0;        // per-substack block slots (voxel blocks and region blocks)
   int64_t nchk = 0;        // per-substack chunk slots
   int64_t edge_cap = 0;    // cross-tile CCL edges per substack
+  int64_t fg_cap = 0;      // foreground-list entries per substack
   int num_sms = 152;
+  int max_smem = 48 * 1024;
+  bool use_sweep = true;   // fused DoG + Hessian sweep when the parameters allow it
   int margin = 0;
   DogTaps taps;
   std::mutex mu;
@@ -185,6 +188,8 @@ struct hdog_ctx {
   uint32_t *root_bits = nullptr, *blk_counts = nullptr, *blk_offsets = nullptr, *chunk = nullptr;
   int2 *edges = nullptr;
   unsigned long long *edge_count = nullptr;
+  FgEntry *fg = nullptr;
+  unsigned long long *fg_count = nullptr;
   RegionAcc acc{};
   RegionOut out{};
   hdog_record *records = nullptr;
@@ -197,7 +202,7 @@ struct hdog_ctx {
   // pinned host staging
   Sub *h_subs = nullptr;
   int64_t *h_seg = nullptr;
-  int64_t *h_counts = nullptr;   // [2*max_sub + 1]: records per substack, regions per substack, status
+  int64_t *h_counts = nullptr;   // [3*max_sub + 2]: records, regions, foreground counts per substack; status
   // device copy of a whole stack for hdog_run_stack with host input
   uint16_t *stack_buf = nullptr;
   size_t stack_bytes = 0;
@@ -213,7 +218,7 @@ struct TimerScope {
 static size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 
 struct Layout {
-  size_t off[32];
+  size_t off[40];
   int n = 0;
   size_t total = 0;
   size_t add(size_t bytes) {
@@ -225,6 +230,7 @@ struct Layout {
 };
 
 static int64_t edge_capacity(int64_t nvox) { return nvox / 8 + 1024; }
+static int64_t fg_capacity(int64_t nvox) { return nvox / 8 + 1024; }
 
 static void plan(const hdog_params *p, int max_sub, int64_t &nvox, int64_t &reg_cap, int64_t &nblk,
                  int64_t &nchk, Layout &L) {
@@ -264,6 +270,8 @@ static void plan(const hdog_params *p, int max_sub, int64_t &nvox, int64_t &reg_
   L.add(6 * S * sizeof(int64_t));            // 27 seg
   L.add(S * edge_capacity(nvox) * sizeof(int2));          // 28 cross-tile edges
   L.add(S * sizeof(unsigned long long));     // 29 edge counts
+  L.add(S * fg_capacity(nvox) * sizeof(FgEntry));         // 30 foreground list
+  L.add(S * sizeof(unsigned long long));     // 31 foreground counts
 }
 
 extern "C" int hdog_ctx_bytes(const hdog_params *p, int max_substacks, size_t *bytes) {
@@ -351,9 +359,13 @@ extern "C" int hdog_ctx_create(const hdog_params *p, int max_substacks, hdog_ctx
   c->edges = (int2 *)at(28);
   c->edge_count = (unsigned long long *)at(29);
   c->edge_cap = edge_capacity(c->nvox);
+  c->fg = (FgEntry *)at(30);
+  c->fg_count = (unsigned long long *)at(31);
+  c->fg_cap = fg_capacity(c->nvox);
   cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->dev);
+  cudaDeviceGetAttribute(&c->max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->dev);
   const size_t hb = (size_t)max_substacks * sizeof(Sub) + 6 * (size_t)max_substacks * sizeof(int64_t) +
-                    (2 * (size_t)max_substacks + 2) * sizeof(int64_t);
+                    (3 * (size_t)max_substacks + 2) * sizeof(int64_t);
   e = cudaMallocHost(&c->h_subs, hb);
   if (e != cudaSuccess) {
     cudaFree(c->arena);
@@ -388,6 +400,8 @@ static void set_sub(hdog_ctx *c, int s, const uint16_t *src, int depth_valid, in
   S.blk = (int64_t)s * c->nblk;
   S.edge = (int64_t)s * c->edge_cap;
   S.edge_cap = c->edge_cap;
+  S.fg = (int64_t)s * c->fg_cap;
+  S.fg_cap = c->fg_cap;
   S.src = src;
   const int ms = c->max_sub;
   c->h_seg[0 * ms + s] = S.blk;
@@ -440,6 +454,46 @@ static void enqueue_dog(hdog_ctx *c, int nsub, const float *norm, float *dog, cu
   launch_dog(c->d_subs, nsub, c->W, c->H, c->D, (int64_t)c->H * c->D, c->taps, norm, c->fa, c->fb, dog, st);
 }
 
+// The chain after normalization: DoG + Hessian (fused sweep or separate passes), CCL,
+// region numbering and accumulation, features and record compaction.
+static void enqueue_after_norm(hdog_ctx *c, int nsub, bool fused, cudaStream_t st) {
+  if (fused) {
+    launch_dog_hess(c->d_subs, nsub, c->W, c->H, c->D, c->taps, c->norm, c->mask, c->fg, c->fg_count, c->status, st);
+  } else {
+    enqueue_dog(c, nsub, c->norm, c->dog, st);
+    launch_hessian_pd(c->d_subs, nsub, c->W, c->H, c->D, c->dog, c->mask, nullptr, st);
+  }
+  launch_ccl(c->d_subs, nsub, c->W, c->H, c->D, c->nvox, c->mask, c->labels, c->edges, c->edge_count, c->root_bits,
+             c->blk_counts, c->status, c->num_sms, st);
+  int32_t *rank = reinterpret_cast<int32_t *>(c->fa);
+  if (fused)
+    launch_regions_fg(c->d_subs, nsub, c->nvox, c->fg_cap, vseg_of(c), c->labels, c->root_bits, c->fg, c->fg_count, rank,
+                      c->blk_counts, c->blk_offsets, c->chunk, c->num_regions, c->acc, c->slots, c->status, c->num_sms,
+                      st);
+  else
+    launch_regions(c->d_subs, nsub, c->nvox, vseg_of(c), c->mask, c->labels, c->root_bits, c->norm, c->dog, rank,
+                   c->blk_counts, c->blk_offsets, c->chunk, c->num_regions, c->acc, c->slots, c->status, st);
+  launch_finalize(c->d_subs, nsub, c->reg_cap, rseg_of(c), c->num_regions, c->acc, c->slots, c->out, filter_of(c->p),
+                  c->blk_counts, c->blk_offsets, c->chunk, c->num_records, c->records, st);
+}
+
+static bool fused_ok(hdog_ctx *c) { return c->use_sweep && sweep_supported(c->taps, c->W, c->max_smem); }
+
+// Reads record / region / foreground counts and the status word back (one sync).
+static int readback(hdog_ctx *c, int nsub, cudaStream_t st) {
+  const int ms = c->max_sub;
+  HDOG_CUDA_TRY(cudaGetLastError());
+  HDOG_CUDA_TRY(cudaMemcpyAsync(c->h_counts, c->num_records, nsub * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  HDOG_CUDA_TRY(cudaMemcpyAsync(c->h_counts + ms, c->num_regions, nsub * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  HDOG_CUDA_TRY(cudaMemcpyAsync(c->h_counts + 2 * ms, c->fg_count, nsub * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  HDOG_CUDA_TRY(cudaMemcpyAsync(c->h_counts + 3 * ms, c->status, sizeof(int), cudaMemcpyDeviceToHost, st));
+  HDOG_CUDA_TRY(cudaStreamSynchronize(st));
+  const int status = *(int *)(c->h_counts + 3 * ms);
+  if (status == HDOG_ERR_CAPACITY) return fail(HDOG_ERR_CAPACITY, "region capacity exceeded");
+  if (status != 0) return fail(status, "a bounded device wait or loop hit its limit");
+  return HDOG_OK;
+}
+
 // Whole chain for nsub substacks whose descriptors are set (host side).  Leaves record
 // counts, region counts and the status word in c->h_counts after a stream sync.
 static int run_batch(hdog_ctx *c, int nsub, cudaStream_t st) {
@@ -457,24 +511,20 @@ static int run_batch(hdog_ctx *c, int nsub, cudaStream_t st) {
     TRY(upload_subs(c, nsub, st));
   }
   enqueue_normalize(c, nsub, c->norm, st);
-  enqueue_dog(c, nsub, c->norm, c->dog, st);
-  launch_hessian_pd(c->d_subs, nsub, c->W, c->H, c->D, c->dog, c->mask, nullptr, st);
-  launch_ccl(c->d_subs, nsub, c->W, c->H, c->D, c->nvox, c->mask, c->labels, c->edges, c->edge_count, c->root_bits,
-             c->blk_counts, c->status, c->num_sms, st);
-  int32_t *rank = reinterpret_cast<int32_t *>(c->fa);
-  launch_regions(c->d_subs, nsub, c->nvox, vseg_of(c), c->mask, c->labels, c->root_bits, c->norm, c->dog, rank,
-                 c->blk_counts, c->blk_offsets, c->chunk, c->num_regions, c->acc, c->slots, c->status, st);
-  launch_finalize(c->d_subs, nsub, c->reg_cap, rseg_of(c), c->num_regions, c->acc, c->slots, c->out,
-                  filter_of(c->p), c->blk_counts, c->blk_offsets, c->chunk, c->num_records, c->records, st);
-  HDOG_CUDA_TRY(cudaGetLastError());
-  HDOG_CUDA_TRY(cudaMemcpyAsync(c->h_counts, c->num_records, nsub * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
-  HDOG_CUDA_TRY(cudaMemcpyAsync(c->h_counts + c->max_sub, c->num_regions, nsub * sizeof(int64_t),
-                                cudaMemcpyDeviceToHost, st));
-  HDOG_CUDA_TRY(cudaMemcpyAsync(c->h_counts + 2 * c->max_sub, c->status, sizeof(int), cudaMemcpyDeviceToHost, st));
-  HDOG_CUDA_TRY(cudaStreamSynchronize(st));
-  const int status = *(int *)(c->h_counts + 2 * c->max_sub);
-  if (status == HDOG_ERR_CAPACITY) return fail(HDOG_ERR_CAPACITY, "region capacity exceeded");
-  if (status != 0) return fail(status, "device loop limit reached in connected-component labelling");
+  const bool fused = fused_ok(c);
+  if (fused) HDOG_CUDA_TRY(cudaMemsetAsync(c->fg_count, 0, nsub * sizeof(unsigned long long), st));
+  enqueue_after_norm(c, nsub, fused, st);
+  TRY(readback(c, nsub, st));
+  if (fused) {
+    bool over = false;
+    for (int s = 0; s < nsub; s++) over |= c->h_counts[2 * c->max_sub + s] > c->fg_cap;
+    if (over) {
+      // more foreground than the list holds: redo this batch with the separate passes
+      HDOG_CUDA_TRY(cudaMemsetAsync(c->status, 0, sizeof(int), st));
+      enqueue_after_norm(c, nsub, false, st);
+      TRY(readback(c, nsub, st));
+    }
+  }
   return HDOG_OK;
 }
 
@@ -845,6 +895,16 @@ extern "C" int hdog_run_param_file(const char *param_path, int verbose) {
   if (h_stack) cudaFreeHost(h_stack);
   hdog_ctx_destroy(ctx);
   return rc;
+}
+
+// ------------------------------------------------------------------ options
+extern "C" int hdog_ctx_set_option(hdog_ctx *c, int option, int value) {
+  if (!c) return fail(HDOG_ERR_ARG, "null context");
+  std::lock_guard<std::mutex> lock(c->mu);
+  switch (option) {
+    case HDOG_OPT_FUSED_SWEEP: c->use_sweep = value != 0; return HDOG_OK;
+    default: return fail(HDOG_ERR_ARG, "unknown option");
+  }
 }
 
 // ------------------------------------------------------------------ timing

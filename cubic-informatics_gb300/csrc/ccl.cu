@@ -79,7 +79,21 @@ constexpr int kTileVox = kTX * kTY * kTZ;     // 32768: parents fit in 16 bits
 constexpr int kCclThreads = 256;              // thread = 4 x-consecutive voxels of one row, all kTZ slices
 constexpr uint16_t kBg = 0xFFFF;
 
+// Find with path halving (stores an ancestor of the parent only, as in the global
+// version); without it "smaller root wins" linking grows long chains.
 __device__ __forceinline__ int sfind(volatile uint16_t *lab, int t) {
+  int p = lab[t];
+  while (p != t) {
+    const int gp = lab[p];
+    if (gp != p) lab[t] = (uint16_t)gp;
+    t = p;
+    p = gp;
+  }
+  return t;
+}
+
+// Read-only find for the final pass over a finished forest.
+__device__ __forceinline__ int sroot(const uint16_t *lab, int t) {
   int p = lab[t];
   while (p != t) {
     t = p;
@@ -207,7 +221,7 @@ __global__ void __launch_bounds__(kCclThreads) k_ccl_local(const Sub *subs, cons
       const int lt = (lz * kTY + ly) * kTX + lx0 + k;
       out[k] = 0;
       if (lab[lt] == kBg) continue;
-      const int r = sfind(lab, lt);
+      const int r = sroot(lab, lt);
       const int rx = r % kTX, ry = (r / kTX) % kTY, rz = r / (kTX * kTY);
       out[k] = (int32_t)((T.z0 + rz) * WH + (int64_t)(T.y0 + ry) * S.W + T.x0 + rx);
       if (n_cross == 0) continue;

@@ -19,7 +19,16 @@ struct Sub {
   int64_t blk;            // offset of its per-block slots in block scratch arrays
   int64_t edge;           // offset of its cross-tile edge list
   int64_t edge_cap;       // edge list capacity
+  int64_t fg;             // offset of its foreground list (fused DoG/Hessian sweep)
+  int64_t fg_cap;         // foreground list capacity
   const uint16_t *src;    // slice 0 of the raw input (device); slices are W*H apart
+};
+
+// A foreground voxel and its six Hessian elements, written by the fused sweep.
+struct FgEntry {
+  int32_t idx;            // linear voxel index inside the substack
+  float norm;             // normalized intensity at the voxel
+  float h[6];             // xx, xy, xz, yy, yz, zz
 };
 
 // Per-region accumulators (SoA over all region slots of a batch).
@@ -70,6 +79,12 @@ void launch_dog(const Sub *d_subs, int nsub, int max_w, int max_h, int max_d, in
                 const DogTaps &T, const float *norm, float2 *t0, float2 *t1, float *dog, cudaStream_t s);
 void launch_hessian_pd(const Sub *d_subs, int nsub, int max_w, int max_h, int max_d,
                        const float *dog, uint8_t *mask, float *hess6, cudaStream_t s);
+// ---- sweep.cu ----
+constexpr int kMaxSweepRxy = 12;
+size_t sweep_smem_bytes(int rxy);
+bool sweep_supported(const DogTaps &T, int W, int max_smem);
+int launch_dog_hess(const Sub *d_subs, int nsub, int W, int H, int D, const DogTaps &T, const float *norm,
+                    uint8_t *mask, FgEntry *fg, unsigned long long *fg_count, int *d_status, cudaStream_t s);
 // ---- ccl.cu ----
 // Segments of a per-substack scan: substack s scans len[s] counts starting at off[s];
 // chk[s] is its offset in the chunk-sum scratch (one slot per 1024 counts).
@@ -89,6 +104,12 @@ void launch_regions(const Sub *d_subs, int nsub, int64_t max_n, const ScanSeg &v
                     const int32_t *labels, const uint32_t *root_bits, const float *norm, const float *dog,
                     int32_t *rank, uint32_t *blk_counts, uint32_t *blk_offsets, uint32_t *chunk,
                     int64_t *d_num_regions, RegionAcc acc, int64_t slots, int *d_status, cudaStream_t s);
+// Accumulation from the fused sweep's foreground list instead of the mask and DoG.
+void launch_regions_fg(const Sub *d_subs, int nsub, int64_t max_n, int64_t max_fg, const ScanSeg &vseg,
+                       const int32_t *labels, const uint32_t *root_bits, const FgEntry *fg,
+                       const unsigned long long *fg_count, int32_t *rank, uint32_t *blk_counts,
+                       uint32_t *blk_offsets, uint32_t *chunk, int64_t *d_num_regions, RegionAcc acc, int64_t slots,
+                       int *d_status, int num_sms, cudaStream_t s);
 void launch_finalize(const Sub *d_subs, int nsub, int64_t max_reg_cap, const ScanSeg &rseg,
                      const int64_t *d_num_regions, RegionAcc acc, int64_t slots, RegionOut out,
                      FilterParams fp, uint32_t *blk_counts, uint32_t *blk_offsets, uint32_t *chunk,

@@ -205,6 +205,51 @@ __global__ void __launch_bounds__(256) k_accumulate(const Sub *subs, const uint8
   run_flush(a, S, acc, slots);
 }
 
+// The same accumulation from the foreground list of the fused sweep: each thread takes
+// kFgChunk consecutive entries (neighbouring voxels of one tile row pair, so mostly one
+// region) and flushes a run whenever the region changes.
+constexpr int kFgChunk = 8;
+
+__global__ void __launch_bounds__(256) k_accumulate_fg(const Sub *subs, const FgEntry *fg,
+                                                       const unsigned long long *fg_count, const int32_t *labels,
+                                                       const int32_t *rank, RegionAcc acc, int64_t slots) {
+  const Sub S = subs[blockIdx.y];
+  const int64_t cnt = (int64_t)fg_count[blockIdx.y];
+  if (cnt > S.fg_cap) return;   // overflowed: the batch is redone without the fused sweep
+  const int W = S.W, H = S.H;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x * kFgChunk;
+  for (int64_t e0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * kFgChunk; e0 < cnt; e0 += stride) {
+    RunAcc a;
+    run_reset(a, -1);
+    const int64_t e1 = min(e0 + kFgChunk, cnt);
+    for (int64_t e = e0; e < e1; e++) {
+      const float4 *src = reinterpret_cast<const float4 *>(fg + S.fg + e);
+      const float4 q0 = __ldg(src), q1 = __ldg(src + 1);
+      const int32_t i = __float_as_int(q0.x);
+      const int32_t lab = labels[S.vox + i];
+      const int64_t r = rank[S.vox + lab];
+      if (r != a.r) {
+        run_flush(a, S, acc, slots);
+        run_reset(a, r);
+      }
+      const int x = i % W, y = (i / W) % H, z = i / (W * H);
+      a.count++;
+      a.max_ord = max(a.max_ord, f2ord(q0.y));
+      a.norm += to_fix(q0.y);
+      a.x += (unsigned long long)x;
+      a.y += (unsigned long long)y;
+      a.z += (unsigned long long)z;
+      a.h[0] += to_fix(q0.z);
+      a.h[1] += to_fix(q0.w);
+      a.h[2] += to_fix(q1.x);
+      a.h[3] += to_fix(q1.y);
+      a.h[4] += to_fix(q1.z);
+      a.h[5] += to_fix(q1.w);
+    }
+    run_flush(a, S, acc, slots);
+  }
+}
+
 // ------------------------------------------------------------------ eigen features
 // EigenvaluesKernel<float> (Eigenvalues.cu:19-96): Eberly's closed form in double on
 // the float region sums; structureness = l0^2 + l1^2 + l2^2, blobness = l2^2 / (l0*l1).
@@ -345,6 +390,23 @@ void launch_regions(const Sub *d_subs, int nsub, int64_t max_n, const ScanSeg &v
                                                                         acc, slots, d_status)));
   KLAUNCH("k_accumulate", s, (k_accumulate<<<dim3(ceil_div(max_n, kScanBlock), nsub), 256, 0, s>>>(d_subs, mask, labels, rank, norm, dog, acc,
                                                                 slots)));
+}
+
+void launch_regions_fg(const Sub *d_subs, int nsub, int64_t max_n, int64_t max_fg, const ScanSeg &vseg,
+                       const int32_t *labels, const uint32_t *root_bits, const FgEntry *fg,
+                       const unsigned long long *fg_count, int32_t *rank, uint32_t *blk_counts,
+                       uint32_t *blk_offsets, uint32_t *chunk, int64_t *d_num_regions, RegionAcc acc, int64_t slots,
+                       int *d_status, int num_sms, cudaStream_t s) {
+  launch_scan(vseg, nsub, blk_counts, blk_offsets, chunk, d_num_regions, 1, s);
+  KLAUNCH("k_rank", s, (k_rank<<<dim3(ceil_div(max_n, kScanBlock), nsub), 256, 0, s>>>(d_subs, root_bits, blk_offsets,
+                                                                                      rank, acc, slots, d_status)));
+  int64_t want = (int64_t)ceil_div(max_fg, 256 * kFgChunk);
+  const int64_t cap = (int64_t)8 * num_sms / (nsub > 0 ? nsub : 1) + 1;
+  if (want > cap) want = cap;
+  if (want < 1) want = 1;
+  const unsigned blocks = (unsigned)want;
+  KLAUNCH("k_accumulate_fg", s, (k_accumulate_fg<<<dim3(blocks, nsub), 256, 0, s>>>(d_subs, fg, fg_count, labels,
+                                                                                    rank, acc, slots)));
 }
 
 void launch_finalize(const Sub *d_subs, int nsub, int64_t max_reg_cap, const ScanSeg &rseg,

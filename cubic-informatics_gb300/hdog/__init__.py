@@ -23,6 +23,7 @@ MAIN_PATH = os.path.join(BUILD_DIR, "hdog_main")
 
 HDOG_OK, HDOG_ERR_ARG, HDOG_ERR_SHAPE, HDOG_ERR_CUDA, HDOG_ERR_IO = 0, 1, 2, 3, 4
 HDOG_ERR_PARAM, HDOG_ERR_CAPACITY, HDOG_ERR_TIMEOUT, HDOG_ERR_NOMEM = 5, 6, 7, 8
+HDOG_OPT_FUSED_SWEEP = 1
 
 # The 28-byte candidate record (FeatureVector, src/3D/utils.h:188-197).
 DT_LOCAL = np.dtype([
@@ -87,6 +88,7 @@ _SIGNATURES = {
     "hdog_run_stack": (ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.c_int, _P, ctypes.c_int64,
                                       ctypes.POINTER(ctypes.c_int64), _P]),
     "hdog_run_param_file": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int]),
+    "hdog_ctx_set_option": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int]),
     "hdog_timing_enable": (ctypes.c_int, [_P, ctypes.c_int]),
     "hdog_timing_read": (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_size_t]),
     "hdog_memcpy": (ctypes.c_int, [_P, _P, ctypes.c_size_t, _P]),
@@ -248,6 +250,10 @@ class Context:
     def _empty(self, dtype):
         import torch
         return torch.empty(self.shape, dtype=dtype, device="cuda:%d" % self.params.dev_id)
+
+    def set_fused_sweep(self, on):
+        """DoG + Hessian + PD in one z-sweep kernel (default) or as separate passes."""
+        check(lib().hdog_ctx_set_option(self._h, HDOG_OPT_FUSED_SWEEP, int(bool(on))))
 
     def timing(self, on=True):
         """Per-kernel CUDA-event timing of this context's launches."""

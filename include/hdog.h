@@ -140,6 +140,13 @@ int hdog_run_stack(hdog_ctx *ctx, const uint16_t *stack, int stack_on_device, in
    writes each dst_path (removed first, then appended per substack). */
 int hdog_run_param_file(const char *param_path, int verbose);
 
+/* ---- context options ---- */
+enum {
+  HDOG_OPT_FUSED_SWEEP = 1   /* 1 (default): DoG, Hessian and the PD test in one z-sweep kernel
+                                when the radii allow; 0: separate passes (same results) */
+};
+int hdog_ctx_set_option(hdog_ctx *ctx, int option, int value);
+
 /* ---- per-kernel timing (CUDA events on the launching stream) ---- */
 /* When on, every kernel launch of the context's calls is bracketed by two events. */
 int hdog_timing_enable(hdog_ctx *ctx, int on);

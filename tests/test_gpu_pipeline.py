@@ -122,3 +122,16 @@ def test_capacity_error_is_reported():
         rc = hdog.lib().hdog_run_substack(ctx._h, vol.ctypes.data, 0, D, 0, out.ctypes.data, 1,
                                           __import__("ctypes").byref(cnt), None)
         assert rc == hdog.HDOG_ERR_CAPACITY and cnt.value == n
+
+
+@pytest.mark.parametrize("W,H,D,dv", [(68, 45, 13, 13), (256, 96, 32, 20), (132, 20, 7, 5), (64, 16, 40, 40)])
+def test_fused_sweep_equals_separate_passes(W, H, D, dv):
+    vol = volume(W, H, D, n_nuclei=max(4, W * H * D // 8000), seed=W + H + D)
+    p = params(W, H, D, sigma_z_large=1.6, extra_depth_margin=0)
+    with hdog.Context(p) as ctx:
+        fused = ctx.run_substack(np.ascontiguousarray(vol[:dv]), dv, 3)
+        ctx.set_fused_sweep(False)
+        plain = ctx.run_substack(np.ascontiguousarray(vol[:dv]), dv, 3)
+    assert fused.tobytes() == plain.tobytes()
+    ref = orc.substack(orc.params_from(p), padded(vol, D, dv), dv, 3)[0]
+    assert_records_match(fused, ref, "fused %dx%dx%d" % (W, H, D))
