@@ -94,6 +94,7 @@ extern "C" int hdog_set_cuda_error(cudaError_t e, const char *what) {
 }
 
 extern "C" const char *hdog_last_error(void) { return g_last_error.c_str(); }
+extern "C" int hdog_set_error(int code, const char *what) { return fail(code, what); }
 extern "C" int hdog_abi_version(void) { return HDOG_ABI_VERSION; }
 
 #define TRY(expr)                          \

@@ -89,6 +89,7 @@ _SIGNATURES = {
                                       ctypes.POINTER(ctypes.c_int64), _P]),
     "hdog_run_param_file": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int]),
     "hdog_ctx_set_option": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int]),
+    "hdog_ccl_noalloc": (ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P]),
     "hdog_timing_enable": (ctypes.c_int, [_P, ctypes.c_int]),
     "hdog_timing_read": (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_size_t]),
     "hdog_memcpy": (ctypes.c_int, [_P, _P, ctypes.c_size_t, _P]),

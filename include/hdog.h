@@ -140,6 +140,19 @@ int hdog_run_stack(hdog_ctx *ctx, const uint16_t *stack, int stack_on_device, in
    writes each dst_path (removed first, then appended per substack). */
 int hdog_run_param_file(const char *param_path, int verbose);
 
+/* ---- labelling without any device allocation ----
+   No counterpart in the reference.  For callers that may not allocate device memory
+   themselves (a host framework that owns all device memory through its own allocator,
+   or a service with a fixed memory budget reserved at start-up): the same labels as
+   hdog_ccl for a mask of at most 2^22 voxels (width * height * depth), with all scratch
+   in one fixed 4.7 MB device array inside the library (per device, for the life of the
+   process).  Larger volumes return HDOG_ERR_SHAPE.  Calls share that array: calls that
+   overlap on the GPU (other streams or host threads) race; calls in sequence on one
+   stream do not.  The first call on a device looks up the array's device address with
+   that device current.  Synchronizes `stream` before returning. */
+int hdog_ccl_noalloc(const uint8_t *d_mask, int32_t *d_labels, int width, int height, int depth,
+                     void *stream);
+
 /* ---- context options ---- */
 enum {
   HDOG_OPT_FUSED_SWEEP = 1   /* 1 (default): DoG, Hessian and the PD test in one z-sweep kernel
