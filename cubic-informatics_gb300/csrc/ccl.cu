@@ -141,9 +141,66 @@ __device__ __forceinline__ bool leaves_tile(const Sub &S, const CclTile &T, int 
   return !(in_vol && in_tile);
 }
 
+constexpr int kFgList = 12288;                // compact foreground list of a tile (37.5%)
+
+__device__ __forceinline__ uint32_t tile_scan(uint32_t v, uint32_t *total) {
+  __shared__ uint32_t ws[kCclThreads / 32 + 1];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  uint32_t inc = v;
+  for (int d = 1; d < 32; d <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, inc, d);
+    if (lane >= d) inc += y;
+  }
+  if (lane == 31) ws[w] = inc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t run = 0;
+    for (int k = 0; k < kCclThreads / 32; k++) { const uint32_t c = ws[k]; ws[k] = run; run += c; }
+    ws[kCclThreads / 32] = run;
+  }
+  __syncthreads();
+  const uint32_t r = ws[w] + inc - v;
+  *total = ws[kCclThreads / 32];
+  __syncthreads();
+  return r;
+}
+
+// Union of tile voxel lt with its backward neighbours inside the tile; counts the
+// foreground edges that leave the tile and, when `emit`, writes them from slot *base.
+__device__ __forceinline__ int tile_voxel_edges(const Sub &S, const CclTile &T, uint16_t *lab, const uint8_t *m,
+                                                int lt, bool do_union, bool emit, int2 *edges,
+                                                unsigned long long *base) {
+  const int lx = lt % kTX, ly = (lt / kTX) % kTY, lz = lt / (kTX * kTY);
+  const int x = T.x0 + lx, y = T.y0 + ly, z = T.z0 + lz;
+  const int64_t WH = (int64_t)S.W * S.H;
+  const int64_t g = z * WH + (int64_t)y * S.W + x;
+  int n_cross = 0;
+  for (int o = 0; o < 13; o++) {
+    int dz, dy, dx;
+    back_offset(o, dz, dy, dx);
+    if (!leaves_tile(S, T, x, y, z, lx, ly, lz, dz, dy, dx)) {
+      if (!do_union) continue;
+      const int ln = lt + (dz * kTY + dy) * kTX + dx;
+      const uint16_t pn = lab[ln];
+      if (pn != kBg && pn != lab[lt]) sunion(lab, lt, ln);
+    } else {
+      const int64_t gn = g + dz * WH + dy * (int64_t)S.W + dx;
+      if (gn >= 1 && m[gn]) {
+        if (emit) {
+          if ((int64_t)*base < S.edge_cap) edges[S.edge + *base] = make_int2((int32_t)g, (int32_t)gn);
+          (*base)++;
+        }
+        n_cross++;
+      }
+    }
+  }
+  return n_cross;
+}
+
 __global__ void __launch_bounds__(kCclThreads) k_ccl_local(const Sub *subs, const uint8_t *mask, int32_t *labels,
                                                           int2 *edges, unsigned long long *edge_count) {
-  extern __shared__ uint16_t lab[];   // kTileVox entries
+  extern __shared__ uint16_t lab[];   // kTileVox parents, then kFgList foreground indices
+  uint16_t *fgl = lab + kTileVox;
   const Sub S = subs[blockIdx.y];
   CclTile T;
   if (!ccl_tile(S, blockIdx.x, T)) return;
@@ -155,7 +212,8 @@ __global__ void __launch_bounds__(kCclThreads) k_ccl_local(const Sub *subs, cons
   const bool row_ok = y < S.H;
   const bool vec = row_ok && x + 3 < S.W && (S.W % 4 == 0) &&
                    ((reinterpret_cast<uintptr_t>(m + (int64_t)y * S.W + x) & 3) == 0);
-  // 1. foreground -> own tile index, background -> kBg
+  // 1. foreground -> own tile index, background -> kBg; count this thread's foreground
+  uint32_t nfg = 0;
   for (int lz = 0; lz < kTZ; lz++) {
     const int lt = (lz * kTY + ly) * kTX + lx0;
     uint32_t w = 0;
@@ -174,33 +232,46 @@ __global__ void __launch_bounds__(kCclThreads) k_ccl_local(const Sub *subs, cons
     v.y = ((w >> 8) & 0xFFu) ? (uint16_t)(lt + 1) : kBg;
     v.z = ((w >> 16) & 0xFFu) ? (uint16_t)(lt + 2) : kBg;
     v.w = (w >> 24) ? (uint16_t)(lt + 3) : kBg;
+    nfg += (v.x != kBg) + (v.y != kBg) + (v.z != kBg) + (v.w != kBg);
     *reinterpret_cast<ushort4 *>(&lab[lt]) = v;
   }
-  __syncthreads();
-  // 2. unions along edges inside the tile; count the edges that leave it
-  int n_cross = 0;
-  for (int lz = 0; lz < T.tz; lz++) {
-    const int z = T.z0 + lz;
-    for (int k = 0; k < 4; k++) {
-      const int lt = (lz * kTY + ly) * kTX + lx0 + k;
-      if (lab[lt] == kBg) continue;
-      const int lx = lx0 + k;
-      for (int o = 0; o < 13; o++) {
-        int dz, dy, dx;
-        back_offset(o, dz, dy, dx);
-        if (!leaves_tile(S, T, x + k, y, z, lx, ly, lz, dz, dy, dx)) {
-          const int ln = lt + (dz * kTY + dy) * kTX + dx;
-          if (lab[ln] != kBg) sunion(lab, lt, ln);
-        } else {
-          const int64_t g = z * WH + (int64_t)y * S.W + x + k;
-          const int64_t gn = g + dz * WH + dy * (int64_t)S.W + dx;
-          if (gn >= 1 && m[gn]) n_cross++;
-        }
+  // 2. compact list of foreground tile indices (block scan of the per-thread counts)
+  uint32_t total;
+  const uint32_t off = tile_scan(nfg, &total);
+  const bool listed = total <= (uint32_t)kFgList;
+  if (listed) {
+    uint32_t o = off;
+    for (int lz = 0; lz < T.tz; lz++)
+      for (int k = 0; k < 4; k++) {
+        const int lt = (lz * kTY + ly) * kTX + lx0 + k;
+        if (lab[lt] != kBg) fgl[o++] = (uint16_t)lt;
       }
-    }
   }
   __syncthreads();
-  // 3. reserve edge slots (one atomic per warp), write labels and edges
+  // 3. unions inside the tile, foreground voxels spread evenly over the threads
+  int n_cross = 0;
+  if (listed) {
+    for (uint32_t i = t; i < total; i += kCclThreads)
+      n_cross += tile_voxel_edges(S, T, lab, m, fgl[i], true, false, nullptr, nullptr);
+  } else {
+    for (int lz = 0; lz < T.tz; lz++)
+      for (int k = 0; k < 4; k++) {
+        const int lt = (lz * kTY + ly) * kTX + lx0 + k;
+        if (lab[lt] != kBg) n_cross += tile_voxel_edges(S, T, lab, m, lt, true, false, nullptr, nullptr);
+      }
+  }
+  __syncthreads();
+  // 4. final roots stored in place (no union runs any more, so only roots are stored)
+  if (listed) {
+    for (uint32_t i = t; i < total; i += kCclThreads) lab[fgl[i]] = (uint16_t)sroot(lab, fgl[i]);
+  } else {
+    for (int lz = 0; lz < T.tz; lz++)
+      for (int k = 0; k < 4; k++) {
+        const int lt = (lz * kTY + ly) * kTX + lx0 + k;
+        if (lab[lt] != kBg) lab[lt] = (uint16_t)sroot(lab, lt);
+      }
+  }
+  // 5. reserve edge slots (one atomic per warp) and emit the edges in the same order
   const int lane = threadIdx.x & 31;
   int incl = n_cross;
   for (int d = 1; d < 32; d <<= 1) {
@@ -211,30 +282,32 @@ __global__ void __launch_bounds__(kCclThreads) k_ccl_local(const Sub *subs, cons
   unsigned long long base = 0;
   if (lane == 31 && warp_total) base = atomicAdd(&edge_count[blockIdx.y], (unsigned long long)warp_total);
   base = __shfl_sync(0xFFFFFFFFu, base, 31) + (unsigned long long)(incl - n_cross);
+  if (n_cross) {
+    if (listed) {
+      for (uint32_t i = t; i < total; i += kCclThreads)
+        tile_voxel_edges(S, T, lab, m, fgl[i], false, true, edges, &base);
+    } else {
+      for (int lz = 0; lz < T.tz; lz++)
+        for (int k = 0; k < 4; k++) {
+          const int lt = (lz * kTY + ly) * kTX + lx0 + k;
+          if (lab[lt] != kBg) tile_voxel_edges(S, T, lab, m, lt, false, true, edges, &base);
+        }
+    }
+  }
+  __syncthreads();
+  // 6. labels: tile root -> its global index, background -> 0 (whole rows, vector stores)
   if (!row_ok) return;
   int32_t *L = labels + S.vox;
   for (int lz = 0; lz < T.tz; lz++) {
-    const int z = T.z0 + lz;
-    const int64_t g = z * WH + (int64_t)y * S.W + x;
+    const int64_t g = (T.z0 + lz) * WH + (int64_t)y * S.W + x;
+    const ushort4 v = *reinterpret_cast<const ushort4 *>(&lab[(lz * kTY + ly) * kTX + lx0]);
+    const uint16_t r4[4] = {v.x, v.y, v.z, v.w};
     int32_t out[4];
     for (int k = 0; k < 4; k++) {
-      const int lt = (lz * kTY + ly) * kTX + lx0 + k;
-      out[k] = 0;
-      if (lab[lt] == kBg) continue;
-      const int r = sroot(lab, lt);
-      const int rx = r % kTX, ry = (r / kTX) % kTY, rz = r / (kTX * kTY);
-      out[k] = (int32_t)((T.z0 + rz) * WH + (int64_t)(T.y0 + ry) * S.W + T.x0 + rx);
-      if (n_cross == 0) continue;
-      for (int o = 0; o < 13; o++) {
-        int dz, dy, dx;
-        back_offset(o, dz, dy, dx);
-        if (!leaves_tile(S, T, x + k, y, z, lx0 + k, ly, lz, dz, dy, dx)) continue;
-        const int64_t gn = g + k + dz * WH + dy * (int64_t)S.W + dx;
-        if (gn >= 1 && m[gn]) {
-          if ((int64_t)base < S.edge_cap) edges[S.edge + base] = make_int2((int32_t)(g + k), (int32_t)gn);
-          base++;
-        }
-      }
+      const int r = r4[k];
+      out[k] = r == kBg ? 0
+                        : (int32_t)((T.z0 + r / (kTX * kTY)) * WH + (int64_t)(T.y0 + (r / kTX) % kTY) * S.W + T.x0 +
+                                    r % kTX);
     }
     if (vec) {
       *reinterpret_cast<int4 *>(L + g) = make_int4(out[0], out[1], out[2], out[3]);
@@ -350,7 +423,7 @@ void launch_ccl(const Sub *d_subs, int nsub, int max_w, int max_h, int max_d, in
                 uint32_t *blk_counts, int *d_status, int num_sms, cudaStream_t s) {
   const int64_t tiles = (int64_t)ceil_div(max_w, kTX) * ceil_div(max_h, kTY) * ceil_div(max_d, kTZ);
   cudaMemsetAsync(edge_count, 0, nsub * sizeof(unsigned long long), s);
-  const int smem = kTileVox * (int)sizeof(uint16_t);
+  const int smem = (kTileVox + kFgList) * (int)sizeof(uint16_t);
   cudaFuncSetAttribute(k_ccl_local, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   KLAUNCH("k_ccl_local", s, (k_ccl_local<<<dim3((unsigned)tiles, nsub), kCclThreads, smem, s>>>(
                                 d_subs, mask, labels, edges, edge_count)));

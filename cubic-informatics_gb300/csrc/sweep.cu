@@ -228,39 +228,66 @@ __global__ void __launch_bounds__(kSweepThreads, 1)
       bool fgv[2] = {false, false};
       if (t < kSX * (kSY / 2)) {
         const int hx0 = t % kSX, hy0 = 2 * (t / kSX);
-        for (int u = 0; u < 2; u++) {
-          const int lx = hx0, ly = hy0 + u;
-          const int X = x0 + lx, Y = y0 + ly;
-          if (X >= W || Y >= H) continue;
-          const int ex = lx + 2, ey = ly + 2;
-          auto Dv = [&](int ddx, int ddy, int ddz) -> float {
-            return ring[((zh + ddz + 5) % 5) * kEY * kEX + (ey + ddy) * kEX + (ex + ddx)];
-          };
-          auto in_vol = [&](int ddx, int ddy, int ddz) -> bool {
-            const int xx = X + ddx, yy = Y + ddy, zz = zh + ddz;
-            return xx >= 0 && xx < W && yy >= 0 && yy < H && zz >= 0 && zz < D;
-          };
-          auto GX = [&](int ddx, int ddy, int ddz) -> float {
-            return in_vol(ddx, ddy, ddz) ? cdiff(Dv(ddx + 1, ddy, ddz), Dv(ddx - 1, ddy, ddz)) : 0.0f;
-          };
-          auto GY = [&](int ddx, int ddy, int ddz) -> float {
-            return in_vol(ddx, ddy, ddz) ? cdiff(Dv(ddx, ddy + 1, ddz), Dv(ddx, ddy - 1, ddz)) : 0.0f;
-          };
-          auto GZ = [&](int ddz) -> float {
-            return in_vol(0, 0, ddz) ? cdiff(Dv(0, 0, ddz + 1), Dv(0, 0, ddz - 1)) : 0.0f;
-          };
-          float *h = hv[u];
-          h[0] = cdiff(GX(1, 0, 0), GX(-1, 0, 0));
-          h[1] = cdiff(GX(0, 1, 0), GX(0, -1, 0));
-          h[2] = cdiff(GX(0, 0, 1), GX(0, 0, -1));
-          h[3] = cdiff(GY(0, 1, 0), GY(0, -1, 0));
-          h[4] = cdiff(GY(0, 0, 1), GY(0, 0, -1));
-          h[5] = cdiff(GZ(1), GZ(-1));
-          const bool pd = pd_test(h[0], h[1], h[2], h[3], h[4], h[5]);
-          idx[u] = zh * WH + (int64_t)Y * W + X;
-          mask[S.vox + idx[u]] = pd ? 1 : 0;
-          fgv[u] = pd && idx[u] != 0;
-          nfg += fgv[u];
+        // tiles whose every voxel has all in-plane neighbours inside the volume take the
+        // fast path: only the z neighbours can fall outside
+        const bool interior = x0 >= 1 && x0 + kSX < W && y0 >= 1 && y0 + kSY < H;
+        if (interior) {
+          const float *P0 = ring + (zh % 5) * kEY * kEX;
+          const float *P1 = ring + ((zh + 1) % 5) * kEY * kEX;
+          const float *P2 = ring + ((zh + 2) % 5) * kEY * kEX;
+          const float *M1 = ring + ((zh + 4) % 5) * kEY * kEX;
+          const float *M2 = ring + ((zh + 3) % 5) * kEY * kEX;
+          const bool zup = zh + 1 < D, zdn = zh >= 1;
+          for (int u = 0; u < 2; u++) {
+            const int c = (hy0 + u + 2) * kEX + (hx0 + 2);
+            float *h = hv[u];
+            h[0] = cdiff(cdiff(P0[c + 2], P0[c]), cdiff(P0[c], P0[c - 2]));
+            h[1] = cdiff(cdiff(P0[c + kEX + 1], P0[c + kEX - 1]), cdiff(P0[c - kEX + 1], P0[c - kEX - 1]));
+            h[2] = cdiff(zup ? cdiff(P1[c + 1], P1[c - 1]) : 0.0f, zdn ? cdiff(M1[c + 1], M1[c - 1]) : 0.0f);
+            h[3] = cdiff(cdiff(P0[c + 2 * kEX], P0[c]), cdiff(P0[c], P0[c - 2 * kEX]));
+            h[4] = cdiff(zup ? cdiff(P1[c + kEX], P1[c - kEX]) : 0.0f, zdn ? cdiff(M1[c + kEX], M1[c - kEX]) : 0.0f);
+            h[5] = cdiff(zup ? cdiff(P2[c], P0[c]) : 0.0f, zdn ? cdiff(P0[c], M2[c]) : 0.0f);
+            const bool pd = pd_test(h[0], h[1], h[2], h[3], h[4], h[5]);
+            idx[u] = zh * WH + (int64_t)(y0 + hy0 + u) * W + (x0 + hx0);
+            mask[S.vox + idx[u]] = pd ? 1 : 0;
+            fgv[u] = pd && idx[u] != 0;
+            nfg += fgv[u];
+          }
+        } else {
+          for (int u = 0; u < 2; u++) {
+            const int lx = hx0, ly = hy0 + u;
+            const int X = x0 + lx, Y = y0 + ly;
+            if (X >= W || Y >= H) continue;
+            const int ex = lx + 2, ey = ly + 2;
+            auto Dv = [&](int ddx, int ddy, int ddz) -> float {
+              return ring[((zh + ddz + 5) % 5) * kEY * kEX + (ey + ddy) * kEX + (ex + ddx)];
+            };
+            auto in_vol = [&](int ddx, int ddy, int ddz) -> bool {
+              const int xx = X + ddx, yy = Y + ddy, zz = zh + ddz;
+              return xx >= 0 && xx < W && yy >= 0 && yy < H && zz >= 0 && zz < D;
+            };
+            auto GX = [&](int ddx, int ddy, int ddz) -> float {
+              return in_vol(ddx, ddy, ddz) ? cdiff(Dv(ddx + 1, ddy, ddz), Dv(ddx - 1, ddy, ddz)) : 0.0f;
+            };
+            auto GY = [&](int ddx, int ddy, int ddz) -> float {
+              return in_vol(ddx, ddy, ddz) ? cdiff(Dv(ddx, ddy + 1, ddz), Dv(ddx, ddy - 1, ddz)) : 0.0f;
+            };
+            auto GZ = [&](int ddz) -> float {
+              return in_vol(0, 0, ddz) ? cdiff(Dv(0, 0, ddz + 1), Dv(0, 0, ddz - 1)) : 0.0f;
+            };
+            float *h = hv[u];
+            h[0] = cdiff(GX(1, 0, 0), GX(-1, 0, 0));
+            h[1] = cdiff(GX(0, 1, 0), GX(0, -1, 0));
+            h[2] = cdiff(GX(0, 0, 1), GX(0, 0, -1));
+            h[3] = cdiff(GY(0, 1, 0), GY(0, -1, 0));
+            h[4] = cdiff(GY(0, 0, 1), GY(0, 0, -1));
+            h[5] = cdiff(GZ(1), GZ(-1));
+            const bool pd = pd_test(h[0], h[1], h[2], h[3], h[4], h[5]);
+            idx[u] = zh * WH + (int64_t)Y * W + X;
+            mask[S.vox + idx[u]] = pd ? 1 : 0;
+            fgv[u] = pd && idx[u] != 0;
+            nfg += fgv[u];
+          }
         }
       }
       // warp-aggregated append to the foreground list
