@@ -39,13 +39,13 @@ WORKLOAD = ("camera stack uint16 2560x2160x128, 60k nuclei (10% touching pairs),
             "radius_norm (20,5)")
 
 # Compulsory bytes per processed voxel of each kernel's own inputs and outputs (each
-# array read once, written once).  Stage totals follow the path's algorithmic bytes:
-# normalize 6, DoG 8, Hessian+mask 5, CCL 5, features 12 (sparse terms excluded).
+# array read once, written once; sparse foreground-list and region traffic excluded).
+# Stage totals: normalize 56 (five passes), DoG 8, Hessian + mask 5, CCL 5, features ~0.
 KERNEL_BYTES_PER_VOXEL = {
-    "k_minmax_z": 2 + 4, "k_minmax_x": 4 + 4, "k_minmax_y": 4 + 4, "k_box_x": 4 + 8, "k_box_y": 8 + 8,
-    "k_box_z_norm": 8 + 2 + 4, "k_conv_x": 4 + 8, "k_conv_y": 8 + 8, "k_conv_z_dog": 8 + 4,
-    "k_hessian_pd": 4 + 1, "k_ccl_init": 1 + 4, "k_ccl_merge": 1, "k_ccl_flatten": 1 + 0.125,
-    "k_rank": 0.125, "k_accumulate": 1,
+    "k_mm_z": 2 + 4, "k_mm_y": 4 + 4, "k_mm_x": 4 + 8, "k_box_y": 8 + 8, "k_box_z_norm": 8 + 2 + 4,
+    "k_dog_sweep": 4 + 4, "k_hess_sweep": 4 + 1, "k_dog_hess": 4 + 1, "k_conv_x": 4 + 8, "k_conv_y": 8 + 8, "k_conv_z_dog": 8 + 4,
+    "k_hessian_pd": 4 + 1, "k_ccl_local": 1 + 4, "k_ccl_flatten": 1 + 0.125, "k_rank": 0.125,
+    "k_accumulate": 1,
 }
 E2E_ALG_BYTES_PER_VOXEL = 6      # 2 B uint16 in + 4 B labels out per processed voxel
 
@@ -301,6 +301,9 @@ def main():
                 "h2d_bytes_per_step": unique * 2, "d2h_bytes_per_step": n_records * 28},
         "gpu_launches": int(launches),
         "kernel_ms_per_step": {k: round(v[1] / args.steps, 4) for k, v in sorted(ktimes.items(), key=lambda kv: -kv[1][1])},
+        # algorithmic GB/s of each dense kernel (its per-voxel bytes over its event time)
+        "kernel_alg_gbs": {k: round(KERNEL_BYTES_PER_VOXEL[k] * processed * v[0] / (v[1] * 1e-3) / 1e9, 1)
+                           for k, v in ktimes.items() if k in KERNEL_BYTES_PER_VOXEL and v[1] > 0},
         "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                      "alg_bytes_per_launch": alg, "avg_launch_ms": avg_ms,

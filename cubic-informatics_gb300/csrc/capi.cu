@@ -380,11 +380,14 @@ extern "C" int hdog_ctx_create(const hdog_params *p, int max_substacks, hdog_ctx
 }
 
 // ------------------------------------------------------------------ batch helpers
-static FilterParams filter_of(const hdog_params &p) {
+// all_eigen: eigen features for every region (the stage API returns them), else only
+// for the regions that become records.
+static FilterParams filter_of(const hdog_params &p, bool all_eigen = false) {
   FilterParams f;
   f.left = p.left_margin; f.right = p.right_margin; f.top = p.top_margin; f.bottom = p.bottom_margin;
   f.min_size = p.min_size;
   f.is_ave_mode = p.is_ave_mode;
+  f.all_eigen = all_eigen ? 1 : 0;
   return f;
 }
 
@@ -413,6 +416,14 @@ static void set_sub(hdog_ctx *c, int s, const uint16_t *src, int depth_valid, in
   c->h_seg[5 * ms + s] = (int64_t)s * c->nchk;
 }
 
+// Whether every substack's input starts on an 8-byte boundary (vector loads of four
+// uint16 in the z min/max pass).
+static bool srcs_aligned8(const hdog_ctx *c, int nsub) {
+  for (int s = 0; s < nsub; s++)
+    if (reinterpret_cast<uintptr_t>(c->h_subs[s].src) & 7) return false;
+  return true;
+}
+
 static int upload_subs(hdog_ctx *c, int nsub, cudaStream_t st) {
   const int ms = c->max_sub;
   HDOG_CUDA_TRY(cudaMemcpyAsync(c->d_subs, c->h_subs, nsub * sizeof(Sub), cudaMemcpyHostToDevice, st));
@@ -433,25 +444,22 @@ static ScanSeg rseg_of(hdog_ctx *c) {
 // Normalization of nsub substacks (descriptors already uploaded): src -> out_norm.
 static void enqueue_normalize(hdog_ctx *c, int nsub, float *out_norm, cudaStream_t st) {
   const hdog_params &p = c->p;
-  const int plane = c->W * c->H;
-  const int64_t rows = (int64_t)c->H * c->D;
   if (p.radius_norm_xy == 0 || p.radius_norm_z == 0) {
     launch_copy_norm(c->d_subs, nsub, c->nvox, (float)p.min_intensity, out_norm, st);
     return;
   }
-  // min/max (exact): z from the raw slices, then x, then y; packed u32 in fb's halves
+  // min/max (exact) z -> y -> x, box means x -> y -> z; packed u32 in fb's halves
   uint32_t *ma = reinterpret_cast<uint32_t *>(c->fb);
   uint32_t *mb = ma + (int64_t)c->max_sub * c->nvox;
-  launch_minmax_z(c->d_subs, nsub, plane, p.radius_norm_z, ma, st);
-  launch_minmax_x(c->d_subs, nsub, rows, c->W, p.radius_norm_xy, ma, mb, st);
-  launch_minmax_y(c->d_subs, nsub, c->W, c->H, c->D, p.radius_norm_xy, mb, ma, st);
-  // box means in the reference order x -> y -> z, then the normalization
-  launch_box_x(c->d_subs, nsub, rows, c->W, p.radius_norm_xy, ma, c->fa, st);
-  launch_box_y(c->d_subs, nsub, c->W, c->H, c->D, p.radius_norm_xy, c->fa, c->fb, st);
-  launch_box_z_norm(c->d_subs, nsub, plane, p.radius_norm_z, (float)p.min_intensity, c->fb, out_norm, st);
+  launch_normalize(c->d_subs, nsub, c->W, c->H, c->D, p.radius_norm_xy, p.radius_norm_z, (float)p.min_intensity,
+                   srcs_aligned8(c, nsub), ma, mb, c->fa, c->fb, out_norm, st);
 }
 
+// DoG volume: the radius-specialised z-sweep where it applies (bit-identical), else the
+// three separate passes.
 static void enqueue_dog(hdog_ctx *c, int nsub, const float *norm, float *dog, cudaStream_t st) {
+  if (c->use_sweep && launch_dog_sweep(c->d_subs, nsub, c->W, c->H, c->D, c->taps, norm, dog, c->status, c->max_smem, st))
+    return;
   launch_dog(c->d_subs, nsub, c->W, c->H, c->D, (int64_t)c->H * c->D, c->taps, norm, c->fa, c->fb, dog, st);
 }
 
@@ -459,7 +467,8 @@ static void enqueue_dog(hdog_ctx *c, int nsub, const float *norm, float *dog, cu
 // region numbering and accumulation, features and record compaction.
 static void enqueue_after_norm(hdog_ctx *c, int nsub, bool fused, cudaStream_t st) {
   if (fused) {
-    launch_dog_hess(c->d_subs, nsub, c->W, c->H, c->D, c->taps, c->norm, c->mask, c->fg, c->fg_count, c->status, st);
+    launch_dog_hess(c->d_subs, nsub, c->W, c->H, c->D, c->taps, c->norm, c->dog, c->mask, c->fg, c->fg_count,
+                    c->status, st);
   } else {
     enqueue_dog(c, nsub, c->norm, c->dog, st);
     launch_hessian_pd(c->d_subs, nsub, c->W, c->H, c->D, c->dog, c->mask, nullptr, st);
@@ -503,8 +512,8 @@ static int run_batch(hdog_ctx *c, int nsub, cudaStream_t st) {
   if (c->p.erosion_radius_xy > 0 || c->p.erosion_radius_z > 0) {
     // opt-in regional erosion of the input (the reference compiles Erosion3DFilter but
     // never calls it); the eroded substacks replace the inputs in c->img
-    launch_erosion(c->d_subs, nsub, c->W, c->H, c->D, (int64_t)c->H * c->D, c->p.erosion_radius_xy,
-                   c->p.erosion_radius_z, nullptr, reinterpret_cast<uint16_t *>(c->fa), c->img, st);
+    launch_erosion(c->d_subs, nsub, c->W, c->H, c->D, c->p.erosion_radius_xy, c->p.erosion_radius_z,
+                   srcs_aligned8(c, nsub), reinterpret_cast<uint32_t *>(c->fa), c->img, st);
     for (int s = 0; s < nsub; s++) {
       c->h_subs[s].src = c->img + (int64_t)s * c->nvox;
       c->h_subs[s].depth_valid = c->D;   // the eroded volume already carries the zero tail
@@ -622,8 +631,8 @@ extern "C" int hdog_regional_features(hdog_ctx *c, const int32_t *d_labels, cons
   int32_t *rank = reinterpret_cast<int32_t *>(c->fa);
   launch_regions(c->d_subs, 1, c->nvox, vseg_of(c), c->mask, d_labels, c->root_bits, d_norm, d_dog, rank,
                  c->blk_counts, c->blk_offsets, c->chunk, c->num_regions, c->acc, c->slots, c->status, st);
-  launch_finalize(c->d_subs, 1, c->reg_cap, rseg_of(c), c->num_regions, c->acc, c->slots, c->out, filter_of(c->p),
-                  c->blk_counts, c->blk_offsets, c->chunk, c->num_records, c->records, st);
+  launch_finalize(c->d_subs, 1, c->reg_cap, rseg_of(c), c->num_regions, c->acc, c->slots, c->out,
+                  filter_of(c->p, true), c->blk_counts, c->blk_offsets, c->chunk, c->num_records, c->records, st);
   HDOG_CUDA_TRY(cudaGetLastError());
   int64_t nr = 0;
   int status = 0;
@@ -650,8 +659,8 @@ extern "C" int hdog_erosion(hdog_ctx *c, const uint16_t *d_src, uint16_t *d_dst,
   cudaStream_t st = (cudaStream_t)stream;
   TRY(single_sub(c, d_src, st));
   // the erosion writes dst at S.vox = 0; its scratch is fa (two packed volumes)
-  launch_erosion(c->d_subs, 1, c->W, c->H, c->D, (int64_t)c->H * c->D, rxy, rz, nullptr,
-                 reinterpret_cast<uint16_t *>(c->fa), d_dst, st);
+  launch_erosion(c->d_subs, 1, c->W, c->H, c->D, rxy, rz, srcs_aligned8(c, 1), reinterpret_cast<uint32_t *>(c->fa),
+                 d_dst, st);
   HDOG_CUDA_TRY(cudaGetLastError());
   return HDOG_OK;
 }

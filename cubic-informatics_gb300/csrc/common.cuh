@@ -18,13 +18,12 @@ struct Geom {
 
 __device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
-// Packed u16 pair: low half = running min (erosion), high half = running max (dilation).
-__device__ __forceinline__ uint32_t pack_mm(uint32_t lo, uint32_t hi) { return lo | (hi << 16); }
-__device__ __forceinline__ uint32_t mm_combine(uint32_t a, uint32_t b) {
-  uint32_t lo = min(a & 0xFFFFu, b & 0xFFFFu);
-  uint32_t hi = max(a >> 16, b >> 16);
-  return lo | (hi << 16);
-}
+// Packed u16 pair of a running min / max: low half = min (erosion), high half =
+// 65535 - max (dilation), so a single __vminu2 combines both halves.
+__device__ __forceinline__ uint32_t pack_mm(uint32_t lo, uint32_t hi) { return lo | ((hi ^ 0xFFFFu) << 16); }
+__device__ __forceinline__ uint32_t mm_combine(uint32_t a, uint32_t b) { return __vminu2(a, b); }
+__device__ __forceinline__ uint32_t mm_lo(uint32_t v) { return v & 0xFFFFu; }
+__device__ __forceinline__ uint32_t mm_hi(uint32_t v) { return (v >> 16) ^ 0xFFFFu; }
 
 // Two IEEE round-to-nearest float adds / FMAs in one instruction (sm_100+ f32x2).  Each
 // lane rounds exactly like a scalar FADD / FFMA, so results equal the scalar chain.
@@ -116,8 +115,10 @@ __device__ __forceinline__ void hessian_at(const float *f, int W, int H, int D, 
 // atomics are associative, so the sums (and every record) are identical run to run.
 constexpr double kFixScale = 68719476736.0;          // 2^36
 constexpr double kFixInv = 1.0 / 68719476736.0;
+// v * 2^36 is exact in float (a power-of-two scaling), so rounding it to an integer
+// gives the same fixed-point value as the double product, without the FP64 pipe.
 __device__ __forceinline__ unsigned long long to_fix(float v) {
-  return (unsigned long long)__double2ll_rn((double)v * kFixScale);
+  return (unsigned long long)__float2ll_rn(v * 68719476736.0f);
 }
 __host__ __device__ __forceinline__ double from_fix(unsigned long long v) { return (double)(long long)v * kFixInv; }
 

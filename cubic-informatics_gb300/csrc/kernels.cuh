@@ -53,27 +53,22 @@ struct FilterParams {
   int left, right, top, bottom;
   int min_size;
   int is_ave_mode;
+  int all_eigen;          // eigen features for every region, not only the kept ones
 };
 
 inline unsigned ceil_div(int64_t a, int64_t b) { return (unsigned)((a + b - 1) / b); }
 
 // ---- norm.cu ----
-void launch_minmax_z(const Sub *d_subs, int nsub, int max_plane, int rz, uint32_t *mm, cudaStream_t s);
-void launch_minmax_x(const Sub *d_subs, int nsub, int64_t max_rows, int max_w, int r,
-                     const uint32_t *in, uint32_t *out, cudaStream_t s);
-void launch_minmax_y(const Sub *d_subs, int nsub, int max_w, int max_h, int max_d, int r,
-                     const uint32_t *in, uint32_t *out, cudaStream_t s);
-void launch_box_x(const Sub *d_subs, int nsub, int64_t max_rows, int max_w, int r,
-                  const uint32_t *in, float2 *out, cudaStream_t s);
-void launch_box_y(const Sub *d_subs, int nsub, int max_w, int max_h, int max_d, int r,
-                  const float2 *in, float2 *out, cudaStream_t s);
-void launch_box_z_norm(const Sub *d_subs, int nsub, int max_plane, int rz, float min_intensity,
-                       const float2 *in, float *norm, cudaStream_t s);
+// ma, mb: packed u32 volumes; fa, fb: float2 volumes (ma/mb may alias fb's two halves).
+// src_aligned8: every substack's src is 8-byte aligned (four-column z loads).
+void launch_normalize(const Sub *d_subs, int nsub, int W, int H, int D, int rxy, int rz, float min_intensity,
+                      bool src_aligned8, uint32_t *ma, uint32_t *mb, float2 *fa, float2 *fb, float *norm,
+                      cudaStream_t s);
 void launch_copy_norm(const Sub *d_subs, int nsub, int64_t max_n, float min_intensity,
                       float *norm, cudaStream_t s);
-void launch_erosion(const Sub *d_subs, int nsub, int max_w, int max_h, int max_d, int64_t max_rows,
-                    int rxy, int rz, const uint16_t *src_override, uint16_t *tmp, uint16_t *dst,
-                    cudaStream_t s);
+// tmp: two packed u32 volumes of nsub substacks each; dst: uint16 (substack s at S.vox).
+void launch_erosion(const Sub *d_subs, int nsub, int W, int H, int D, int rxy, int rz, bool src_aligned8,
+                    uint32_t *tmp, uint16_t *dst, cudaStream_t s);
 // ---- dog.cu ----
 void launch_dog(const Sub *d_subs, int nsub, int max_w, int max_h, int max_d, int64_t max_rows,
                 const DogTaps &T, const float *norm, float2 *t0, float2 *t1, float *dog, cudaStream_t s);
@@ -83,8 +78,15 @@ void launch_hessian_pd(const Sub *d_subs, int nsub, int max_w, int max_h, int ma
 constexpr int kMaxSweepRxy = 12;
 size_t sweep_smem_bytes(int rxy);
 bool sweep_supported(const DogTaps &T, int W, int max_smem);
+// DoG volume by the radius-specialised z-sweep; false (nothing launched) when the radii
+// have no instantiation or the buffers do not suit TMA.
+bool launch_dog_sweep(const Sub *d_subs, int nsub, int W, int H, int D, const DogTaps &T, const float *norm,
+                      float *dog, int *d_status, int max_smem, cudaStream_t s);
+// DoG + Hessian + PD: the radius-specialised pair (norm -> dog -> mask + list) when the tap
+// radii have an instantiation, else the generic fused sweep (dog untouched).
 int launch_dog_hess(const Sub *d_subs, int nsub, int W, int H, int D, const DogTaps &T, const float *norm,
-                    uint8_t *mask, FgEntry *fg, unsigned long long *fg_count, int *d_status, cudaStream_t s);
+                    float *dog, uint8_t *mask, FgEntry *fg, unsigned long long *fg_count, int *d_status,
+                    cudaStream_t s);
 // ---- ccl.cu ----
 // Segments of a per-substack scan: substack s scans len[s] counts starting at off[s];
 // chk[s] is its offset in the chunk-sum scratch (one slot per 1024 counts).
@@ -115,7 +117,7 @@ void launch_finalize(const Sub *d_subs, int nsub, int64_t max_reg_cap, const Sca
                      FilterParams fp, uint32_t *blk_counts, uint32_t *blk_offsets, uint32_t *chunk,
                      int64_t *d_num_records, hdog_record *records, cudaStream_t s);
 
-constexpr int kMaxRadiusXY = 421;    // shared-memory bound of the min/max y pass
+constexpr int kMaxRadiusXY = 421;    // shared-memory bound of the min/max x and y passes
 constexpr int kScanBlock = 4096;     // voxels per block in the region scans (16 per thread)
 constexpr int kFinalizeBlock = 256;  // regions per block in finalize / record compaction
 

@@ -7,283 +7,346 @@
 //   ero_l = box mean of ero, dil_l = box mean of dil                 (nearest border)
 //   norm = I >= min_intensity ? (I - ero_l) / (dil_l - ero_l) : 0
 //
-// Min and max are exact, so they are computed in whatever order is cheapest: the z pass
-// first, straight from the raw slices, then x and y with a sparse-table (doubling)
-// sliding window, O(log r) per voxel instead of O(r).  Erosion and dilation travel
-// together as one packed u16 pair per voxel (low half min, high half max).
+// Min and max are exact, so they run in whatever order is cheapest; the box means must
+// round exactly like the reference, whose passes go x -> y -> z and each is the
+// sequential float sum `val = 0; for j in 0..2r: val += s[j]` times 1.0f/(2r+1).
+// Five passes, each one read and one write of the volume:
 //
-// The box means must round exactly like the reference, whose every pass is the
-// sequential float sum `val = 0; for j in 0..2r: val += s[j]` times 1.0f/(2r+1):
-//   x pass: the inputs are integers and every partial sum stays below 2^24 when
-//           2r+1 <= 256, so the float chain is exact and equals an integer prefix-sum
-//           difference; wider windows fall back to the literal chain;
-//   y, z:   the literal chain, erosion and dilation side by side in one f32x2 add.
+//   mm_z      uint16 -> packed u32     z window, four columns per thread
+//   mm_y      u32 -> u32               van Herk / Gil-Werman column window in smem
+//   mm_x_box  u32 -> float2            van Herk / Gil-Werman row window, then the x box
+//                                      sum as exact integer sliding sums (2r+1 <= 256:
+//                                      every partial sum of the reference's float chain
+//                                      is an integer below 2^24, hence exact)
+//   box_y     float2 -> float2         the literal y chain, erosion and dilation side by
+//                                      side, K outputs per thread from a register window
+//   box_z_norm float2 + uint16 -> float the literal z chain fused with the normalization
+//
+// Erosion and dilation travel as one packed u32 per voxel: low half the running min,
+// high half 65535 minus the running max, so one __vminu2 combines both.
 #include "kernels.cuh"
 
 namespace hdog {
 
+// pack_mm(0, 0): the value a zero-border position contributes
+constexpr uint32_t kZeroPacked = 0xFFFF0000u;
+
 // ---------------------------------------------------------------- z pass (min/max)
-// One thread per (x, y) column; slices at or past depth_valid read as zero (the zero
-// tail HDoG3D_main.cpp:166-169 writes for a short last substack).  BORDER: 0 nearest
+// VEC consecutive positions of the slice plane per thread (VEC 4: one 8-byte load of
+// four uint16 per slice).  Slices at or past depth_valid read as zero (the zero tail
+// HDoG3D_main.cpp:166-169 writes for a short last substack).  BORDER: 0 nearest
 // (normalization), 1 zero (erosion operator).
-template <int BORDER>
-__global__ void k_minmax_z(const Sub *subs, int rz, uint32_t *mm) {
+template <int BORDER, int VEC>
+__global__ void __launch_bounds__(256) k_mm_z(const Sub *subs, int rz, uint32_t *mm) {
   const Sub S = subs[blockIdx.y];
   const int64_t plane = (int64_t)S.W * S.H;
-  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t p = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * VEC;
   if (p >= plane) return;
+  const int D = S.D, dv = S.depth_valid;
   const uint16_t *src = S.src + p;
   uint32_t *out = mm + S.vox + p;
-  for (int z = 0; z < S.D; z++) {
-    uint32_t lo = 0xFFFFu, hi = 0u;
-    for (int j = -rz; j <= rz; j++) {
-      int zz = z + j;
-      uint32_t v;
-      if (BORDER == 1 && (zz < 0 || zz >= S.D)) {
-        v = 0;
-      } else {
-        zz = clampi(zz, 0, S.D - 1);
-        v = zz < S.depth_valid ? (uint32_t)__ldg(src + zz * plane) : 0u;
+  for (int z = 0; z < D; z++) {
+    int lo = z - rz, hi = z + rz;
+    // nearest border repeats the edge slice (no new value); a zero border, or a slice
+    // of the zero tail inside the window, adds a 0
+    bool zero = BORDER == 1 && (lo < 0 || hi >= D);
+    lo = max(lo, 0);
+    hi = min(hi, D - 1);
+    if (hi >= dv) zero = true;
+    hi = min(hi, dv - 1);
+    const uint16_t *q = src + (int64_t)lo * plane;
+    if (VEC == 4) {
+      uint32_t mn0 = 0xFFFFFFFFu, mn1 = 0xFFFFFFFFu, mx0 = 0u, mx1 = 0u;
+      for (int zz = lo; zz <= hi; zz++, q += plane) {
+        const uint2 v = __ldg(reinterpret_cast<const uint2 *>(q));
+        mn0 = __vminu2(mn0, v.x);
+        mx0 = __vmaxu2(mx0, v.x);
+        mn1 = __vminu2(mn1, v.y);
+        mx1 = __vmaxu2(mx1, v.y);
       }
-      lo = min(lo, v);
-      hi = max(hi, v);
+      if (zero) { mn0 = 0u; mn1 = 0u; }
+      const uint32_t n0 = ~mx0, n1 = ~mx1;
+      uint4 o;
+      o.x = __byte_perm(mn0, n0, 0x5410);
+      o.y = __byte_perm(mn0, n0, 0x7632);
+      o.z = __byte_perm(mn1, n1, 0x5410);
+      o.w = __byte_perm(mn1, n1, 0x7632);
+      *reinterpret_cast<uint4 *>(out + (int64_t)z * plane) = o;
+    } else {
+      uint32_t mn = 0xFFFFu, mx = 0u;
+      for (int zz = lo; zz <= hi; zz++, q += plane) {
+        const uint32_t v = __ldg(q);
+        mn = min(mn, v);
+        mx = max(mx, v);
+      }
+      out[(int64_t)z * plane] = pack_mm(zero ? 0u : mn, mx);
     }
-    out[z * plane] = pack_mm(lo, hi);
   }
 }
 
-// Sparse-table sliding min/max over a window of L = 2r+1 entries of a smem line.
-// buf0 holds n0 = count + 2r entries; after the call buf0 (or buf1) holds M_P, the
-// combine of P = 2^floor(log2 L) consecutive entries.  Returns the buffer holding M_P.
-__device__ __forceinline__ uint32_t *sparse_levels(uint32_t *buf0, uint32_t *buf1, int n0, int L,
-                                                   int tid, int nthreads, int stride) {
-  uint32_t *a = buf0, *b = buf1;
-  int n = n0;
-  for (int step = 1; 2 * step <= L; step *= 2) {
-    const int m = n - step;
-    for (int t = tid; t < m; t += nthreads) b[t * stride] = mm_combine(a[t * stride], a[(t + step) * stride]);
-    __syncthreads();
-    uint32_t *c = a; a = b; b = c;
-    n = m;
+// Van Herk / Gil-Werman over blocks of L entries of a smem line: g = running min from
+// each block's start (written to G), h = running min to each block's end (written over
+// A).  The window [t, t + L - 1] is then min(h[t], g[t + L - 1]).
+__device__ __forceinline__ void vhgw_chain(uint32_t *A, uint32_t *G, int i0, int i1, int step) {
+  uint32_t run = 0xFFFFFFFFu;
+  for (int i = i0; i < i1; i++) {
+    run = __vminu2(run, A[i * step]);
+    G[i * step] = run;
   }
-  return a;
-}
-
-// ---------------------------------------------------------------- x pass (min/max)
-constexpr int kRowSeg = 256;   // outputs per block along x
-
-template <int BORDER>
-__global__ void k_minmax_x(const Sub *subs, int r, const uint32_t *in, uint32_t *out) {
-  extern __shared__ uint32_t smx[];
-  const Sub S = subs[blockIdx.y];
-  const int segs = (S.W + kRowSeg - 1) / kRowSeg;
-  const int64_t rows = (int64_t)S.H * S.D;
-  const int64_t bid = blockIdx.x;
-  if (bid >= rows * segs) return;
-  const int64_t row = bid / segs;
-  const int x0 = (int)(bid % segs) * kRowSeg;
-  const int L = 2 * r + 1, n0 = kRowSeg + 2 * r;
-  uint32_t *b0 = smx, *b1 = smx + n0;
-  const uint32_t *line = in + S.vox + row * S.W;
-  for (int t = threadIdx.x; t < n0; t += blockDim.x) {
-    int x = x0 - r + t;
-    uint32_t v;
-    if (BORDER == 1 && (x < 0 || x >= S.W)) v = 0;
-    else v = line[clampi(x, 0, S.W - 1)];
-    b0[t] = v;
+  run = 0xFFFFFFFFu;
+  for (int i = i1 - 1; i >= i0; i--) {
+    run = __vminu2(run, A[i * step]);
+    A[i * step] = run;
   }
-  __syncthreads();
-  int P = 1;
-  while (2 * P <= L) P *= 2;
-  uint32_t *m = sparse_levels(b0, b1, n0, L, threadIdx.x, blockDim.x, 1);
-  const int t = threadIdx.x;
-  const int x = x0 + t;
-  if (x < S.W) out[S.vox + row * S.W + x] = mm_combine(m[t], m[t + L - P]);
 }
 
 // ---------------------------------------------------------------- y pass (min/max)
-constexpr int kColTileX = 32;    // columns per block
-constexpr int kColTileY = 64;    // output rows per block
-
+// A block owns 32 columns x ty output rows of one slice; it stages rows
+// [y0 - r, y0 + ty + r) (border rule applied) and runs one chain per (column, block).
 template <int BORDER>
-__global__ void k_minmax_y(const Sub *subs, int r, const uint32_t *in, uint32_t *out) {
+__global__ void __launch_bounds__(256) k_mm_y(const Sub *subs, int r, int ty, const uint32_t *in, uint32_t *out) {
   extern __shared__ uint32_t smy[];
   const Sub S = subs[blockIdx.y];
-  const int tx_n = (S.W + kColTileX - 1) / kColTileX, ty_n = (S.H + kColTileY - 1) / kColTileY;
+  const int W = S.W, H = S.H;
+  const int tx_n = (W + 31) / 32, ty_n = (H + ty - 1) / ty;
   const int64_t bid = blockIdx.x;
   if (bid >= (int64_t)tx_n * ty_n * S.D) return;
   const int z = (int)(bid / ((int64_t)tx_n * ty_n));
   const int rem = (int)(bid % ((int64_t)tx_n * ty_n));
-  const int x0 = (rem % tx_n) * kColTileX, y0 = (rem / tx_n) * kColTileY;
-  const int L = 2 * r + 1, n0 = kColTileY + 2 * r;
-  uint32_t *b0 = smy, *b1 = smy + n0 * kColTileX;
-  const int lx = threadIdx.x, ly = threadIdx.y;
-  const int x = x0 + lx;
-  const uint32_t *sl = in + S.vox + (int64_t)z * S.W * S.H;
-  for (int t = ly; t < n0; t += blockDim.y) {
-    int y = y0 - r + t;
-    uint32_t v = 0;
-    if (x < S.W) {
-      if (BORDER == 1 && (y < 0 || y >= S.H)) v = 0;
-      else v = sl[(int64_t)clampi(y, 0, S.H - 1) * S.W + x];
-    }
-    b0[t * kColTileX + lx] = v;
+  const int x0 = (rem % tx_n) * 32, y0 = (rem / tx_n) * ty;
+  const int L = 2 * r + 1, n0 = ty + 2 * r;
+  uint32_t *A = smy, *G = smy + n0 * 32;
+  const int c = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int x = x0 + c;
+  const bool xin = x < W;
+  const uint32_t *sl = in + S.vox + (int64_t)z * W * H + (xin ? x : 0);
+  for (int i = w; i < n0; i += nw) {
+    const int y = y0 - r + i;
+    uint32_t v;
+    if (BORDER == 1 && (y < 0 || y >= H)) v = kZeroPacked;
+    else v = sl[(int64_t)clampi(y, 0, H - 1) * W];
+    A[i * 32 + c] = v;
   }
   __syncthreads();
-  // Doubling along y: each (lx, t) pair handled by thread (lx, t mod blockDim.y).
-  uint32_t *a = b0, *b = b1;
-  int n = n0, P = 1;
-  for (int step = 1; 2 * step <= L; step *= 2) {
-    const int m = n - step;
-    for (int t = ly; t < m; t += blockDim.y)
-      b[t * kColTileX + lx] = mm_combine(a[t * kColTileX + lx], a[(t + step) * kColTileX + lx]);
-    __syncthreads();
-    uint32_t *c = a; a = b; b = c;
-    n = m;
-    P = 2 * step;
+  const int nb = (n0 + L - 1) / L;
+  for (int b = w; b < nb; b += nw) vhgw_chain(A + c, G + c, b * L, min(b * L + L, n0), 32);
+  __syncthreads();
+  if (!xin) return;
+  uint32_t *o = out + S.vox + (int64_t)z * W * H + x;
+  const int tn = min(ty, H - y0);
+  for (int t = w; t < tn; t += nw) o[(int64_t)(y0 + t) * W] = __vminu2(A[t * 32 + c], G[(t + 2 * r) * 32 + c]);
+}
+
+// ---------------------------------------------------------------- x pass (min/max + box)
+// A block owns ry rows x tx outputs.  MODE 0: min/max window, then the exact x box sum
+// -> float2 (ero_x, dil_x); MODE 1: min window only -> uint16 (erosion result); MODE 2:
+// min/max window only -> packed u32 (followed by the float-chain box for 2r+1 > 256).
+constexpr int kBoxC = 16;   // box outputs per thread (sliding integer sums)
+
+template <int BORDER, int MODE>
+__global__ void __launch_bounds__(256) k_mm_x(const Sub *subs, int r, int ry, int tx, const uint32_t *in,
+                                              void *out) {
+  extern __shared__ uint32_t smx[];
+  const Sub S = subs[blockIdx.y];
+  const int W = S.W;
+  const int64_t rows = (int64_t)S.H * S.D;
+  const int segs = (W + tx - 1) / tx;
+  const int64_t bid = blockIdx.x;
+  if (bid >= ((rows + ry - 1) / ry) * segs) return;
+  const int64_t row0 = (bid / segs) * ry;
+  const int x0 = (int)(bid % segs) * tx;
+  const int hm = MODE == 0 ? r : 0;            // halo of the min/max result the box needs
+  const int n0 = tx + 2 * hm + 2 * r;          // staged entries per row
+  const int stride = n0 | 1;                   // odd: chains of neighbouring rows hit distinct banks
+  uint32_t *A = smx, *G = smx + ry * stride;
+  const int base = x0 - hm - r;                // x of A[row][0]
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5, nw = blockDim.x >> 5;
+  for (int rl = w; rl < ry; rl += nw) {
+    const int64_t row = min(row0 + rl, rows - 1);
+    const uint32_t *line = in + S.vox + row * W;
+    for (int i = lane; i < n0; i += 32) {
+      const int xx = base + i;
+      uint32_t v;
+      if (BORDER == 1 && (xx < 0 || xx >= W)) v = kZeroPacked;
+      else v = line[clampi(xx, 0, W - 1)];
+      A[rl * stride + i] = v;
+    }
   }
-  if (x >= S.W) return;
-  for (int t = ly; t < kColTileY; t += blockDim.y) {
-    const int y = y0 + t;
-    if (y < S.H) out[S.vox + ((int64_t)z * S.H + y) * S.W + x] =
-        mm_combine(a[t * kColTileX + lx], a[(t + L - P) * kColTileX + lx]);
+  __syncthreads();
+  const int L = 2 * r + 1;
+  const int nb = (n0 + L - 1) / L;
+  for (int ch = tid; ch < ry * nb; ch += blockDim.x) {
+    const int rl = ch % ry, b = ch / ry;
+    vhgw_chain(A + rl * stride, G + rl * stride, b * L, min(b * L + L, n0), 1);
+  }
+  __syncthreads();
+  const int tn = min(tx, W - x0);
+  if (MODE != 0) {
+    for (int rl = w; rl < ry; rl += nw) {
+      const int64_t row = row0 + rl;
+      if (row >= rows) break;
+      for (int k = lane; k < tn; k += 32) {
+        const uint32_t m = __vminu2(A[rl * stride + k], G[rl * stride + k + 2 * r]);
+        if (MODE == 1) reinterpret_cast<uint16_t *>(out)[S.vox + row * W + x0 + k] = (uint16_t)(m & 0xFFFFu);
+        else reinterpret_cast<uint32_t *>(out)[S.vox + row * W + x0 + k] = m;
+      }
+    }
+    return;
+  }
+  // m at x = x0 - r + k (nearest border: positions outside the row take the edge value)
+  const int nm = tx + 2 * r, mstride = nm | 1;
+  uint32_t *M = G + ry * stride;
+  for (int e = tid; e < ry * nm; e += blockDim.x) {
+    const int rl = e / nm, k = e % nm;
+    const int kc = clampi(x0 - r + k, 0, W - 1) - (x0 - r);
+    M[rl * mstride + k] = __vminu2(A[rl * stride + kc], G[rl * stride + kc + 2 * r]);
+  }
+  __syncthreads();
+  // sliding sums, C outputs per thread; results staged (over A and G) for coalesced stores
+  float2 *stage = reinterpret_cast<float2 *>(smx);
+  const int sstride = tx + 1;
+  const float inv = 1.0f / (float)L;
+  const uint32_t full = (uint32_t)L * 0xFFFFu;
+  const int nchunks = tx / kBoxC;
+  for (int ch = tid; ch < ry * nchunks; ch += blockDim.x) {
+    const int rl = ch % ry, c0 = (ch / ry) * kBoxC;
+    const uint32_t *m = M + rl * mstride + c0;
+    uint32_t slo = 0, shi = 0;
+    for (int j = 0; j < L; j++) {
+      const uint32_t v = m[j];
+      slo += v & 0xFFFFu;
+      shi += v >> 16;
+    }
+    float2 res[kBoxC];
+#pragma unroll
+    for (int t = 0; t < kBoxC; t++) {
+      res[t] = make_float2((float)slo * inv, (float)(full - shi) * inv);
+      if (t + 1 < kBoxC) {
+        const uint32_t vn = m[t + L], vo = m[t];
+        slo += (vn & 0xFFFFu) - (vo & 0xFFFFu);
+        shi += (vn >> 16) - (vo >> 16);
+      }
+    }
+    // A and G are free once M is built: the stage overwrites them while M is still read
+#pragma unroll
+    for (int t = 0; t < kBoxC; t++) stage[rl * sstride + c0 + t] = res[t];
+  }
+  __syncthreads();
+  float2 *o = reinterpret_cast<float2 *>(out);
+  for (int rl = w; rl < ry; rl += nw) {
+    const int64_t row = row0 + rl;
+    if (row >= rows) break;
+    for (int k = lane; k < tn; k += 32) o[S.vox + row * W + x0 + k] = stage[rl * sstride + k];
   }
 }
 
-// ---------------------------------------------------------------- x pass (box mean)
-// Exact integer window sums (prefix-sum differences) when 2r+1 <= 256; the literal
-// float chain otherwise.
-__global__ void k_box_x(const Sub *subs, int r, const uint32_t *in, float2 *out) {
-  extern __shared__ unsigned long long smb[];
+// ---------------------------------------------------------------- x pass (box, float chain)
+// The literal float chain of the x box for windows wider than 256 (where the partial
+// sums stop being exact integers), over a packed min/max volume.
+__global__ void k_box_x_chain(const Sub *subs, int r, const uint32_t *in, float2 *out) {
+  extern __shared__ float2 sfx[];
+  constexpr int kSeg = 256;
   const Sub S = subs[blockIdx.y];
-  const int segs = (S.W + kRowSeg - 1) / kRowSeg;
+  const int segs = (S.W + kSeg - 1) / kSeg;
   const int64_t rows = (int64_t)S.H * S.D;
   const int64_t bid = blockIdx.x;
   if (bid >= rows * segs) return;
   const int64_t row = bid / segs;
-  const int x0 = (int)(bid % segs) * kRowSeg;
-  const int L = 2 * r + 1, n0 = kRowSeg + 2 * r;
+  const int x0 = (int)(bid % segs) * kSeg;
+  const int L = 2 * r + 1, n0 = kSeg + 2 * r;
   const float inv = 1.0f / (float)L;
   const uint32_t *line = in + S.vox + row * S.W;
-  const int t = threadIdx.x;
-  const int x = x0 + t;
-  if (L <= 256) {
-    // smb[0..n0]: exclusive prefix of packed (lo | hi << 32) sums; both halves stay
-    // below 2^32 because n0 * 65535 < 2^32.
-    __shared__ unsigned long long warp_tot[32];
-    const int per = (n0 + blockDim.x - 1) / blockDim.x;
-    const int beg = t * per, end = min(beg + per, n0);
-    unsigned long long run = 0;
-    for (int i = beg; i < end; i++) {
-      uint32_t v = line[clampi(x0 - r + i, 0, S.W - 1)];
-      smb[i] = run;
-      run += (unsigned long long)(v & 0xFFFFu) | ((unsigned long long)(v >> 16) << 32);
-    }
-    // block exclusive scan of the per-thread totals
-    unsigned long long inc = run;
-    for (int o = 1; o < 32; o <<= 1) {
-      unsigned long long y = __shfl_up_sync(0xFFFFFFFFu, inc, o);
-      if ((t & 31) >= o) inc += y;
-    }
-    if ((t & 31) == 31) warp_tot[t >> 5] = inc;
-    __syncthreads();
-    if (t < 32) {
-      const int nw = blockDim.x >> 5;
-      unsigned long long w = t < nw ? warp_tot[t] : 0ull, wi = w;
-      for (int o = 1; o < 32; o <<= 1) {
-        unsigned long long y = __shfl_up_sync(0xFFFFFFFFu, wi, o);
-        if (t >= o) wi += y;
-      }
-      if (t < nw) warp_tot[t] = wi - w;
-    }
-    __syncthreads();
-    const unsigned long long off = warp_tot[t >> 5] + (inc - run);
-    for (int i = beg; i < end; i++) smb[i] += off;
-    if (t == blockDim.x - 1) smb[n0] = off + run;
-    __syncthreads();
-    if (x < S.W) {
-      const unsigned long long d = smb[t + L] - smb[t];
-      const float lo = (float)(uint32_t)(d & 0xFFFFFFFFull), hi = (float)(uint32_t)(d >> 32);
-      out[S.vox + row * S.W + x] = make_float2(lo * inv, hi * inv);
-    }
-  } else {
-    float2 *sf = reinterpret_cast<float2 *>(smb);
-    for (int i = t; i < n0; i += blockDim.x) {
-      uint32_t v = line[clampi(x0 - r + i, 0, S.W - 1)];
-      sf[i] = make_float2((float)(v & 0xFFFFu), (float)(v >> 16));
-    }
-    __syncthreads();
-    if (x < S.W) {
-      float2 acc = make_float2(0.f, 0.f);
-      for (int j = 0; j < L; j++) acc = add2(acc, sf[t + j]);
-      out[S.vox + row * S.W + x] = mul2(acc, make_float2(inv, inv));
-    }
+  for (int i = threadIdx.x; i < n0; i += blockDim.x) {
+    const uint32_t v = line[clampi(x0 - r + i, 0, S.W - 1)];
+    sfx[i] = make_float2((float)mm_lo(v), (float)mm_hi(v));
   }
+  __syncthreads();
+  const int x = x0 + threadIdx.x;
+  if (x >= S.W) return;
+  float2 acc = make_float2(0.f, 0.f);
+  for (int j = 0; j < L; j++) acc = add2(acc, sfx[threadIdx.x + j]);
+  out[S.vox + row * S.W + x] = mul2(acc, make_float2(inv, inv));
 }
 
 // ---------------------------------------------------------------- y / z passes (box mean)
 // Register-blocked sequential sums: a thread produces K consecutive outputs along the
 // axis; slot (u + k) % K of a K-entry rotating window feeds output k at tap u of each
 // block of K taps, so the window never moves between registers.  Every output still
-// sums its 2r+1 inputs from 0.0f in the reference order.
-constexpr int kBoxK = 8;
-
-template <class LoadF>
-__device__ __forceinline__ void box_chain(int c0, int r, LoadF load, float2 (&acc)[kBoxK]) {
-  float2 win[kBoxK];
+// sums its 2r+1 inputs from 0.0f in the reference order.  load(i) returns input
+// c0 - r + i.
+template <int K, class LoadF>
+__device__ __forceinline__ void box_chain(int L, LoadF load, float2 (&acc)[K]) {
+  float2 win[K];
 #pragma unroll
-  for (int k = 0; k < kBoxK; k++) { win[k] = load(c0 - r + k); acc[k] = make_float2(0.f, 0.f); }
-  const int L = 2 * r + 1;
-  for (int jb = 0; jb < L; jb += kBoxK) {
+  for (int k = 0; k < K; k++) {
+    win[k] = load(k);
+    acc[k] = make_float2(0.f, 0.f);
+  }
+  int jb = 0;
+  for (; jb + K <= L; jb += K) {
 #pragma unroll
-    for (int u = 0; u < kBoxK; u++) {
-      const int j = jb + u;
-      if (j < L) {
+    for (int u = 0; u < K; u++) {
 #pragma unroll
-        for (int k = 0; k < kBoxK; k++) acc[k] = add2(acc[k], win[(u + k) % kBoxK]);
-        win[u] = load(c0 - r + j + kBoxK);
-      }
+      for (int k = 0; k < K; k++) acc[k] = add2(acc[k], win[(u + k) % K]);
+      win[u] = load(jb + u + K);
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < K; u++) {
+    if (jb + u < L) {
+#pragma unroll
+      for (int k = 0; k < K; k++) acc[k] = add2(acc[k], win[(u + k) % K]);
+      if (jb + u + K < L + K - 1) win[u] = load(jb + u + K);
     }
   }
 }
 
-__global__ void k_box_y(const Sub *subs, int r, const float2 *in, float2 *out) {
+constexpr int kBoxYK = 16;   // y outputs per thread
+
+__global__ void __launch_bounds__(128) k_box_y(const Sub *subs, int r, const float2 *in, float2 *out) {
   const Sub S = subs[blockIdx.y];
-  const int rows_per_blk = blockDim.y * kBoxK;
+  const int rows_per_blk = blockDim.y * kBoxYK;
   const int tx_n = (S.W + 31) / 32, ty_n = (S.H + rows_per_blk - 1) / rows_per_blk;
   const int64_t bid = blockIdx.x;
   if (bid >= (int64_t)tx_n * ty_n * S.D) return;
   const int z = (int)(bid / ((int64_t)tx_n * ty_n));
   const int rem = (int)(bid % ((int64_t)tx_n * ty_n));
   const int x = (rem % tx_n) * 32 + threadIdx.x;
-  const int y0 = (rem / tx_n) * rows_per_blk + threadIdx.y * kBoxK;
+  const int y0 = (rem / tx_n) * rows_per_blk + threadIdx.y * kBoxYK;
   if (x >= S.W || y0 >= S.H) return;
-  const float2 *col = in + S.vox + (int64_t)z * S.W * S.H + x;
-  const int H = S.H, W = S.W;
-  float2 acc[kBoxK];
-  box_chain(y0, r, [&](int y) { return col[(int64_t)clampi(y, 0, H - 1) * W]; }, acc);
-  const float inv = 1.0f / (float)(2 * r + 1);
-  float2 *o = out + S.vox + (int64_t)z * S.W * S.H + x;
+  const int H = S.H, W = S.W, L = 2 * r + 1;
+  const float2 *col = in + S.vox + (int64_t)z * W * H + x;
+  float2 acc[kBoxYK];
+  if (y0 - r >= 0 && y0 + kBoxYK + r <= H) {
+    const float2 *p = col + (int64_t)(y0 - r) * W;
+    box_chain<kBoxYK>(L, [&](int i) { return __ldg(p + (int64_t)i * W); }, acc);
+  } else {
+    box_chain<kBoxYK>(L, [&](int i) { return __ldg(col + (int64_t)clampi(y0 - r + i, 0, H - 1) * W); }, acc);
+  }
+  const float inv = 1.0f / (float)L;
+  float2 *o = out + S.vox + (int64_t)z * W * H + x;
 #pragma unroll
-  for (int k = 0; k < kBoxK; k++)
+  for (int k = 0; k < kBoxYK; k++)
     if (y0 + k < H) o[(int64_t)(y0 + k) * W] = mul2(acc[k], make_float2(inv, inv));
 }
 
 // z pass of the box mean fused with Normalize3DKernel (NormalizeFilter.cu:571-586).
-__global__ void k_box_z_norm(const Sub *subs, int rz, float min_intensity, const float2 *in,
-                             float *norm) {
+constexpr int kBoxZK = 8;
+
+__global__ void __launch_bounds__(128) k_box_z_norm(const Sub *subs, int rz, float min_intensity, const float2 *in,
+                                                    float *norm) {
   const Sub S = subs[blockIdx.y];
   const int64_t plane = (int64_t)S.W * S.H;
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= plane) return;
   const float2 *col = in + S.vox + p;
-  const int D = S.D;
-  const float inv = 1.0f / (float)(2 * rz + 1);
-  for (int z0 = 0; z0 < D; z0 += kBoxK) {
-    float2 acc[kBoxK];
-    box_chain(z0, rz, [&](int z) { return col[clampi(z, 0, D - 1) * plane]; }, acc);
+  const int D = S.D, L = 2 * rz + 1;
+  const float inv = 1.0f / (float)L;
+  for (int z0 = 0; z0 < D; z0 += kBoxZK) {
+    float2 acc[kBoxZK];
+    box_chain<kBoxZK>(L, [&](int i) { return __ldg(col + clampi(z0 - rz + i, 0, D - 1) * plane); }, acc);
 #pragma unroll
-    for (int k = 0; k < kBoxK; k++) {
+    for (int k = 0; k < kBoxZK; k++) {
       const int z = z0 + k;
       if (z < D) {
         const float2 el = mul2(acc[k], make_float2(inv, inv));
@@ -305,56 +368,93 @@ __global__ void k_copy_norm(const Sub *subs, float min_intensity, float *norm) {
   norm[S.vox + i] = (v >= min_intensity) ? v : 0.0f;
 }
 
-__global__ void k_unpack_lo(const Sub *subs, const uint32_t *mm, uint16_t *dst) {
-  const Sub S = subs[blockIdx.y];
-  const int64_t n = (int64_t)S.W * S.H * S.D;
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  dst[S.vox + i] = (uint16_t)(mm[S.vox + i] & 0xFFFFu);
-}
-
 // ---------------------------------------------------------------- launchers
-static size_t minmax_y_smem(int r) { return (size_t)2 * (kColTileY + 2 * r) * kColTileX * sizeof(uint32_t); }
-
-void launch_minmax_z(const Sub *d_subs, int nsub, int max_plane, int rz, uint32_t *mm, cudaStream_t s) {
-  dim3 grid(ceil_div(max_plane, 256), nsub);
-  KLAUNCH("k_minmax_z", s, (k_minmax_z<0><<<grid, 256, 0, s>>>(d_subs, rz, mm)));
+static int max_optin_smem() {
+  static int v = 0;
+  if (!v) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (v <= 0) v = 48 * 1024;
+  }
+  return v;
 }
 
-void launch_minmax_x(const Sub *d_subs, int nsub, int64_t max_rows, int max_w, int r,
-                     const uint32_t *in, uint32_t *out, cudaStream_t s) {
-  dim3 grid((unsigned)(max_rows * ceil_div(max_w, kRowSeg)), nsub);
-  size_t smem = (size_t)2 * (kRowSeg + 2 * r) * sizeof(uint32_t);
-  KLAUNCH("k_minmax_x", s, (k_minmax_x<0><<<grid, kRowSeg, smem, s>>>(d_subs, r, in, out)));
+template <class F>
+static void allow_smem(F *fn, size_t bytes) {
+  if (bytes > 48 * 1024) cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
-void launch_minmax_y(const Sub *d_subs, int nsub, int max_w, int max_h, int max_d, int r,
-                     const uint32_t *in, uint32_t *out, cudaStream_t s) {
-  dim3 grid((unsigned)((int64_t)ceil_div(max_w, kColTileX) * ceil_div(max_h, kColTileY) * max_d), nsub);
-  size_t smem = minmax_y_smem(r);
-  if (smem > 48 * 1024) cudaFuncSetAttribute(k_minmax_y<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  KLAUNCH("k_minmax_y", s, (k_minmax_y<0><<<grid, dim3(kColTileX, 8), smem, s>>>(d_subs, r, in, out)));
+template <int BORDER>
+static void mm_z(const Sub *d_subs, int nsub, int plane, int rz, bool vec4, uint32_t *mm, cudaStream_t s) {
+  if (vec4) {
+    dim3 grid(ceil_div(plane / 4, 256), nsub);
+    KLAUNCH("k_mm_z", s, (k_mm_z<BORDER, 4><<<grid, 256, 0, s>>>(d_subs, rz, mm)));
+  } else {
+    dim3 grid(ceil_div(plane, 256), nsub);
+    KLAUNCH("k_mm_z", s, (k_mm_z<BORDER, 1><<<grid, 256, 0, s>>>(d_subs, rz, mm)));
+  }
 }
 
-void launch_box_x(const Sub *d_subs, int nsub, int64_t max_rows, int max_w, int r,
-                  const uint32_t *in, float2 *out, cudaStream_t s) {
-  dim3 grid((unsigned)(max_rows * ceil_div(max_w, kRowSeg)), nsub);
-  size_t smem = (size_t)(kRowSeg + 2 * r + 1) * sizeof(unsigned long long);
-  if (smem > 48 * 1024) cudaFuncSetAttribute(k_box_x, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  KLAUNCH("k_box_x", s, (k_box_x<<<grid, kRowSeg, smem, s>>>(d_subs, r, in, out)));
+template <int BORDER>
+static void mm_y(const Sub *d_subs, int nsub, int W, int H, int D, int r, const uint32_t *in, uint32_t *out,
+                 cudaStream_t s) {
+  // rows per block: 128, fewer when the staged window would not fit in shared memory
+  const int cap_rows = max_optin_smem() / (2 * 32 * 4);
+  int ty = 128;
+  while (ty > 16 && ty + 2 * r > cap_rows) ty /= 2;
+  const size_t smem = (size_t)2 * (ty + 2 * r) * 32 * 4;
+  allow_smem(k_mm_y<BORDER>, smem);
+  dim3 grid((unsigned)((int64_t)ceil_div(W, 32) * ceil_div(H, ty) * D), nsub);
+  KLAUNCH("k_mm_y", s, (k_mm_y<BORDER><<<grid, 256, smem, s>>>(d_subs, r, ty, in, out)));
 }
 
-void launch_box_y(const Sub *d_subs, int nsub, int max_w, int max_h, int max_d, int r,
-                  const float2 *in, float2 *out, cudaStream_t s) {
+static size_t mm_x_smem(int mode, int r, int ry, int tx) {
+  const int hm = mode == 0 ? r : 0;
+  const int stride = (tx + 2 * hm + 2 * r) | 1;
+  size_t words = (size_t)2 * ry * stride;
+  if (mode == 0) {
+    words += (size_t)ry * ((tx + 2 * r) | 1);
+    words = words > (size_t)ry * (tx + 1) * 2 ? words : (size_t)ry * (tx + 1) * 2;   // staging fits over A + G
+  }
+  return words * 4;
+}
+
+template <int BORDER, int MODE>
+static void mm_x(const Sub *d_subs, int nsub, int W, int64_t rows, int r, const uint32_t *in, void *out,
+                 cudaStream_t s) {
+  // 16 rows x 256 outputs per block, narrower until the staged rows fit in shared
+  // memory; MODE 0 runs one thread per (row, chunk of kBoxC outputs).
+  int ry = 16, tx = 256;
+  while (mm_x_smem(MODE, r, ry, tx) > (size_t)max_optin_smem() && tx > 64) tx /= 2;
+  const size_t smem = mm_x_smem(MODE, r, ry, tx);
+  const int threads = MODE == 0 ? ry * (tx / kBoxC) : 256;
+  allow_smem(k_mm_x<BORDER, MODE>, smem);
+  dim3 grid((unsigned)(((rows + ry - 1) / ry) * ceil_div(W, tx)), nsub);
+  KLAUNCH("k_mm_x", s, (k_mm_x<BORDER, MODE><<<grid, threads, smem, s>>>(d_subs, r, ry, tx, in, out)));
+}
+
+void launch_normalize(const Sub *d_subs, int nsub, int W, int H, int D, int rxy, int rz, float min_intensity,
+                      bool src_aligned8, uint32_t *ma, uint32_t *mb, float2 *fa, float2 *fb, float *norm,
+                      cudaStream_t s) {
+  const int plane = W * H;
+  const int64_t rows = (int64_t)H * D;
+  mm_z<0>(d_subs, nsub, plane, rz, src_aligned8 && plane % 4 == 0, ma, s);
+  mm_y<0>(d_subs, nsub, W, H, D, rxy, ma, mb, s);
+  if (2 * rxy + 1 <= 256) {
+    mm_x<0, 0>(d_subs, nsub, W, rows, rxy, mb, fa, s);
+  } else {
+    mm_x<0, 2>(d_subs, nsub, W, rows, rxy, mb, ma, s);
+    const size_t smem = (size_t)(256 + 2 * rxy) * sizeof(float2);
+    allow_smem(k_box_x_chain, smem);
+    KLAUNCH("k_box_x_chain", s, (k_box_x_chain<<<dim3((unsigned)(rows * ceil_div(W, 256)), nsub), 256, smem, s>>>(
+                                    d_subs, rxy, ma, fa)));
+  }
   const int by = 4;
-  dim3 grid((unsigned)((int64_t)ceil_div(max_w, 32) * ceil_div(max_h, by * kBoxK) * max_d), nsub);
-  KLAUNCH("k_box_y", s, (k_box_y<<<grid, dim3(32, by), 0, s>>>(d_subs, r, in, out)));
-}
-
-void launch_box_z_norm(const Sub *d_subs, int nsub, int max_plane, int rz, float min_intensity,
-                       const float2 *in, float *norm, cudaStream_t s) {
-  dim3 grid(ceil_div(max_plane, 128), nsub);
-  KLAUNCH("k_box_z_norm", s, (k_box_z_norm<<<grid, 128, 0, s>>>(d_subs, rz, min_intensity, in, norm)));
+  dim3 gy((unsigned)((int64_t)ceil_div(W, 32) * ceil_div(H, by * kBoxYK) * D), nsub);
+  KLAUNCH("k_box_y", s, (k_box_y<<<gy, dim3(32, by), 0, s>>>(d_subs, rxy, fa, fb)));
+  KLAUNCH("k_box_z_norm", s, (k_box_z_norm<<<dim3(ceil_div(plane, 128), nsub), 128, 0, s>>>(
+                                 d_subs, rz, min_intensity, fb, norm)));
 }
 
 void launch_copy_norm(const Sub *d_subs, int nsub, int64_t max_n, float min_intensity, float *norm,
@@ -363,24 +463,16 @@ void launch_copy_norm(const Sub *d_subs, int nsub, int64_t max_n, float min_inte
   KLAUNCH("k_copy_norm", s, (k_copy_norm<<<grid, 256, 0, s>>>(d_subs, min_intensity, norm)));
 }
 
-// Erosion3DFilter: min with a zero border.  Min is separable and exact, so z -> x -> y
+// Erosion3DFilter: min with a zero border.  Min is separable and exact, so z -> y -> x
 // gives the reference's x -> y -> z result.  `tmp` holds two packed u32 volumes.
-void launch_erosion(const Sub *d_subs, int nsub, int max_w, int max_h, int max_d, int64_t max_rows,
-                    int rxy, int rz, const uint16_t *src_override, uint16_t *tmp_u16, uint16_t *dst,
-                    cudaStream_t s) {
-  (void)src_override;
-  uint32_t *a = reinterpret_cast<uint32_t *>(tmp_u16);
-  const int64_t max_n = max_rows * max_w;
-  uint32_t *b = a + max_n * nsub;
-  const int max_plane = max_w * max_h;
-  KLAUNCH("k_minmax_z", s, (k_minmax_z<1><<<dim3(ceil_div(max_plane, 256), nsub), 256, 0, s>>>(d_subs, rz, a)));
-  size_t smx = (size_t)2 * (kRowSeg + 2 * rxy) * sizeof(uint32_t);
-  KLAUNCH("k_minmax_x", s, (k_minmax_x<1><<<dim3((unsigned)(max_rows * ceil_div(max_w, kRowSeg)), nsub), kRowSeg, smx, s>>>(d_subs, rxy, a, b)));
-  size_t smy = minmax_y_smem(rxy);
-  if (smy > 48 * 1024) cudaFuncSetAttribute(k_minmax_y<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smy);
-  KLAUNCH("k_minmax_y", s, (k_minmax_y<1><<<dim3((unsigned)((int64_t)ceil_div(max_w, kColTileX) * ceil_div(max_h, kColTileY) * max_d), nsub),
-                  dim3(kColTileX, 8), smy, s>>>(d_subs, rxy, b, a)));
-  KLAUNCH("k_unpack_lo", s, (k_unpack_lo<<<dim3(ceil_div(max_n, 256), nsub), 256, 0, s>>>(d_subs, a, dst)));
+void launch_erosion(const Sub *d_subs, int nsub, int W, int H, int D, int rxy, int rz, bool src_aligned8,
+                    uint32_t *tmp, uint16_t *dst, cudaStream_t s) {
+  const int plane = W * H;
+  const int64_t n = (int64_t)plane * D;
+  uint32_t *a = tmp, *b = tmp + n * nsub;
+  mm_z<1>(d_subs, nsub, plane, rz, src_aligned8 && plane % 4 == 0, a, s);
+  mm_y<1>(d_subs, nsub, W, H, D, rxy, a, b, s);
+  mm_x<1, 1>(d_subs, nsub, W, (int64_t)H * D, rxy, b, dst, s);
 }
 
 }  // namespace hdog

@@ -308,19 +308,22 @@ __global__ void __launch_bounds__(kFinalizeBlock) k_finalize(const Sub *subs, co
     float hs[6];
 #pragma unroll
     for (int k = 0; k < 6; k++) hs[k] = __double2float_rn(from_fix(acc.hess[k * slots + g]));
-    float st, bl;
-    eigen_features(hs, &st, &bl);
     out.intensity[g] = inten;
     out.centroid[g] = cx; out.centroid[slots + g] = cy; out.centroid[2 * slots + g] = cz;
 #pragma unroll
     for (int k = 0; k < 6; k++) out.hessian[k * slots + g] = hs[k];
-    out.eigen[g] = st; out.eigen[slots + g] = bl;
     if (r >= 1) {
       keep = true;
       if (cz < (float)S.margin || cz >= (float)(S.depth_valid - S.margin)) keep = false;
       if (cx < (float)fp.left || cx >= (float)(S.W - fp.right)) keep = false;
       if (cy < (float)fp.top || cy >= (float)(S.H - fp.bottom)) keep = false;
       if ((int)(cnt & 0xFFFFu) < fp.min_size || inten <= 0.0f) keep = false;
+    }
+    // the FP64 eigen solve only where its result is read
+    if (keep || fp.all_eigen) {
+      float st, bl;
+      eigen_features(hs, &st, &bl);
+      out.eigen[g] = st; out.eigen[slots + g] = bl;
     }
     out.keep[g] = keep ? 1 : 0;
   }

@@ -320,6 +320,387 @@ __global__ void __launch_bounds__(kSweepThreads, 1)
   }
 }
 
+// ------------------------------------------------------------------ radius-specialised sweeps
+// For common sigma pairs the chain runs as two z-sweeps with the four tap radii as
+// template parameters (RA/RB: xy radius of the small/large scale, ZA/ZB: z radius):
+//
+//   k_dog_sweep   normalized -> DoG volume.  A block owns a 64 x 16 tile and sweeps z;
+//                 stage A filters slice it along x (TMA-loaded, double-buffered), stage B
+//                 filters slice it-1 along y and feeds the z shift register, which emits
+//                 DoG slice it-1-RZ straight to global memory.  One barrier per slice.
+//                 Taps are compile-time offsets into the constant bank.  The z shift
+//                 register never moves: output zo lives in slot zo mod (2RZ+1), and a
+//                 switch on the step's phase picks the compile-time slot of every tap.
+//                 Every output is the reference's FMA chain, zero taps at the borders
+//                 included, so the volume equals the separate passes bit for bit.
+//   k_hess_sweep  DoG -> mask + foreground list.  A block owns a 64 x 16 tile; DoG slices
+//                 (tile + 2-voxel halo, zero outside the volume) arrive by TMA into an
+//                 8-slot ring, up to five slices ahead; each thread tests one x quad.
+//
+// The split costs one write and one read of the DoG volume but frees the Hessian stage
+// from the z shift register's registers, so several Hessian blocks share an SM.
+constexpr int kDTX = 64, kDTY = 16;     // DoG tile
+constexpr int kHTX = 64, kHTY = 16;     // Hessian tile
+constexpr int kHPX = kHTX + 8;          // Hessian ring row: columns x0-4 .. x0+67 (16-byte aligned start)
+constexpr int kHPY = kHTY + 4;
+constexpr int kHRing = 8;              // ring slots; a slot is 72 x 20 floats = 45 x 128 bytes
+constexpr int kHThreads = kHTX / 4 * kHTY;   // one x quad per thread
+
+template <int RA, int RB, int ZA, int ZB>
+struct DogT {
+  static constexpr int RXY = RA > RB ? RA : RB;
+  static constexpr int RZ = ZA > ZB ? ZA : ZB;
+  static constexpr int WIN = 2 * RZ + 1;
+  static constexpr int HX = (RXY + 3) / 4 * 4;                // x halo, 16-byte aligned
+  static constexpr int BW = kDTX + 2 * HX;                    // staged input box
+  static constexpr int BH = kDTY + 2 * RXY;
+  static constexpr int IN_FLOATS = (BW * BH + 31) / 32 * 32;  // 128-byte multiple
+  static constexpr int XQ = kDTX / 4;                         // x-pass items per row
+  static constexpr int XITEMS = BH * XQ;
+  static constexpr int OFF = HX - RXY;                        // item q reads from column 4q + OFF
+  static constexpr int NV = (OFF + 2 * RXY + 4 + 3) / 4 * 4;  // inputs staged per item
+  static constexpr int NT = kDTX * kDTY / 2;                  // 512: two z columns per thread
+  static constexpr size_t SMEM = (size_t)2 * IN_FLOATS * 4 + (size_t)2 * BH * kDTX * 8 + 64;
+};
+
+// One tap of both scales: j is the input offset, the coefficient index r - j as in the
+// reference's `sum = fma(k[r - j], s[x + j], sum)`.
+template <int RA, int RB, int J>
+__device__ __forceinline__ void tap2(const DogTaps &T, int ka, int kb, float2 v, float2 &acc) {
+  constexpr bool a = J >= -RA && J <= RA, b = J >= -RB && J <= RB;
+  if (a && b) acc = fma2(make_float2(T.k[ka][RA - J], T.k[kb][RB - J]), v, acc);
+  else if (b) acc.y = __fmaf_rn(T.k[kb][RB - J], v.y, acc.y);
+  else if (a) acc.x = __fmaf_rn(T.k[ka][RA - J], v.x, acc.x);
+}
+
+template <int RA, int RB, int J, int N>
+struct TapLoop {
+  // x pass: taps J .. J+N-1 for the four outputs of an item
+  template <int NV>
+  __device__ __forceinline__ static void x4(const DogTaps &T, const float (&w)[NV], int base, float2 (&a)[4]) {
+    if constexpr (N > 0) {
+#pragma unroll
+      for (int o = 0; o < 4; o++) {
+        const float x = w[base + o + J];
+        tap2<RA, RB, J>(T, 0, 2, make_float2(x, x), a[o]);
+      }
+      TapLoop<RA, RB, J + 1, N - 1>::x4(T, w, base, a);
+    }
+  }
+  // y pass of rows cy (g0) and cy + 1 (g1): input row i is tap i - R of g0 and tap
+  // i - R - 1 of g1, loaded once, in ascending tap order for both
+  template <int STRIDE>
+  __device__ __forceinline__ static void y2(const DogTaps &T, const float2 *col, float2 &g0, float2 &g1) {
+    if constexpr (N > 0) {
+      constexpr int R = RA > RB ? RA : RB;
+      const float2 v = col[(J + R) * STRIDE];
+      tap2<RA, RB, J>(T, 0, 2, v, g0);
+      if constexpr (J > -R) tap2<RA, RB, J - 1>(T, 0, 2, v, g1);
+      if constexpr (N == 1) tap2<RA, RB, J>(T, 0, 2, col[(J + R + 1) * STRIDE], g1);
+      TapLoop<RA, RB, J + 1, N - 1>::template y2<STRIDE>(T, col, g0, g1);
+    }
+  }
+};
+
+// z step of phase P = zy mod WIN: input slice zy is tap d of output zo = zy - d, which
+// lives in slot (zo mod WIN); then output zy - RZ is complete and its slot is cleared for
+// output zy - RZ + WIN.
+template <class C, int ZA, int ZB, int P, int D0, int N>
+struct ZTaps {
+  __device__ __forceinline__ static void run(const DogTaps &T, float2 (&a0)[C::WIN], float2 (&a1)[C::WIN], float2 g0,
+                                             float2 g1) {
+    if constexpr (N > 0) {
+      constexpr int s = ((P - D0) % C::WIN + C::WIN) % C::WIN;
+      tap2<ZA, ZB, D0>(T, 1, 3, g0, a0[s]);
+      tap2<ZA, ZB, D0>(T, 1, 3, g1, a1[s]);
+      ZTaps<C, ZA, ZB, P, D0 + 1, N - 1>::run(T, a0, a1, g0, g1);
+    }
+  }
+};
+
+template <class C, int ZA, int ZB, int P>
+__device__ __forceinline__ void z_step(const DogTaps &T, float2 (&a0)[C::WIN], float2 (&a1)[C::WIN], float2 g0,
+                                       float2 g1, float &d0, float &d1) {
+  ZTaps<C, ZA, ZB, P, -C::RZ, C::WIN>::run(T, a0, a1, g0, g1);
+  constexpr int se = ((P - C::RZ) % C::WIN + C::WIN) % C::WIN;
+  d0 = __fmul_rn(__fsub_rn(a0[se].x, a0[se].y), T.normalizer);
+  d1 = __fmul_rn(__fsub_rn(a1[se].x, a1[se].y), T.normalizer);
+  a0[se] = make_float2(0.f, 0.f);
+  a1[se] = make_float2(0.f, 0.f);
+}
+
+template <class C, int ZA, int ZB, int P = 0>
+__device__ __forceinline__ void z_dispatch(int phase, const DogTaps &T, float2 (&a0)[C::WIN], float2 (&a1)[C::WIN],
+                                           float2 g0, float2 g1, float &d0, float &d1) {
+  if constexpr (P < C::WIN) {
+    if (phase == P) z_step<C, ZA, ZB, P>(T, a0, a1, g0, g1, d0, d1);
+    else z_dispatch<C, ZA, ZB, P + 1>(phase, T, a0, a1, g0, g1, d0, d1);
+  }
+}
+
+template <int RA, int RB, int ZA, int ZB>
+__global__ void __launch_bounds__(DogT<RA, RB, ZA, ZB>::NT, 1)
+    k_dog_sweep(const __grid_constant__ CUtensorMap map, const __grid_constant__ DogTaps T, const Sub *subs,
+                float *dog, int *status) {
+  using C = DogT<RA, RB, ZA, ZB>;
+  extern __shared__ __align__(128) unsigned char smem[];
+  const Sub S = subs[blockIdx.y];
+  const int ntx = (S.W + kDTX - 1) / kDTX, nty = (S.H + kDTY - 1) / kDTY;
+  if ((int64_t)blockIdx.x >= (int64_t)ntx * nty) return;
+  const int x0 = (int)(blockIdx.x % ntx) * kDTX, y0 = (int)(blockIdx.x / ntx) * kDTY;
+  float *inb = reinterpret_cast<float *>(smem);
+  float2 *xb = reinterpret_cast<float2 *>(smem + (size_t)2 * C::IN_FLOATS * 4);
+  uint64_t *bar = reinterpret_cast<uint64_t *>(smem + (size_t)2 * C::IN_FLOATS * 4 + (size_t)2 * C::BH * kDTX * 8);
+  const int t = threadIdx.x;
+  const int D = S.D, W = S.W, H = S.H;
+  if (t == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  constexpr uint32_t tma_bytes = (uint32_t)(C::BW * C::BH * 4);
+  const int tx = x0 - C::HX, ty = y0 - C::RXY;
+  if (t == 0 && D > 0) tma_slice(&map, inb, &bar[0], tx, ty, 0, blockIdx.y, tma_bytes);
+  bool ok = true;
+  // stage B ownership: columns (cx, cy) and (cx, cy + 1) of the tile
+  const int cx = t % kDTX, cy = 2 * (t / kDTX);
+  const int gx = x0 + cx, gy = y0 + cy;
+  const bool w0 = gx < W && gy < H, w1 = gx < W && gy + 1 < H;
+  float *out0 = dog + S.vox + (int64_t)gy * W + gx;
+  const int64_t WH = (int64_t)W * H;
+  float2 acc0[C::WIN], acc1[C::WIN];
+#pragma unroll
+  for (int s = 0; s < C::WIN; s++) { acc0[s] = make_float2(0.f, 0.f); acc1[s] = make_float2(0.f, 0.f); }
+  const int nit = D + C::RZ + 1;
+  for (int it = 0; it < nit; it++) {
+    if (t == 0 && ok && it + 1 < D)
+      tma_slice(&map, inb + ((it + 1) & 1) * C::IN_FLOATS, &bar[(it + 1) & 1], tx, ty, it + 1, blockIdx.y, tma_bytes);
+    // ---- B: y pass of slice zy (zero past the volume: the border taps still multiply),
+    // z shift register, DoG slice zy - RZ
+    const int zy = it - 1;
+    if (zy >= 0) {
+      float2 g0 = make_float2(0.f, 0.f), g1 = make_float2(0.f, 0.f);
+      if (zy < D)
+        TapLoop<RA, RB, -C::RXY, 2 * C::RXY + 1>::template y2<kDTX>(T, xb + (zy & 1) * C::BH * kDTX + cy * kDTX + cx,
+                                                                     g0, g1);
+      float d0, d1;
+      z_dispatch<C, ZA, ZB>(zy % C::WIN, T, acc0, acc1, g0, g1, d0, d1);
+      const int zo = zy - C::RZ;
+      if (zo >= 0) {
+        if (w0) out0[zo * WH] = d0;
+        if (w1) out0[zo * WH + W] = d1;
+      }
+    }
+    // ---- A: x pass of slice it
+    if (it < D) {
+      if (ok && !mbar_wait(&bar[it & 1], (it >> 1) & 1)) {
+        ok = false;
+        atomicExch(status, HDOG_ERR_TIMEOUT);
+      }
+      const float *ib = inb + (it & 1) * C::IN_FLOATS;
+      float2 *xo = xb + (it & 1) * C::BH * kDTX;
+      for (int item = t; item < C::XITEMS; item += C::NT) {
+        const int row = item / C::XQ, q = item % C::XQ;
+        const float *in = ib + row * C::BW + 4 * q;
+        float w[C::NV];
+#pragma unroll
+        for (int i = 0; i < C::NV; i += 4) {
+          const float4 f = *reinterpret_cast<const float4 *>(in + i);
+          w[i] = f.x; w[i + 1] = f.y; w[i + 2] = f.z; w[i + 3] = f.w;
+        }
+        float2 a[4] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+        TapLoop<RA, RB, -C::RXY, 2 * C::RXY + 1>::x4(T, w, C::OFF + C::RXY, a);
+        float4 *o = reinterpret_cast<float4 *>(xo + row * kDTX + 4 * q);
+        o[0] = make_float4(a[0].x, a[0].y, a[1].x, a[1].y);
+        o[1] = make_float4(a[2].x, a[2].y, a[3].x, a[3].y);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Central difference of the Hessian stage.  The reference writes ((0 + a) - b) * 0.5; the
+// `0 +` only turns -0 into +0, and a zero's sign never changes a magnitude, a comparison
+// or a fixed-point sum, so the mask and every record stay identical without it.
+__device__ __forceinline__ float hdiff(float plus, float minus) { return __fmul_rn(__fsub_rn(plus, minus), 0.5f); }
+
+__global__ void __launch_bounds__(kHThreads, 3)
+    k_hess_sweep(const __grid_constant__ CUtensorMap map, const Sub *subs, const float *norm, uint8_t *mask, FgEntry *fg,
+                 unsigned long long *fg_count, int *status) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  constexpr int PL = kHPX * kHPY;
+  constexpr uint32_t tma_bytes = (uint32_t)(PL * 4);
+  const Sub S = subs[blockIdx.y];
+  const int ntx = (S.W + kHTX - 1) / kHTX, nty = (S.H + kHTY - 1) / kHTY;
+  if ((int64_t)blockIdx.x >= (int64_t)ntx * nty) return;
+  const int x0 = (int)(blockIdx.x % ntx) * kHTX, y0 = (int)(blockIdx.x / ntx) * kHTY;
+  float *ring = reinterpret_cast<float *>(smem);
+  uint64_t *bar = reinterpret_cast<uint64_t *>(smem + (size_t)kHRing * PL * 4);
+  const int t = threadIdx.x;
+  const int D = S.D, W = S.W, H = S.H;
+  const int32_t WH = W * H;
+  if (t == 0) {
+    for (int i = 0; i < kHRing; i++) mbar_init(&bar[i], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  const int tx = x0 - 4, ty = y0 - 2;
+  // ring slot of DoG slice z (z = -2 .. D+1; slices outside the volume arrive zero-filled)
+  auto slot = [](int z) { return (z + 2 * kHRing) % kHRing; };
+  // use k of slot s (k-th slice loaded into it) completes barrier phase k & 1
+  auto use = [](int z) { return (z + 2) / kHRing; };
+  // slices -2 .. 4 up front, then slice zh + 5 while slice zh is tested: the slot it
+  // reuses held slice zh - 3, last read one barrier earlier
+  if (t == 0)
+    for (int z = -2; z <= 4 && z <= D + 1; z++)
+      tma_slice(&map, ring + slot(z) * PL, &bar[slot(z)], tx, ty, z, blockIdx.y, tma_bytes);
+  bool ok = true;
+  for (int z = -2; z <= 1; z++)
+    if (ok && !mbar_wait(&bar[slot(z)], use(z) & 1)) {
+      ok = false;
+      atomicExch(status, HDOG_ERR_TIMEOUT);
+    }
+  const int q = t % (kHTX / 4), ly = t / (kHTX / 4);
+  const int X0 = x0 + 4 * q, Y = y0 + ly;
+  const bool interior = x0 >= 1 && x0 + kHTX < W && y0 >= 1 && y0 + kHTY < H;
+  const int b = (ly + 2) * kHPX + 4 * q;   // ring index of column X0 - 4 on row Y
+  for (int zh = 0; zh < D; zh++) {
+    if (t == 0 && ok && zh + 5 <= D + 1)
+      tma_slice(&map, ring + slot(zh + 5) * PL, &bar[slot(zh + 5)], tx, ty, zh + 5, blockIdx.y, tma_bytes);
+    // slices zh-2 .. zh+1 were waited for already; zh+2 is new
+    if (ok && !mbar_wait(&bar[slot(zh + 2)], use(zh + 2) & 1)) {
+      ok = false;
+      atomicExch(status, HDOG_ERR_TIMEOUT);
+    }
+    const float *P0 = ring + slot(zh) * PL, *P1 = ring + slot(zh + 1) * PL, *P2 = ring + slot(zh + 2) * PL;
+    const float *M1 = ring + slot(zh - 1) * PL, *M2 = ring + slot(zh - 2) * PL;
+    const bool zup = zh + 1 < D, zdn = zh >= 1;
+    float hv[4][6];
+    bool fgv[4] = {false, false, false, false};
+    int nfg = 0;
+    const int32_t i0 = zh * WH + Y * W + X0;
+    if (interior) {
+      auto ld12 = [&](const float *src, float *dst) {   // columns X0-4 .. X0+7
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+          const float4 f = *reinterpret_cast<const float4 *>(src + 4 * i);
+          dst[4 * i] = f.x; dst[4 * i + 1] = f.y; dst[4 * i + 2] = f.z; dst[4 * i + 3] = f.w;
+        }
+      };
+      auto ld4 = [&](const float *src, float *dst) {    // columns X0 .. X0+3
+        const float4 f = *reinterpret_cast<const float4 *>(src + 4);
+        dst[0] = f.x; dst[1] = f.y; dst[2] = f.z; dst[3] = f.w;
+      };
+      // voxel o sits at index o + 4 of a 12-column row
+      {
+        float a[12], v[4], w[4], p2[4], m2[4];
+        ld12(P0 + b, a);
+        ld4(P0 + b - 2 * kHPX, v);
+        ld4(P0 + b + 2 * kHPX, w);
+        ld4(P2 + b, p2);
+        ld4(M2 + b, m2);
+#pragma unroll
+        for (int o = 0; o < 4; o++) {
+          const float c = a[o + 4];
+          hv[o][0] = hdiff(hdiff(a[o + 6], c), hdiff(c, a[o + 2]));
+          hv[o][3] = hdiff(hdiff(w[o], c), hdiff(c, v[o]));
+          hv[o][5] = hdiff(zup ? hdiff(p2[o], c) : 0.0f, zdn ? hdiff(c, m2[o]) : 0.0f);
+        }
+      }
+      {
+        float u[12], dn[12];
+        ld12(P0 + b - kHPX, u);
+        ld12(P0 + b + kHPX, dn);
+#pragma unroll
+        for (int o = 0; o < 4; o++) hv[o][1] = hdiff(hdiff(dn[o + 5], dn[o + 3]), hdiff(u[o + 5], u[o + 3]));
+      }
+      {
+        float p[12], m[12];
+        ld12(P1 + b, p);
+        ld12(M1 + b, m);
+#pragma unroll
+        for (int o = 0; o < 4; o++)
+          hv[o][2] = hdiff(zup ? hdiff(p[o + 5], p[o + 3]) : 0.0f, zdn ? hdiff(m[o + 5], m[o + 3]) : 0.0f);
+      }
+      {
+        float pu[4], pd[4], mu[4], md[4];
+        ld4(P1 + b - kHPX, pu);
+        ld4(P1 + b + kHPX, pd);
+        ld4(M1 + b - kHPX, mu);
+        ld4(M1 + b + kHPX, md);
+#pragma unroll
+        for (int o = 0; o < 4; o++)
+          hv[o][4] = hdiff(zup ? hdiff(pd[o], pu[o]) : 0.0f, zdn ? hdiff(md[o], mu[o]) : 0.0f);
+      }
+      uint32_t mword = 0;
+#pragma unroll
+      for (int o = 0; o < 4; o++) {
+        const bool pdv = pd_test(hv[o][0], hv[o][1], hv[o][2], hv[o][3], hv[o][4], hv[o][5]);
+        mword |= (pdv ? 1u : 0u) << (8 * o);
+        fgv[o] = pdv;
+        nfg += pdv;
+      }
+      *reinterpret_cast<uint32_t *>(mask + S.vox + i0) = mword;
+    } else {
+#pragma unroll
+      for (int o = 0; o < 4; o++) {
+        const int X = X0 + o;
+        if (X >= W || Y >= H) continue;
+        const int ex = 4 * q + o + 4, ey = ly + 2;
+        auto Dv = [&](int ddx, int ddy, int ddz) -> float {
+          return ring[slot(zh + ddz) * PL + (ey + ddy) * kHPX + (ex + ddx)];
+        };
+        auto in_vol = [&](int ddx, int ddy, int ddz) -> bool {
+          const int xx = X + ddx, yy = Y + ddy, zz = zh + ddz;
+          return xx >= 0 && xx < W && yy >= 0 && yy < H && zz >= 0 && zz < D;
+        };
+        auto GX = [&](int ddx, int ddy, int ddz) -> float {
+          return in_vol(ddx, ddy, ddz) ? hdiff(Dv(ddx + 1, ddy, ddz), Dv(ddx - 1, ddy, ddz)) : 0.0f;
+        };
+        auto GY = [&](int ddx, int ddy, int ddz) -> float {
+          return in_vol(ddx, ddy, ddz) ? hdiff(Dv(ddx, ddy + 1, ddz), Dv(ddx, ddy - 1, ddz)) : 0.0f;
+        };
+        auto GZ = [&](int ddz) -> float {
+          return in_vol(0, 0, ddz) ? hdiff(Dv(0, 0, ddz + 1), Dv(0, 0, ddz - 1)) : 0.0f;
+        };
+        hv[o][0] = hdiff(GX(1, 0, 0), GX(-1, 0, 0));
+        hv[o][1] = hdiff(GX(0, 1, 0), GX(0, -1, 0));
+        hv[o][2] = hdiff(GX(0, 0, 1), GX(0, 0, -1));
+        hv[o][3] = hdiff(GY(0, 1, 0), GY(0, -1, 0));
+        hv[o][4] = hdiff(GY(0, 0, 1), GY(0, 0, -1));
+        hv[o][5] = hdiff(GZ(1), GZ(-1));
+        const bool pdv = pd_test(hv[o][0], hv[o][1], hv[o][2], hv[o][3], hv[o][4], hv[o][5]);
+        mask[S.vox + i0 + o] = pdv ? 1 : 0;
+        fgv[o] = pdv && i0 + o != 0;
+        nfg += fgv[o];
+      }
+    }
+    // warp-aggregated append to the foreground list (every lane of the block takes part)
+    const int lane = t & 31;
+    int incl = nfg;
+    for (int dd = 1; dd < 32; dd <<= 1) {
+      const int vv = __shfl_up_sync(0xFFFFFFFFu, incl, dd);
+      if (lane >= dd) incl += vv;
+    }
+    const int tot = __shfl_sync(0xFFFFFFFFu, incl, 31);
+    unsigned long long base = 0;
+    if (lane == 31 && tot) base = atomicAdd(&fg_count[blockIdx.y], (unsigned long long)tot);
+    base = __shfl_sync(0xFFFFFFFFu, base, 31) + (unsigned long long)(incl - nfg);
+#pragma unroll
+    for (int o = 0; o < 4; o++) {
+      if (!fgv[o]) continue;
+      if ((int64_t)base < S.fg_cap) {
+        float4 *dst = reinterpret_cast<float4 *>(fg + S.fg + base);
+        dst[0] = make_float4(__int_as_float(i0 + o), __ldcg(norm + S.vox + i0 + o), hv[o][0], hv[o][1]);
+        dst[1] = make_float4(hv[o][2], hv[o][3], hv[o][4], hv[o][5]);
+      }
+      base++;
+    }
+    __syncthreads();   // slot of zh-2 is reloaded in the next iteration
+  }
+}
+
 // ------------------------------------------------------------------ host side
 typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
                                   const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
@@ -337,29 +718,89 @@ static EncodeTiledFn encode_fn() {
   return fn;
 }
 
+// Radius-specialised instantiations: (small xy, large xy, small z, large z) tap radii.
+// (4, 6, 3, 5): sigma (2.0, 1.5) / (3.2, 2.4); (8, 12, 4, 5): sigma (4.0, 1.8) / (6.0, 2.7).
+typedef void (*DogSweepKernel)(CUtensorMap, DogTaps, const Sub *, float *, int *);
+struct SweepInst {
+  int ra, rb, za, zb;
+  DogSweepKernel fn;
+  size_t smem;
+  int threads, bw, bh, hx, rxy;
+};
+template <int RA, int RB, int ZA, int ZB>
+constexpr SweepInst sweep_inst() {
+  using C = DogT<RA, RB, ZA, ZB>;
+  return SweepInst{RA, RB, ZA, ZB, k_dog_sweep<RA, RB, ZA, ZB>, C::SMEM, C::NT, C::BW, C::BH, C::HX, C::RXY};
+}
+static const SweepInst kSweepInst[] = {sweep_inst<4, 6, 3, 5>(), sweep_inst<8, 12, 4, 5>()};
+
+static const SweepInst *find_inst(const DogTaps &T) {
+  for (const SweepInst &s : kSweepInst)
+    if (s.ra == T.r[0] && s.rb == T.r[2] && s.za == T.r[1] && s.zb == T.r[3]) return &s;
+  return nullptr;
+}
+
+static constexpr size_t kHessSmem = (size_t)kHRing * kHPX * kHPY * 4 + kHRing * 8;
+static_assert((kHPX * kHPY * 4) % 128 == 0, "TMA ring slots must start on 128-byte boundaries");
+
 // Whether the fused sweep handles these parameters (else the separate passes run).
 bool sweep_supported(const DogTaps &T, int W, int max_smem) {
+  if (W % 4 != 0 || encode_fn() == nullptr) return false;
+  const SweepInst *si = find_inst(T);
+  if (si) return (int)si->smem <= max_smem && (int)kHessSmem <= max_smem;
   const int rxy = max(T.r[0], T.r[2]), rz = max(T.r[1], T.r[3]);
-  if (rxy > kMaxSweepRxy || rz > 8 || W % 4 != 0) return false;
-  if ((int)sweep_smem_bytes(rxy) > max_smem) return false;
-  return encode_fn() != nullptr;
+  if (rxy > kMaxSweepRxy || rz > 8) return false;
+  return (int)sweep_smem_bytes(rxy) <= max_smem;
+}
+
+static CUresult encode_map(CUtensorMap *map, const float *base, int W, int H, int D, int nsub, int bw, int bh) {
+  const cuuint64_t dims[4] = {(cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)D, (cuuint64_t)nsub};
+  const cuuint64_t strides[3] = {(cuuint64_t)W * 4, (cuuint64_t)W * H * 4, (cuuint64_t)W * H * D * 4};
+  const cuuint32_t box[4] = {(cuuint32_t)bw, (cuuint32_t)bh, 1, 1};
+  const cuuint32_t estr[4] = {1, 1, 1, 1};
+  return encode_fn()(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, const_cast<float *>(base), dims, strides, box, estr,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+}
+
+bool launch_dog_sweep(const Sub *d_subs, int nsub, int W, int H, int D, const DogTaps &T, const float *norm,
+                      float *dog, int *d_status, int max_smem, cudaStream_t s) {
+  const SweepInst *si = find_inst(T);
+  if (!si || W % 4 != 0 || (int)si->smem > max_smem || encode_fn() == nullptr) return false;
+  if ((reinterpret_cast<uintptr_t>(norm) & 15) != 0) return false;
+  CUtensorMap map_n;
+  if (encode_map(&map_n, norm, W, H, D, nsub, si->bw, si->bh) != CUDA_SUCCESS) return false;
+  const unsigned tiles_d = ceil_div(W, kDTX) * ceil_div(H, kDTY);
+  cudaFuncSetAttribute(si->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)si->smem);
+  KLAUNCH("k_dog_sweep", s, (si->fn<<<dim3(tiles_d, nsub), si->threads, si->smem, s>>>(map_n, T, d_subs, dog,
+                                                                                        d_status)));
+  return true;
 }
 
 int launch_dog_hess(const Sub *d_subs, int nsub, int W, int H, int D, const DogTaps &T, const float *norm,
-                    uint8_t *mask, FgEntry *fg, unsigned long long *fg_count, int *d_status, cudaStream_t s) {
+                    float *dog, uint8_t *mask, FgEntry *fg, unsigned long long *fg_count, int *d_status,
+                    cudaStream_t s) {
   const int rxy = max(T.r[0], T.r[2]), rz = max(T.r[1], T.r[3]);
-  CUtensorMap map;
-  const cuuint64_t dims[4] = {(cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)D, (cuuint64_t)nsub};
-  const cuuint64_t strides[3] = {(cuuint64_t)W * 4, (cuuint64_t)W * H * 4, (cuuint64_t)W * H * D * 4};
-  const cuuint32_t box[4] = {(cuuint32_t)sweep_bw(rxy), (cuuint32_t)sweep_bh(rxy), 1, 1};
-  const cuuint32_t estr[4] = {1, 1, 1, 1};
-  CUresult r = encode_fn()(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, const_cast<float *>(norm), dims, strides, box,
-                           estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                           CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-  if (r != CUDA_SUCCESS) return -1;
-  const size_t smem = sweep_smem_bytes(rxy);
-  const unsigned tiles = ceil_div(W, kSX) * ceil_div(H, kSY);
   cudaMemsetAsync(fg_count, 0, nsub * sizeof(unsigned long long), s);
+  const SweepInst *si = find_inst(T);
+  if (si) {
+    CUtensorMap map_n, map_d;
+    if (encode_map(&map_n, norm, W, H, D, nsub, si->bw, si->bh) != CUDA_SUCCESS) return -1;
+    if (encode_map(&map_d, dog, W, H, D, nsub, kHPX, kHPY) != CUDA_SUCCESS) return -1;
+    const unsigned tiles_d = ceil_div(W, kDTX) * ceil_div(H, kDTY);
+    cudaFuncSetAttribute(si->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)si->smem);
+    KLAUNCH("k_dog_sweep", s, (si->fn<<<dim3(tiles_d, nsub), si->threads, si->smem, s>>>(map_n, T, d_subs, dog,
+                                                                                          d_status)));
+    const unsigned tiles_h = ceil_div(W, kHTX) * ceil_div(H, kHTY);
+    cudaFuncSetAttribute(k_hess_sweep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kHessSmem);
+    KLAUNCH("k_hess_sweep", s, (k_hess_sweep<<<dim3(tiles_h, nsub), kHThreads, kHessSmem, s>>>(
+                                   map_d, d_subs, norm, mask, fg, fg_count, d_status)));
+    return 0;
+  }
+  CUtensorMap map;
+  if (encode_map(&map, norm, W, H, D, nsub, sweep_bw(rxy), sweep_bh(rxy)) != CUDA_SUCCESS) return -1;
+  const unsigned tiles = ceil_div(W, kSX) * ceil_div(H, kSY);
+  const size_t smem = sweep_smem_bytes(rxy);
   if (rz <= 5) {
     cudaFuncSetAttribute(k_dog_hess<5>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     KLAUNCH("k_dog_hess", s, (k_dog_hess<5><<<dim3(tiles, nsub), kSweepThreads, smem, s>>>(

@@ -124,14 +124,25 @@ def test_capacity_error_is_reported():
         assert rc == hdog.HDOG_ERR_CAPACITY and cnt.value == n
 
 
-@pytest.mark.parametrize("W,H,D,dv", [(68, 45, 13, 13), (256, 96, 32, 20), (132, 20, 7, 5), (64, 16, 40, 40)])
-def test_fused_sweep_equals_separate_passes(W, H, D, dv):
+# sigma sets: the workload's (tap radii 4, 6, 3, 5) and the reference example's (8, 12, 4,
+# 5) run the radius-specialised sweep; (4, 6, 3, 3) runs the generic one.
+SIGMA_SETS = {
+    "workload": dict(sigma_xy_small=2.0, sigma_z_small=1.5, sigma_xy_large=3.2, sigma_z_large=2.4),
+    "reference_example": dict(sigma_xy_small=4.0, sigma_z_small=1.8, sigma_xy_large=6.0, sigma_z_large=2.7),
+    "generic": dict(sigma_xy_small=2.0, sigma_z_small=1.5, sigma_xy_large=3.2, sigma_z_large=1.6),
+}
+
+
+@pytest.mark.parametrize("sigmas", sorted(SIGMA_SETS))
+@pytest.mark.parametrize("W,H,D,dv", [(68, 45, 13, 13), (256, 96, 32, 20), (132, 20, 7, 5), (64, 16, 40, 40),
+                                      (184, 70, 24, 24)])
+def test_fused_sweep_equals_separate_passes(W, H, D, dv, sigmas):
     vol = volume(W, H, D, n_nuclei=max(4, W * H * D // 8000), seed=W + H + D)
-    p = params(W, H, D, sigma_z_large=1.6, extra_depth_margin=0)
+    p = params(W, H, D, extra_depth_margin=0, **SIGMA_SETS[sigmas])
     with hdog.Context(p) as ctx:
         fused = ctx.run_substack(np.ascontiguousarray(vol[:dv]), dv, 3)
         ctx.set_fused_sweep(False)
         plain = ctx.run_substack(np.ascontiguousarray(vol[:dv]), dv, 3)
     assert fused.tobytes() == plain.tobytes()
     ref = orc.substack(orc.params_from(p), padded(vol, D, dv), dv, 3)[0]
-    assert_records_match(fused, ref, "fused %dx%dx%d" % (W, H, D))
+    assert_records_match(fused, ref, "fused %dx%dx%d %s" % (W, H, D, sigmas))
