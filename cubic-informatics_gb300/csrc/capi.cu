@@ -175,6 +175,7 @@ struct hdog_ctx {
   int num_sms = 152;
   int max_smem = 48 * 1024;
   bool use_sweep = true;   // fused DoG + Hessian sweep when the parameters allow it
+  std::vector<hdog_record> last;   // records of the last whole-chain call (hdog_last_records)
   int margin = 0;
   DogTaps taps;
   std::mutex mu;
@@ -679,10 +680,10 @@ extern "C" int hdog_run_substack(hdog_ctx *c, const uint16_t *img, int img_on_de
     src = c->img;
   }
   set_sub(c, 0, src, depth_valid, z0);
+  c->last.clear();
   TRY(run_batch(c, 1, st));
-  std::vector<hdog_record> v;
-  TRY(collect_records(c, 1, v, st));
-  return copy_out(v, out, cap, n_records);
+  TRY(collect_records(c, 1, c->last, st));
+  return copy_out(c->last, out, cap, n_records);
 }
 
 // z0 schedule of HDoG3D_main.cpp:309-314.
@@ -731,9 +732,15 @@ extern "C" int hdog_run_stack(hdog_ctx *c, const uint16_t *stack, int stack_on_d
                               hdog_record *out, int64_t cap, int64_t *n_records, void *stream) {
   CTX_GUARD(c);
   if (!stack || !n_records || length < 0 || (cap > 0 && !out)) return fail(HDOG_ERR_ARG, "hdog_run_stack: bad argument");
-  std::vector<hdog_record> v;
-  TRY(run_stack_locked(c, stack, stack_on_device, length, v, (cudaStream_t)stream));
-  return copy_out(v, out, cap, n_records);
+  c->last.clear();
+  TRY(run_stack_locked(c, stack, stack_on_device, length, c->last, (cudaStream_t)stream));
+  return copy_out(c->last, out, cap, n_records);
+}
+
+extern "C" int hdog_last_records(hdog_ctx *c, hdog_record *out, int64_t cap, int64_t *n_records) {
+  if (!c || !n_records || (cap > 0 && !out)) return fail(HDOG_ERR_ARG, "hdog_last_records: bad argument");
+  std::lock_guard<std::mutex> lock(c->mu);
+  return copy_out(c->last, out, cap, n_records);
 }
 
 // ------------------------------------------------------------------ parameter file

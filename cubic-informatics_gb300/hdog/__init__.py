@@ -87,6 +87,7 @@ _SIGNATURES = {
                                          ctypes.POINTER(ctypes.c_int64), _P]),
     "hdog_run_stack": (ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.c_int, _P, ctypes.c_int64,
                                       ctypes.POINTER(ctypes.c_int64), _P]),
+    "hdog_last_records": (ctypes.c_int, [_P, _P, ctypes.c_int64, ctypes.POINTER(ctypes.c_int64)]),
     "hdog_run_param_file": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int]),
     "hdog_ctx_set_option": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int]),
     "hdog_ccl_noalloc": (ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P]),
@@ -350,10 +351,7 @@ class Context:
         n = ctypes.c_int64()
         rc = lib().hdog_run_substack(self._h, ptr, on_dev, int(depth_valid), int(z0), out.ctypes.data, cap,
                                      ctypes.byref(n), _stream(stream) if on_dev else None)
-        if rc == HDOG_ERR_CAPACITY:
-            return self.run_substack(img, depth_valid, z0, cap=int(n.value), stream=stream)
-        check(rc)
-        return out[: n.value].copy()
+        return self._finish(rc, out, n)
 
     def run_stack(self, stack, cap=None, stream=None):
         """All substacks of one stack (length, H, W) in the reference's schedule."""
@@ -364,8 +362,14 @@ class Context:
         n = ctypes.c_int64()
         rc = lib().hdog_run_stack(self._h, ptr, on_dev, length, out.ctypes.data, cap, ctypes.byref(n),
                                   _stream(stream) if on_dev else None)
+        return self._finish(rc, out, n)
+
+    def _finish(self, rc, out, n):
+        """Records of a whole-chain call; a buffer that was too small is refilled from the
+        context's copy of the result, without running the chain again."""
         if rc == HDOG_ERR_CAPACITY:
-            return self.run_stack(stack, cap=int(n.value), stream=stream)
+            out = np.empty(int(n.value), DT_LOCAL)
+            rc = lib().hdog_last_records(self._h, out.ctypes.data, len(out), ctypes.byref(n))
         check(rc)
         return out[: n.value].copy()
 

@@ -136,6 +136,12 @@ int hdog_run_substack(hdog_ctx *ctx, const uint16_t *img, int img_on_device, int
    context has room, records appended in substack order. */
 int hdog_run_stack(hdog_ctx *ctx, const uint16_t *stack, int stack_on_device, int length,
                    hdog_record *out, int64_t cap, int64_t *n_records, void *stream);
+/* The records of the context's last hdog_run_substack / hdog_run_stack call, kept by the
+   context (also after that call returned HDOG_ERR_CAPACITY): a caller whose buffer was
+   too small sizes a new one from *n_records and fetches them here instead of running
+   the chain again.  No counterpart in the reference (HDoG3D_main writes records to a
+   file as it goes). */
+int hdog_last_records(hdog_ctx *ctx, hdog_record *out, int64_t cap, int64_t *n_records);
 /* The HDoG3D_main executable as a call: reads the parameter file, processes every stack,
    writes each dst_path (removed first, then appended per substack). */
 int hdog_run_param_file(const char *param_path, int verbose);

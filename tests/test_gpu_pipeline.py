@@ -5,6 +5,7 @@ order.  structureness / blobness come from region Hessian sums whose summation o
 differs (double accumulation here, the reference's CUB order there): they are checked
 within a relative tolerance stated below, against the oracle's sequential float sums.
 """
+import ctypes
 import os
 import subprocess
 
@@ -115,13 +116,17 @@ def test_capacity_error_is_reported():
     vol = volume(W, H, D, n_nuclei=40, seed=5)
     p = params(W, H, D, sigma_z_large=1.6, extra_depth_margin=1)
     with hdog.Context(p) as ctx:
-        n = len(ctx.run_substack(vol, D, 0))
+        full = ctx.run_substack(vol, D, 0)
+        n = len(full)
         assert n > 2
         out = np.empty(1, hdog.DT_LOCAL)
-        cnt = __import__("ctypes").c_int64()
-        rc = hdog.lib().hdog_run_substack(ctx._h, vol.ctypes.data, 0, D, 0, out.ctypes.data, 1,
-                                          __import__("ctypes").byref(cnt), None)
+        cnt = ctypes.c_int64()
+        rc = hdog.lib().hdog_run_substack(ctx._h, vol.ctypes.data, 0, D, 0, out.ctypes.data, 1, ctypes.byref(cnt), None)
         assert rc == hdog.HDOG_ERR_CAPACITY and cnt.value == n
+        # the context kept the result: fetched without running the chain again
+        again = np.empty(n, hdog.DT_LOCAL)
+        assert hdog.lib().hdog_last_records(ctx._h, again.ctypes.data, n, ctypes.byref(cnt)) == hdog.HDOG_OK
+        assert cnt.value == n and again.tobytes() == full.tobytes()
 
 
 # sigma sets: the workload's (tap radii 4, 6, 3, 5) and the reference example's (8, 12, 4,
