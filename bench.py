@@ -198,6 +198,24 @@ def run_reference(args):
     return 0
 
 
+def profile_case():
+    """A small case of the same kernels for multi-pass ncu captures: one 1280 x 1080 x 32
+    substack (15000 seeded nuclei, the workload's parameters), run twice."""
+    import torch
+    import hdog
+    from hdog import synth
+    w, h, d = 1280, 1080, 32
+    vol = synth.volume(synth.spec(w, h, d, 15000, synth.SEED_BASE + 21, pair_fraction=0.1))
+    p = hdog.make_params(**dict(PARAMS, width=w, height=h, depth=d))
+    with hdog.Context(p) as ctx:
+        dv = torch.from_numpy(vol).cuda()
+        for _ in range(2):
+            r = ctx.run_substack(dv, d, 0)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_case": "1280x1080x32 substack", "records": int(len(r))}))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -205,9 +223,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-case", action="store_true",
+                    help="run one 1280x1080x32 substack twice (the small case the ncu summaries capture)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.profile_case:
+        return profile_case()
 
     import torch
     import hdog

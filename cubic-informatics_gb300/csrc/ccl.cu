@@ -9,8 +9,8 @@
 //
 // Here the same labels come from union-find in three passes, with no host round trip:
 //   1. k_ccl_local: a 64 x 16 x 32 tile (a whole 32-slice substack column) is labelled in
-//      shared memory with 16-bit parents; the tile's foreground edges that leave the
-//      tile (its x and y faces, and the wrap-around offsets) go to a compact edge list.
+//      shared memory over its 2 x 2 x 2 cells (see below); the foreground edges that
+//      leave the tile (its x and y faces, and the wrap-around offsets) go to an edge list.
 //   2. k_ccl_edges: a persistent pass merges those edges in the global label array.
 //      If the list overflowed, k_ccl_cross_direct merges the same edges from the mask.
 //   3. k_ccl_flatten: every foreground voxel gets its root (a read-only walk, so every
@@ -75,17 +75,20 @@ __device__ __forceinline__ void back_offset(int k, int &dz, int &dy, int &dx) {
 
 // ------------------------------------------------------------------ pass 1: tile-local
 constexpr int kTX = 64, kTY = 16, kTZ = 32;
-constexpr int kTileVox = kTX * kTY * kTZ;     // 32768: parents fit in 16 bits
+constexpr int kTileVox = kTX * kTY * kTZ;     // 32768 voxels
 constexpr int kCclThreads = 256;              // thread = 4 x-consecutive voxels of one row, all kTZ slices
-constexpr uint16_t kBg = 0xFFFF;
 
-// Find with path halving (stores an ancestor of the parent only, as in the global
-// version); without it "smaller root wins" linking grows long chains.
-__device__ __forceinline__ int sfind(volatile uint16_t *lab, int t) {
-  int p = lab[t];
+// Shared-memory union-find over the tile's cells, 32-bit parents (native shared atomics;
+// kBg32 marks a background cell).  Find with path halving (stores an ancestor of the
+// parent only, as in the global version); without it "smaller root wins" linking grows
+// long chains.
+constexpr uint32_t kBg32 = 0xFFFFFFFFu;
+
+__device__ __forceinline__ uint32_t sfind(volatile uint32_t *par, uint32_t t) {
+  uint32_t p = par[t];
   while (p != t) {
-    const int gp = lab[p];
-    if (gp != p) lab[t] = (uint16_t)gp;
+    const uint32_t gp = par[p];
+    if (gp != p) par[t] = gp;
     t = p;
     p = gp;
   }
@@ -93,24 +96,23 @@ __device__ __forceinline__ int sfind(volatile uint16_t *lab, int t) {
 }
 
 // Read-only find for the final pass over a finished forest.
-__device__ __forceinline__ int sroot(const uint16_t *lab, int t) {
-  int p = lab[t];
+__device__ __forceinline__ uint32_t sroot(const uint32_t *par, uint32_t t) {
+  uint32_t p = par[t];
   while (p != t) {
     t = p;
-    p = lab[t];
+    p = par[t];
   }
   return t;
 }
 
-__device__ __forceinline__ void sunion(uint16_t *lab, int a, int b) {
-  volatile uint16_t *v = lab;
-  for (int it = 0; it < 2 * kTileVox; it++) {
+__device__ __forceinline__ void sunion(uint32_t *par, uint32_t a, uint32_t b, uint32_t limit) {
+  volatile uint32_t *v = par;
+  for (uint32_t it = 0; it < limit; it++) {
     a = sfind(v, a);
     b = sfind(v, b);
     if (a == b) return;
-    if (a > b) { const int t = a; a = b; b = t; }
-    const unsigned short cur = atomicCAS(reinterpret_cast<unsigned short *>(&lab[b]), (unsigned short)b,
-                                         (unsigned short)a);
+    if (a > b) { const uint32_t t = a; a = b; b = t; }
+    const uint32_t cur = atomicCAS(&par[b], b, a);
     if (cur == b) return;
     b = cur;
   }
@@ -141,177 +143,279 @@ __device__ __forceinline__ bool leaves_tile(const Sub &S, const CclTile &T, int 
   return !(in_vol && in_tile);
 }
 
-constexpr int kFgList = 12288;                // compact foreground list of a tile (37.5%)
+constexpr int kEdgeBuf = 2048;                // cross-tile edges staged per tile before one global reservation
 
-__device__ __forceinline__ uint32_t tile_scan(uint32_t v, uint32_t *total) {
-  __shared__ uint32_t ws[kCclThreads / 32 + 1];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  uint32_t inc = v;
-  for (int d = 1; d < 32; d <<= 1) {
-    const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, inc, d);
-    if (lane >= d) inc += y;
-  }
-  if (lane == 31) ws[w] = inc;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    uint32_t run = 0;
-    for (int k = 0; k < kCclThreads / 32; k++) { const uint32_t c = ws[k]; ws[k] = run; run += c; }
-    ws[kCclThreads / 32] = run;
-  }
-  __syncthreads();
-  const uint32_t r = ws[w] + inc - v;
-  *total = ws[kCclThreads / 32];
-  __syncthreads();
-  return r;
+// ---- cell union-find inside the tile
+// Inside a tile every edge is a plain 26-neighbour step (the reference's row and slice
+// wrap-arounds always leave the tile and go to the edge list), and any two foreground
+// voxels of one 2 x 2 x 2 cell are 26-neighbours.  So the tile is labelled over cells:
+// a cell is one union-find node, its 8-bit occupancy says which voxels are foreground
+// (bit 4*dz + 2*dy + dx, i.e. linear voxel order), and two neighbouring cells are
+// connected exactly when each has a foreground voxel on the side facing the other --
+// two mask tests per pair.  A component's label is then the minimum voxel index over
+// its cells, found with one shared-memory atomicMin per cell.
+constexpr int kCX = kTX / 2, kCY = kTY / 2, kCZ = kTZ / 2;
+constexpr int kCells = kCX * kCY * kCZ;       // 4096
+
+// Occupancy bits of a cell whose voxels have local coordinate `side` along one axis
+// (0 or 1); axis 0 = x, 1 = y, 2 = z.
+__host__ __device__ constexpr uint8_t cell_side(int axis, int side) {
+  uint8_t m = 0;
+  for (int v = 0; v < 8; v++)
+    if (((v >> axis) & 1) == side) m |= (uint8_t)(1u << v);
+  return m;
 }
+// For cell offset d (-1, 0, +1) along an axis: the voxels of this cell (self) and of the
+// neighbour that can touch across it.
+__host__ __device__ constexpr uint8_t cell_face(int axis, int d, bool self) {
+  return d == 0 ? (uint8_t)0xFF : (d < 0 ? cell_side(axis, self ? 0 : 1) : cell_side(axis, self ? 1 : 0));
+}
+struct CellNb {
+  int dz, dy, dx;
+  uint8_t self, other;
+};
+__host__ __device__ constexpr CellNb cell_nb(int dz, int dy, int dx) {
+  return CellNb{dz, dy, dx,
+                (uint8_t)(cell_face(0, dx, true) & cell_face(1, dy, true) & cell_face(2, dz, true)),
+                (uint8_t)(cell_face(0, dx, false) & cell_face(1, dy, false) & cell_face(2, dz, false))};
+}
+// The 13 backward cell neighbours (the other 13 are their mirror images).
+__constant__ CellNb kCellNb[13] = {
+    cell_nb(-1, -1, -1), cell_nb(-1, -1, 0), cell_nb(-1, -1, 1), cell_nb(-1, 0, -1), cell_nb(-1, 0, 0),
+    cell_nb(-1, 0, 1),   cell_nb(-1, 1, -1), cell_nb(-1, 1, 0),  cell_nb(-1, 1, 1),  cell_nb(0, -1, -1),
+    cell_nb(0, -1, 0),   cell_nb(0, -1, 1),  cell_nb(0, 0, -1)};
 
-// Union of tile voxel lt with its backward neighbours inside the tile; counts the
-// foreground edges that leave the tile and, when `emit`, writes them from slot *base.
-__device__ __forceinline__ int tile_voxel_edges(const Sub &S, const CclTile &T, uint16_t *lab, const uint8_t *m,
-                                                int lt, bool do_union, bool emit, int2 *edges,
-                                                unsigned long long *base) {
-  const int lx = lt % kTX, ly = (lt / kTX) % kTY, lz = lt / (kTX * kTY);
-  const int x = T.x0 + lx, y = T.y0 + ly, z = T.z0 + lz;
-  const int64_t WH = (int64_t)S.W * S.H;
-  const int64_t g = z * WH + (int64_t)y * S.W + x;
-  int n_cross = 0;
-  for (int o = 0; o < 13; o++) {
-    int dz, dy, dx;
-    back_offset(o, dz, dy, dx);
-    if (!leaves_tile(S, T, x, y, z, lx, ly, lz, dz, dy, dx)) {
-      if (!do_union) continue;
-      const int ln = lt + (dz * kTY + dy) * kTX + dx;
-      const uint16_t pn = lab[ln];
-      if (pn != kBg && pn != lab[lt]) sunion(lab, lt, ln);
-    } else {
-      const int64_t gn = g + dz * WH + dy * (int64_t)S.W + dx;
-      if (gn >= 1 && m[gn]) {
-        if (emit) {
-          if ((int64_t)*base < S.edge_cap) edges[S.edge + *base] = make_int2((int32_t)g, (int32_t)gn);
-          (*base)++;
-        }
-        n_cross++;
+// Occupancy of a halo-framed block of cells: the tile's cells plus one cell on each x
+// and y side and one layer below (cell coordinates -1 .. kC? along each axis).
+constexpr int kHX = kCX + 2, kHY = kCY + 2, kHZ = kCZ + 1;
+constexpr int kHalo = kHX * kHY * kHZ;        // 5780
+__device__ __forceinline__ int halo_of(int cx, int cy, int cz) { return ((cz + 1) * kHY + (cy + 1)) * kHX + (cx + 1); }
+__device__ __forceinline__ int cell_bit(int lx, int ly, int lz) { return ((lz & 1) << 2) | ((ly & 1) << 1) | (lx & 1); }
+
+// Occupancy of the cell whose first voxel is (x, y, z) (volume coordinates; voxels outside
+// the volume, past depth_valid handling or at index 0 count as background).
+__device__ __forceinline__ uint32_t cell_occ(const Sub &S, const uint8_t *m, int64_t WH, int x, int y, int z) {
+  uint32_t o = 0;
+  if (x + 1 < 0 || x >= S.W || y + 1 < 0 || y >= S.H || z + 1 < 0 || z >= S.D) return 0;
+  const bool pair = x >= 0 && x + 1 < S.W && (S.W % 2 == 0);
+#pragma unroll
+  for (int dz = 0; dz < 2; dz++)
+#pragma unroll
+    for (int dy = 0; dy < 2; dy++) {
+      const int zz = z + dz, yy = y + dy;
+      if (zz < 0 || zz >= S.D || yy < 0 || yy >= S.H) continue;
+      const int64_t g = zz * WH + (int64_t)yy * S.W + x;
+      uint32_t v;
+      if (pair) {
+        const uint16_t two = __ldg(reinterpret_cast<const uint16_t *>(m + g));
+        v = ((two & 0xFFu) ? 1u : 0u) | ((two >> 8) ? 2u : 0u);
+      } else {
+        v = (x >= 0 && m[g]) ? 1u : 0u;
+        if (x + 1 < S.W && m[g + 1]) v |= 2u;
       }
+      if (g == 0) v &= ~1u;   // voxel 0 is background
+      o |= v << (4 * dz + 2 * dy);
     }
-  }
-  return n_cross;
+  return o;
 }
 
 __global__ void __launch_bounds__(kCclThreads) k_ccl_local(const Sub *subs, const uint8_t *mask, int32_t *labels,
                                                           int2 *edges, unsigned long long *edge_count) {
-  extern __shared__ uint16_t lab[];   // kTileVox parents, then kFgList foreground indices
-  uint16_t *fgl = lab + kTileVox;
+  __shared__ uint32_t par[kCells];
+  __shared__ uint8_t occ[kHalo];
+  __shared__ uint32_t minv[kCells];
+  __shared__ int2 ebuf[kEdgeBuf];
+  __shared__ uint32_t n_local_edges;
+  __shared__ unsigned long long edge_base;
   const Sub S = subs[blockIdx.y];
   CclTile T;
   if (!ccl_tile(S, blockIdx.x, T)) return;
   const int t = threadIdx.x;
+  const int64_t WH = (int64_t)S.W * S.H;
+  const int64_t N = WH * S.D;
+  const uint8_t *m = mask + S.vox;
+  if (t == 0) n_local_edges = 0;
+  // 1. occupancy of the tile's cells and of the halo (the layer below only when the tile
+  //    does not start at slice 0); union-find nodes for the tile's cells
+  const int ncz = (T.tz + 1) / 2;
+  for (int h = t; h < kHalo; h += kCclThreads) {
+    const int hx = h % kHX, hy = (h / kHX) % kHY, hz = h / (kHX * kHY);
+    const int cx = hx - 1, cy = hy - 1, cz = hz - 1;
+    uint32_t o = 0;
+    if (cz < ncz && (cz >= 0 || T.z0 > 0)) {
+      o = cell_occ(S, m, WH, T.x0 + 2 * cx, T.y0 + 2 * cy, T.z0 + 2 * cz);
+      if (cz >= 0 && 2 * cz + 1 >= T.tz) o &= 0x0Fu;   // a tile's last odd slice: no second layer
+    }
+    occ[h] = (uint8_t)o;
+    if (cx >= 0 && cx < kCX && cy >= 0 && cy < kCY && cz >= 0) {
+      const int c = (cz * kCY + cy) * kCX + cx;
+      par[c] = o ? (uint32_t)c : kBg32;
+      minv[c] = 0xFFFFFFFFu;
+    }
+  }
+  __syncthreads();
+  // 2. unions between neighbouring cells of the tile.  The unrolled neighbour tests only
+  //    collect a 13-bit list; the unions then run in warp-wide rounds, one per lane and
+  //    round, re-converged after each, so lanes whose finds and retries differ in length
+  //    do not split the warp for the rest of the pass.
+  const int cx = t % kCX, cy = t / kCX;
+  for (int cz = 0; cz < ncz; cz++) {
+    const int c = (cz * kCY + cy) * kCX + cx;
+    const uint32_t oc = occ[halo_of(cx, cy, cz)];
+    uint32_t todo = 0;
+#pragma unroll
+    for (int k = 0; k < 13; k++) {
+      const CellNb nb = kCellNb[k];
+      const int nx = cx + nb.dx, ny = cy + nb.dy, nz = cz + nb.dz;
+      if (nx < 0 || nx >= kCX || ny < 0 || ny >= kCY || nz < 0) continue;
+      if ((oc & nb.self) && (occ[halo_of(nx, ny, nz)] & nb.other)) todo |= 1u << k;
+    }
+    while (__any_sync(0xFFFFFFFFu, todo != 0)) {
+      if (todo) {
+        const int k = __ffs(todo) - 1;
+        todo &= todo - 1;
+        // backward cell offset k: (dz, dy, dx) as in kCellNb
+        const int dz = k < 9 ? -1 : 0;
+        const int dy = k < 9 ? k / 3 - 1 : (k < 12 ? -1 : 0);
+        const int dx = k < 9 ? k % 3 - 1 : (k < 12 ? k - 10 : -1);
+        const int cn = c + (dz * kCY + dy) * kCX + dx;
+        if (par[cn] != par[c]) sunion(par, c, cn, 2 * kCells);
+      }
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+  // 3. roots in place, then each component's minimum voxel (tile order = volume order)
+  for (int cz = 0; cz < ncz; cz++) {
+    const int c = (cz * kCY + cy) * kCX + cx;
+    if (occ[halo_of(cx, cy, cz)]) par[c] = sroot(par, c);
+  }
+  __syncthreads();
+  for (int cz = 0; cz < ncz; cz++) {
+    const int c = (cz * kCY + cy) * kCX + cx;
+    const uint32_t oc = occ[halo_of(cx, cy, cz)];
+    if (!oc) continue;
+    const int b = __ffs(oc) - 1;   // first voxel of the cell in linear order
+    const uint32_t v = ((2 * cz + (b >> 2)) * kTY + 2 * cy + ((b >> 1) & 1)) * kTX + 2 * cx + (b & 1);
+    atomicMin(&minv[par[c]], v);
+  }
+  // 4a. plain cross-tile edges, cell to cell: a face cell and its backward neighbour cell
+  //     outside the tile are connected when their facing voxels are foreground; the edge
+  //     joins the first foreground voxel of each
+  auto first_voxel = [&](int ccx, int ccy, int ccz, uint32_t o) -> int64_t {
+    const int b = __ffs(o) - 1;
+    return (int64_t)(T.z0 + 2 * ccz + (b >> 2)) * WH + (int64_t)(T.y0 + 2 * ccy + ((b >> 1) & 1)) * S.W + T.x0 +
+           2 * ccx + (b & 1);
+  };
+  auto emit = [&](int64_t a, int64_t b) {
+    const uint32_t i = atomicAdd(&n_local_edges, 1u);
+    if (i < (uint32_t)kEdgeBuf) {
+      ebuf[i] = make_int2((int32_t)a, (int32_t)b);
+    } else {
+      const unsigned long long j = atomicAdd(&edge_count[blockIdx.y], 1ull);
+      if ((int64_t)j < S.edge_cap) edges[S.edge + j] = make_int2((int32_t)a, (int32_t)b);
+    }
+  };
+  {
+    constexpr int kFacePerLayer = 2 * kCX + 2 * (kCY - 2);   // rows cy = 0, kCY-1 and columns cx = 0, kCX-1
+    const bool zface = T.z0 > 0;
+    const int nf = zface ? ncz * kFacePerLayer + kCX * kCY : ncz * kFacePerLayer;
+    for (int f = t; f < nf; f += kCclThreads) {
+      int fx, fy, fz;
+      if (f < ncz * kFacePerLayer) {
+        fz = f / kFacePerLayer;
+        const int j = f % kFacePerLayer;
+        if (j < kCX) { fx = j; fy = 0; }
+        else if (j < 2 * kCX) { fx = j - kCX; fy = kCY - 1; }
+        else if (j < 2 * kCX + kCY - 2) { fx = 0; fy = j - 2 * kCX + 1; }
+        else { fx = kCX - 1; fy = j - 2 * kCX - (kCY - 2) + 1; }
+      } else {   // the bottom layer of a tile above slice 0, interior cells (faces done above)
+        const int j = f - ncz * kFacePerLayer;
+        fx = j % kCX; fy = j / kCX; fz = 0;
+        if (fx == 0 || fx == kCX - 1 || fy == 0 || fy == kCY - 1) continue;
+      }
+      const uint32_t oc = occ[halo_of(fx, fy, fz)];
+      if (!oc) continue;
+      uint32_t todo = 0;
+#pragma unroll
+      for (int k = 0; k < 13; k++) {
+        const CellNb nb = kCellNb[k];
+        const int nx = fx + nb.dx, ny = fy + nb.dy, nz = fz + nb.dz;
+        if (nx >= 0 && nx < kCX && ny >= 0 && ny < kCY && nz >= 0) continue;   // inside the tile
+        if (nz < 0 && !zface) continue;
+        if ((oc & nb.self) && (occ[halo_of(nx, ny, nz)] & nb.other)) todo |= 1u << k;
+      }
+      if (!todo) continue;
+      const int64_t a = first_voxel(fx, fy, fz, oc);
+      while (todo) {
+        const int k = __ffs(todo) - 1;
+        todo &= todo - 1;
+        const int dz = k < 9 ? -1 : 0;
+        const int dy = k < 9 ? k / 3 - 1 : (k < 12 ? -1 : 0);
+        const int dx = k < 9 ? k % 3 - 1 : (k < 12 ? k - 10 : -1);
+        const int nx = fx + dx, ny = fy + dy, nz = fz + dz;
+        emit(a, first_voxel(nx, ny, nz, occ[halo_of(nx, ny, nz)]));
+      }
+    }
+  }
+  // 4b. the reference's wrap-around edges: backward linear offsets of a voxel in the first
+  //     or last column or row that leave the row or slice (only border tiles hold such voxels)
+  if (T.x0 == 0 || T.x0 + kTX >= S.W || T.y0 == 0 || T.y0 + kTY >= S.H) {
+    const int lastx = min(kTX - 1, S.W - 1 - T.x0), lasty = min(kTY - 1, S.H - 1 - T.y0);
+    for (int v = t; v < kTX * kTY * T.tz; v += kCclThreads) {
+      const int lx = v % kTX, ly = (v / kTX) % kTY, lz = v / (kTX * kTY);
+      if (lx > lastx || ly > lasty) continue;
+      const int x = T.x0 + lx, y = T.y0 + ly, z = T.z0 + lz;
+      if (x != 0 && x != S.W - 1 && y != 0 && y != S.H - 1) continue;
+      if (!((occ[halo_of(lx >> 1, ly >> 1, lz >> 1)] >> cell_bit(lx, ly, lz)) & 1u)) continue;
+      const int64_t g = z * WH + (int64_t)y * S.W + x;
+      for (int o = 0; o < 13; o++) {
+        int dz, dy, dx;
+        back_offset(o, dz, dy, dx);
+        if (x + dx >= 0 && x + dx < S.W && y + dy >= 0 && y + dy < S.H) continue;   // a plain step
+        const int64_t gn = g + dz * WH + dy * (int64_t)S.W + dx;
+        if (gn >= 1 && gn < N && m[gn]) emit(g, gn);
+      }
+    }
+  }
+  __syncthreads();
+  // 5. staged edges to their global slots
+  if (t == 0) {
+    const uint32_t ne = min(n_local_edges, (uint32_t)kEdgeBuf);
+    edge_base = ne ? atomicAdd(&edge_count[blockIdx.y], (unsigned long long)ne) : 0ull;
+  }
+  __syncthreads();
+  {
+    const uint32_t ne = min(n_local_edges, (uint32_t)kEdgeBuf);
+    for (uint32_t i = t; i < ne; i += kCclThreads) {
+      const unsigned long long j = edge_base + i;
+      if ((int64_t)j < S.edge_cap) edges[S.edge + j] = ebuf[i];
+    }
+  }
+  // 6. labels: the component's minimum voxel as a global index, background -> 0 (whole
+  //    rows, vector stores)
   const int lx0 = (t % (kTX / 4)) * 4, ly = t / (kTX / 4);
   const int x = T.x0 + lx0, y = T.y0 + ly;
-  const int64_t WH = (int64_t)S.W * S.H;
-  const uint8_t *m = mask + S.vox;
-  const bool row_ok = y < S.H;
-  const bool vec = row_ok && x + 3 < S.W && (S.W % 4 == 0) &&
-                   ((reinterpret_cast<uintptr_t>(m + (int64_t)y * S.W + x) & 3) == 0);
-  // 1. foreground -> own tile index, background -> kBg; count this thread's foreground
-  uint32_t nfg = 0;
-  for (int lz = 0; lz < kTZ; lz++) {
-    const int lt = (lz * kTY + ly) * kTX + lx0;
-    uint32_t w = 0;
-    if (lz < T.tz) {
-      const int64_t g = (T.z0 + lz) * WH + (int64_t)y * S.W + x;
-      if (vec) {
-        w = __ldg(reinterpret_cast<const uint32_t *>(m + g));
-      } else if (row_ok) {
-        for (int k = 0; k < 4; k++)
-          if (x + k < S.W && m[g + k]) w |= 0xFFu << (8 * k);
-      }
-      if (g == 0) w &= ~0xFFu;   // voxel 0 is background
-    }
-    ushort4 v;
-    v.x = (w & 0xFFu) ? (uint16_t)lt : kBg;
-    v.y = ((w >> 8) & 0xFFu) ? (uint16_t)(lt + 1) : kBg;
-    v.z = ((w >> 16) & 0xFFu) ? (uint16_t)(lt + 2) : kBg;
-    v.w = (w >> 24) ? (uint16_t)(lt + 3) : kBg;
-    nfg += (v.x != kBg) + (v.y != kBg) + (v.z != kBg) + (v.w != kBg);
-    *reinterpret_cast<ushort4 *>(&lab[lt]) = v;
-  }
-  // 2. compact list of foreground tile indices (block scan of the per-thread counts)
-  uint32_t total;
-  const uint32_t off = tile_scan(nfg, &total);
-  const bool listed = total <= (uint32_t)kFgList;
-  if (listed) {
-    uint32_t o = off;
-    for (int lz = 0; lz < T.tz; lz++)
-      for (int k = 0; k < 4; k++) {
-        const int lt = (lz * kTY + ly) * kTX + lx0 + k;
-        if (lab[lt] != kBg) fgl[o++] = (uint16_t)lt;
-      }
-  }
-  __syncthreads();
-  // 3. unions inside the tile, foreground voxels spread evenly over the threads
-  int n_cross = 0;
-  if (listed) {
-    for (uint32_t i = t; i < total; i += kCclThreads)
-      n_cross += tile_voxel_edges(S, T, lab, m, fgl[i], true, false, nullptr, nullptr);
-  } else {
-    for (int lz = 0; lz < T.tz; lz++)
-      for (int k = 0; k < 4; k++) {
-        const int lt = (lz * kTY + ly) * kTX + lx0 + k;
-        if (lab[lt] != kBg) n_cross += tile_voxel_edges(S, T, lab, m, lt, true, false, nullptr, nullptr);
-      }
-  }
-  __syncthreads();
-  // 4. final roots stored in place (no union runs any more, so only roots are stored)
-  if (listed) {
-    for (uint32_t i = t; i < total; i += kCclThreads) lab[fgl[i]] = (uint16_t)sroot(lab, fgl[i]);
-  } else {
-    for (int lz = 0; lz < T.tz; lz++)
-      for (int k = 0; k < 4; k++) {
-        const int lt = (lz * kTY + ly) * kTX + lx0 + k;
-        if (lab[lt] != kBg) lab[lt] = (uint16_t)sroot(lab, lt);
-      }
-  }
-  // 5. reserve edge slots (one atomic per warp) and emit the edges in the same order
-  const int lane = threadIdx.x & 31;
-  int incl = n_cross;
-  for (int d = 1; d < 32; d <<= 1) {
-    const int v = __shfl_up_sync(0xFFFFFFFFu, incl, d);
-    if (lane >= d) incl += v;
-  }
-  const int warp_total = __shfl_sync(0xFFFFFFFFu, incl, 31);
-  unsigned long long base = 0;
-  if (lane == 31 && warp_total) base = atomicAdd(&edge_count[blockIdx.y], (unsigned long long)warp_total);
-  base = __shfl_sync(0xFFFFFFFFu, base, 31) + (unsigned long long)(incl - n_cross);
-  if (n_cross) {
-    if (listed) {
-      for (uint32_t i = t; i < total; i += kCclThreads)
-        tile_voxel_edges(S, T, lab, m, fgl[i], false, true, edges, &base);
-    } else {
-      for (int lz = 0; lz < T.tz; lz++)
-        for (int k = 0; k < 4; k++) {
-          const int lt = (lz * kTY + ly) * kTX + lx0 + k;
-          if (lab[lt] != kBg) tile_voxel_edges(S, T, lab, m, lt, false, true, edges, &base);
-        }
-    }
-  }
-  __syncthreads();
-  // 6. labels: tile root -> its global index, background -> 0 (whole rows, vector stores)
-  if (!row_ok) return;
+  if (y >= S.H) return;
+  const bool vec = x + 3 < S.W && (S.W % 4 == 0);
   int32_t *L = labels + S.vox;
   for (int lz = 0; lz < T.tz; lz++) {
     const int64_t g = (T.z0 + lz) * WH + (int64_t)y * S.W + x;
-    const ushort4 v = *reinterpret_cast<const ushort4 *>(&lab[(lz * kTY + ly) * kTX + lx0]);
-    const uint16_t r4[4] = {v.x, v.y, v.z, v.w};
     int32_t out[4];
+#pragma unroll
     for (int k = 0; k < 4; k++) {
-      const int r = r4[k];
-      out[k] = r == kBg ? 0
-                        : (int32_t)((T.z0 + r / (kTX * kTY)) * WH + (int64_t)(T.y0 + (r / kTX) % kTY) * S.W + T.x0 +
-                                    r % kTX);
+      const int lx = lx0 + k;
+      out[k] = 0;
+      if ((occ[halo_of(lx >> 1, ly >> 1, lz >> 1)] >> cell_bit(lx, ly, lz)) & 1u) {
+        const uint32_t r = minv[par[((lz >> 1) * kCY + (ly >> 1)) * kCX + (lx >> 1)]];
+        out[k] = (int32_t)((T.z0 + (int)(r / (kTX * kTY))) * WH + (int64_t)(T.y0 + (int)((r / kTX) % kTY)) * S.W +
+                           T.x0 + (int)(r % kTX));
+      }
     }
     if (vec) {
       *reinterpret_cast<int4 *>(L + g) = make_int4(out[0], out[1], out[2], out[3]);
     } else {
+#pragma unroll
       for (int k = 0; k < 4; k++)
         if (x + k < S.W) L[g + k] = out[k];
     }
@@ -423,9 +527,7 @@ void launch_ccl(const Sub *d_subs, int nsub, int max_w, int max_h, int max_d, in
                 uint32_t *blk_counts, int *d_status, int num_sms, cudaStream_t s) {
   const int64_t tiles = (int64_t)ceil_div(max_w, kTX) * ceil_div(max_h, kTY) * ceil_div(max_d, kTZ);
   cudaMemsetAsync(edge_count, 0, nsub * sizeof(unsigned long long), s);
-  const int smem = (kTileVox + kFgList) * (int)sizeof(uint16_t);
-  cudaFuncSetAttribute(k_ccl_local, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  KLAUNCH("k_ccl_local", s, (k_ccl_local<<<dim3((unsigned)tiles, nsub), kCclThreads, smem, s>>>(
+  KLAUNCH("k_ccl_local", s, (k_ccl_local<<<dim3((unsigned)tiles, nsub), kCclThreads, 0, s>>>(
                                 d_subs, mask, labels, edges, edge_count)));
   const unsigned eb = (unsigned)max(1, (8 * num_sms + nsub - 1) / nsub);
   KLAUNCH("k_ccl_edges", s, (k_ccl_edges<<<dim3(eb, nsub), 256, 0, s>>>(d_subs, edges, edge_count, labels,

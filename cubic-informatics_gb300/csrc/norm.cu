@@ -196,11 +196,11 @@ __global__ void __launch_bounds__(256) k_mm_x(const Sub *subs, int r, int ry, in
   // m at x = x0 - r + k (nearest border: positions outside the row take the edge value)
   const int nm = tx + 2 * r, mstride = nm | 1;
   uint32_t *M = G + ry * stride;
-  for (int e = tid; e < ry * nm; e += blockDim.x) {
-    const int rl = e / nm, k = e % nm;
-    const int kc = clampi(x0 - r + k, 0, W - 1) - (x0 - r);
-    M[rl * mstride + k] = __vminu2(A[rl * stride + kc], G[rl * stride + kc + 2 * r]);
-  }
+  for (int rl = w; rl < ry; rl += nw)
+    for (int k = lane; k < nm; k += 32) {
+      const int kc = clampi(x0 - r + k, 0, W - 1) - (x0 - r);
+      M[rl * mstride + k] = __vminu2(A[rl * stride + kc], G[rl * stride + kc + 2 * r]);
+    }
   __syncthreads();
   // sliding sums, C outputs per thread; results staged (over A and G) for coalesced stores
   float2 *stage = reinterpret_cast<float2 *>(smx);
@@ -357,6 +357,44 @@ __global__ void __launch_bounds__(128) k_box_z_norm(const Sub *subs, int rz, flo
   }
 }
 
+// The same pass specialised on the z radius: one thread per (column, chunk of kBoxZK
+// slices), every window input loaded before the first add so that all loads of a thread
+// are in flight together; threadIdx.y picks the chunk, so the chunks of one column share
+// their overlapping inputs through L1.
+template <int RZ>
+__global__ void __launch_bounds__(128) k_box_z_norm_t(const Sub *subs, float min_intensity, const float2 *in,
+                                                      float *norm) {
+  constexpr int L = 2 * RZ + 1, NW = kBoxZK + 2 * RZ;
+  const Sub S = subs[blockIdx.z];
+  const int64_t plane = (int64_t)S.W * S.H;
+  const int64_t p = (int64_t)blockIdx.x * 32 + threadIdx.x;
+  const int z0 = (blockIdx.y * blockDim.y + threadIdx.y) * kBoxZK;
+  const int D = S.D;
+  if (p >= plane || z0 >= D) return;
+  const float2 *col = in + S.vox + p;
+  float2 win[NW];
+#pragma unroll
+  for (int i = 0; i < NW; i++) win[i] = __ldg(col + clampi(z0 - RZ + i, 0, D - 1) * plane);
+  float v[kBoxZK];
+#pragma unroll
+  for (int k = 0; k < kBoxZK; k++) {
+    const int z = min(z0 + k, D - 1);
+    v[k] = z < S.depth_valid ? (float)__ldg(S.src + z * plane + p) : 0.0f;
+  }
+  const float inv = 1.0f / (float)L;
+#pragma unroll
+  for (int k = 0; k < kBoxZK; k++) {
+    float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int j = 0; j < L; j++) acc = add2(acc, win[k + j]);
+    const int z = z0 + k;
+    if (z < D) {
+      const float2 el = mul2(acc, make_float2(inv, inv));
+      norm[S.vox + z * plane + p] = (v[k] >= min_intensity) ? (v[k] - el.x) / (el.y - el.x) : 0.0f;
+    }
+  }
+}
+
 // Copy3DKernel (NormalizeFilter.cu:588-601), used when a normalization radius is 0.
 __global__ void k_copy_norm(const Sub *subs, float min_intensity, float *norm) {
   const Sub S = subs[blockIdx.y];
@@ -453,8 +491,19 @@ void launch_normalize(const Sub *d_subs, int nsub, int W, int H, int D, int rxy,
   const int by = 4;
   dim3 gy((unsigned)((int64_t)ceil_div(W, 32) * ceil_div(H, by * kBoxYK) * D), nsub);
   KLAUNCH("k_box_y", s, (k_box_y<<<gy, dim3(32, by), 0, s>>>(d_subs, rxy, fa, fb)));
-  KLAUNCH("k_box_z_norm", s, (k_box_z_norm<<<dim3(ceil_div(plane, 128), nsub), 128, 0, s>>>(
-                                 d_subs, rz, min_intensity, fb, norm)));
+  const dim3 gz(ceil_div(plane, 32), ceil_div(D, 4 * kBoxZK), nsub), bz(32, 4);
+  switch (rz) {
+#define HDOG_BOXZ_CASE(R)                                                                                   \
+  case R:                                                                                                   \
+    KLAUNCH("k_box_z_norm", s, (k_box_z_norm_t<R><<<gz, bz, 0, s>>>(d_subs, min_intensity, fb, norm)));     \
+    break;
+    HDOG_BOXZ_CASE(1) HDOG_BOXZ_CASE(2) HDOG_BOXZ_CASE(3) HDOG_BOXZ_CASE(4)
+    HDOG_BOXZ_CASE(5) HDOG_BOXZ_CASE(6) HDOG_BOXZ_CASE(7) HDOG_BOXZ_CASE(8)
+#undef HDOG_BOXZ_CASE
+    default:
+      KLAUNCH("k_box_z_norm", s, (k_box_z_norm<<<dim3(ceil_div(plane, 128), nsub), 128, 0, s>>>(
+                                     d_subs, rz, min_intensity, fb, norm)));
+  }
 }
 
 void launch_copy_norm(const Sub *d_subs, int nsub, int64_t max_n, float min_intensity, float *norm,

@@ -429,12 +429,21 @@ __device__ __forceinline__ void z_step(const DogTaps &T, float2 (&a0)[C::WIN], f
   a1[se] = make_float2(0.f, 0.f);
 }
 
-template <class C, int ZA, int ZB, int P = 0>
+// One switch (an indexed jump) over the WIN phases, WIN <= 17.
+template <class C, int ZA, int ZB>
 __device__ __forceinline__ void z_dispatch(int phase, const DogTaps &T, float2 (&a0)[C::WIN], float2 (&a1)[C::WIN],
                                            float2 g0, float2 g1, float &d0, float &d1) {
-  if constexpr (P < C::WIN) {
-    if (phase == P) z_step<C, ZA, ZB, P>(T, a0, a1, g0, g1, d0, d1);
-    else z_dispatch<C, ZA, ZB, P + 1>(phase, T, a0, a1, g0, g1, d0, d1);
+  static_assert(C::WIN <= 17, "z radius above 8");
+  switch (phase) {
+#define HDOG_ZCASE(P)                                                         \
+  case P:                                                                     \
+    if constexpr (P < C::WIN) z_step<C, ZA, ZB, P>(T, a0, a1, g0, g1, d0, d1); \
+    break;
+    HDOG_ZCASE(0) HDOG_ZCASE(1) HDOG_ZCASE(2) HDOG_ZCASE(3) HDOG_ZCASE(4) HDOG_ZCASE(5)
+    HDOG_ZCASE(6) HDOG_ZCASE(7) HDOG_ZCASE(8) HDOG_ZCASE(9) HDOG_ZCASE(10) HDOG_ZCASE(11)
+    HDOG_ZCASE(12) HDOG_ZCASE(13) HDOG_ZCASE(14) HDOG_ZCASE(15) HDOG_ZCASE(16)
+#undef HDOG_ZCASE
+    default: break;
   }
 }
 
