@@ -490,13 +490,20 @@ __global__ void __launch_bounds__(256) k_ccl_flatten(const Sub *subs, uint8_t *m
     } else {
       for (int k = 0; k < 16; k++) mk[k] = (i0 + k < n) ? m[i0 + k] : 0;
     }
+    // level by level over the 16 voxels: their labels, then the labels' parents, so the
+    // loads of a level are in flight together; deeper walks (labels merged across tiles
+    // more than once) continue one by one
+    int32_t l[16], p[16];
+#pragma unroll
+    for (int k = 0; k < 16; k++) l[k] = (mk[k] && i0 + k != 0) ? __ldcg(L + i0 + k) : -1;
+#pragma unroll
+    for (int k = 0; k < 16; k++) p[k] = l[k] >= 0 ? __ldcg(L + l[k]) : -1;
+#pragma unroll
     for (int k = 0; k < 16; k++) {
-      const int64_t i = i0 + k;
-      if (i == 0 || !mk[k]) continue;
-      const int32_t l = __ldcg(L + i);
-      const int32_t r = uf_root(L, l, n, status);
-      if (r != l) L[i] = r;
-      if (r == (int32_t)i) bits |= 1u << k;
+      if (l[k] < 0) continue;
+      const int32_t r = p[k] == l[k] ? l[k] : uf_root(L, p[k], n, status);
+      if (r != l[k]) L[i0 + k] = r;
+      if (r == (int32_t)(i0 + k)) bits |= 1u << k;
     }
   } else {
     // labels produced elsewhere: foreground = nonzero label, roots label themselves

@@ -210,7 +210,7 @@ __global__ void __launch_bounds__(256) k_accumulate(const Sub *subs, const uint8
 // region) and flushes a run whenever the region changes.
 constexpr int kFgChunk = 8;
 
-__global__ void __launch_bounds__(256) k_accumulate_fg(const Sub *subs, const FgEntry *fg,
+__global__ void __launch_bounds__(256, 2) k_accumulate_fg(const Sub *subs, const FgEntry *fg,
                                                        const unsigned long long *fg_count, const int32_t *labels,
                                                        const int32_t *rank, RegionAcc acc, int64_t slots) {
   const Sub S = subs[blockIdx.y];
@@ -219,28 +219,40 @@ __global__ void __launch_bounds__(256) k_accumulate_fg(const Sub *subs, const Fg
   const int W = S.W, H = S.H;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x * kFgChunk;
   for (int64_t e0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * kFgChunk; e0 < cnt; e0 += stride) {
+    // the chunk's gathers level by level (entries, then labels, then ranks), so a thread
+    // has all loads of a level in flight at once instead of one dependent chain per entry
+    const int ne = (int)min((int64_t)kFgChunk, cnt - e0);
+    float4 q0[kFgChunk];
+    int32_t lab[kFgChunk];
+    int32_t rk[kFgChunk];
+    const float4 *src = reinterpret_cast<const float4 *>(fg + S.fg + e0);
+#pragma unroll
+    for (int k = 0; k < kFgChunk; k++)
+      if (k < ne) q0[k] = __ldg(src + 2 * k);
+#pragma unroll
+    for (int k = 0; k < kFgChunk; k++) lab[k] = k < ne ? labels[S.vox + __float_as_int(q0[k].x)] : 0;
+#pragma unroll
+    for (int k = 0; k < kFgChunk; k++) rk[k] = k < ne ? rank[S.vox + lab[k]] : -1;
     RunAcc a;
     run_reset(a, -1);
-    const int64_t e1 = min(e0 + kFgChunk, cnt);
-    for (int64_t e = e0; e < e1; e++) {
-      const float4 *src = reinterpret_cast<const float4 *>(fg + S.fg + e);
-      const float4 q0 = __ldg(src), q1 = __ldg(src + 1);
-      const int32_t i = __float_as_int(q0.x);
-      const int32_t lab = labels[S.vox + i];
-      const int64_t r = rank[S.vox + lab];
-      if (r != a.r) {
+#pragma unroll
+    for (int k = 0; k < kFgChunk; k++) {
+      if (k >= ne) break;
+      const int32_t i = __float_as_int(q0[k].x);
+      const float4 q1 = __ldg(src + 2 * k + 1);
+      if (rk[k] != a.r) {
         run_flush(a, S, acc, slots);
-        run_reset(a, r);
+        run_reset(a, rk[k]);
       }
       const int x = i % W, y = (i / W) % H, z = i / (W * H);
       a.count++;
-      a.max_ord = max(a.max_ord, f2ord(q0.y));
-      a.norm += to_fix(q0.y);
+      a.max_ord = max(a.max_ord, f2ord(q0[k].y));
+      a.norm += to_fix(q0[k].y);
       a.x += (unsigned long long)x;
       a.y += (unsigned long long)y;
       a.z += (unsigned long long)z;
-      a.h[0] += to_fix(q0.z);
-      a.h[1] += to_fix(q0.w);
+      a.h[0] += to_fix(q0[k].z);
+      a.h[1] += to_fix(q0[k].w);
       a.h[2] += to_fix(q1.x);
       a.h[3] += to_fix(q1.y);
       a.h[4] += to_fix(q1.z);

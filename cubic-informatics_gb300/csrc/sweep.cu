@@ -345,6 +345,7 @@ constexpr int kHPX = kHTX + 8;          // Hessian ring row: columns x0-4 .. x0+
 constexpr int kHPY = kHTY + 4;
 constexpr int kHRing = 8;              // ring slots; a slot is 72 x 20 floats = 45 x 128 bytes
 constexpr int kHThreads = kHTX / 4 * kHTY;   // one x quad per thread
+constexpr int kNRing = 4;                     // normalized-slice slots of the Hessian sweep
 
 template <int RA, int RB, int ZA, int ZB>
 struct DogT {
@@ -363,12 +364,27 @@ struct DogT {
   static constexpr size_t SMEM = (size_t)2 * IN_FLOATS * 4 + (size_t)2 * BH * kDTX * 8 + 64;
 };
 
+// Coefficient pairs (small, large) of the taps both scales share, |j| <= min(RA, RB),
+// held in registers for the whole sweep: an f32x2 FMA takes its operands from registers,
+// so pairs re-read from the constant bank would cost a load each use.  Taps of the
+// wider scale alone stay constant-bank operands of scalar FMAs.
+template <int RA, int RB>
+struct TapPairs {
+  static constexpr int RS = RA < RB ? RA : RB;
+  float2 k[2 * RS + 1];
+  __device__ __forceinline__ void load(const DogTaps &T, int ka, int kb) {
+#pragma unroll
+    for (int j = -RS; j <= RS; j++) k[j + RS] = make_float2(T.k[ka][RA - j], T.k[kb][RB - j]);
+  }
+};
+
 // One tap of both scales: j is the input offset, the coefficient index r - j as in the
 // reference's `sum = fma(k[r - j], s[x + j], sum)`.
 template <int RA, int RB, int J>
-__device__ __forceinline__ void tap2(const DogTaps &T, int ka, int kb, float2 v, float2 &acc) {
+__device__ __forceinline__ void tap2(const DogTaps &T, const TapPairs<RA, RB> &K, int ka, int kb, float2 v,
+                                     float2 &acc) {
   constexpr bool a = J >= -RA && J <= RA, b = J >= -RB && J <= RB;
-  if (a && b) acc = fma2(make_float2(T.k[ka][RA - J], T.k[kb][RB - J]), v, acc);
+  if (a && b) acc = fma2(K.k[J + TapPairs<RA, RB>::RS], v, acc);
   else if (b) acc.y = __fmaf_rn(T.k[kb][RB - J], v.y, acc.y);
   else if (a) acc.x = __fmaf_rn(T.k[ka][RA - J], v.x, acc.x);
 }
@@ -377,27 +393,29 @@ template <int RA, int RB, int J, int N>
 struct TapLoop {
   // x pass: taps J .. J+N-1 for the four outputs of an item
   template <int NV>
-  __device__ __forceinline__ static void x4(const DogTaps &T, const float (&w)[NV], int base, float2 (&a)[4]) {
+  __device__ __forceinline__ static void x4(const DogTaps &T, const TapPairs<RA, RB> &K, const float (&w)[NV],
+                                            int base, float2 (&a)[4]) {
     if constexpr (N > 0) {
 #pragma unroll
       for (int o = 0; o < 4; o++) {
         const float x = w[base + o + J];
-        tap2<RA, RB, J>(T, 0, 2, make_float2(x, x), a[o]);
+        tap2<RA, RB, J>(T, K, 0, 2, make_float2(x, x), a[o]);
       }
-      TapLoop<RA, RB, J + 1, N - 1>::x4(T, w, base, a);
+      TapLoop<RA, RB, J + 1, N - 1>::x4(T, K, w, base, a);
     }
   }
   // y pass of rows cy (g0) and cy + 1 (g1): input row i is tap i - R of g0 and tap
   // i - R - 1 of g1, loaded once, in ascending tap order for both
   template <int STRIDE>
-  __device__ __forceinline__ static void y2(const DogTaps &T, const float2 *col, float2 &g0, float2 &g1) {
+  __device__ __forceinline__ static void y2(const DogTaps &T, const TapPairs<RA, RB> &K, const float2 *col,
+                                            float2 &g0, float2 &g1) {
     if constexpr (N > 0) {
       constexpr int R = RA > RB ? RA : RB;
       const float2 v = col[(J + R) * STRIDE];
-      tap2<RA, RB, J>(T, 0, 2, v, g0);
-      if constexpr (J > -R) tap2<RA, RB, J - 1>(T, 0, 2, v, g1);
-      if constexpr (N == 1) tap2<RA, RB, J>(T, 0, 2, col[(J + R + 1) * STRIDE], g1);
-      TapLoop<RA, RB, J + 1, N - 1>::template y2<STRIDE>(T, col, g0, g1);
+      tap2<RA, RB, J>(T, K, 0, 2, v, g0);
+      if constexpr (J > -R) tap2<RA, RB, J - 1>(T, K, 0, 2, v, g1);
+      if constexpr (N == 1) tap2<RA, RB, J>(T, K, 0, 2, col[(J + R + 1) * STRIDE], g1);
+      TapLoop<RA, RB, J + 1, N - 1>::template y2<STRIDE>(T, K, col, g0, g1);
     }
   }
 };
@@ -407,21 +425,21 @@ struct TapLoop {
 // output zy - RZ + WIN.
 template <class C, int ZA, int ZB, int P, int D0, int N>
 struct ZTaps {
-  __device__ __forceinline__ static void run(const DogTaps &T, float2 (&a0)[C::WIN], float2 (&a1)[C::WIN], float2 g0,
-                                             float2 g1) {
+  __device__ __forceinline__ static void run(const DogTaps &T, const TapPairs<ZA, ZB> &K, float2 (&a0)[C::WIN],
+                                             float2 (&a1)[C::WIN], float2 g0, float2 g1) {
     if constexpr (N > 0) {
       constexpr int s = ((P - D0) % C::WIN + C::WIN) % C::WIN;
-      tap2<ZA, ZB, D0>(T, 1, 3, g0, a0[s]);
-      tap2<ZA, ZB, D0>(T, 1, 3, g1, a1[s]);
-      ZTaps<C, ZA, ZB, P, D0 + 1, N - 1>::run(T, a0, a1, g0, g1);
+      tap2<ZA, ZB, D0>(T, K, 1, 3, g0, a0[s]);
+      tap2<ZA, ZB, D0>(T, K, 1, 3, g1, a1[s]);
+      ZTaps<C, ZA, ZB, P, D0 + 1, N - 1>::run(T, K, a0, a1, g0, g1);
     }
   }
 };
 
 template <class C, int ZA, int ZB, int P>
-__device__ __forceinline__ void z_step(const DogTaps &T, float2 (&a0)[C::WIN], float2 (&a1)[C::WIN], float2 g0,
-                                       float2 g1, float &d0, float &d1) {
-  ZTaps<C, ZA, ZB, P, -C::RZ, C::WIN>::run(T, a0, a1, g0, g1);
+__device__ __forceinline__ void z_step(const DogTaps &T, const TapPairs<ZA, ZB> &K, float2 (&a0)[C::WIN],
+                                       float2 (&a1)[C::WIN], float2 g0, float2 g1, float &d0, float &d1) {
+  ZTaps<C, ZA, ZB, P, -C::RZ, C::WIN>::run(T, K, a0, a1, g0, g1);
   constexpr int se = ((P - C::RZ) % C::WIN + C::WIN) % C::WIN;
   d0 = __fmul_rn(__fsub_rn(a0[se].x, a0[se].y), T.normalizer);
   d1 = __fmul_rn(__fsub_rn(a1[se].x, a1[se].y), T.normalizer);
@@ -431,13 +449,14 @@ __device__ __forceinline__ void z_step(const DogTaps &T, float2 (&a0)[C::WIN], f
 
 // One switch (an indexed jump) over the WIN phases, WIN <= 17.
 template <class C, int ZA, int ZB>
-__device__ __forceinline__ void z_dispatch(int phase, const DogTaps &T, float2 (&a0)[C::WIN], float2 (&a1)[C::WIN],
-                                           float2 g0, float2 g1, float &d0, float &d1) {
+__device__ __forceinline__ void z_dispatch(int phase, const DogTaps &T, const TapPairs<ZA, ZB> &K,
+                                           float2 (&a0)[C::WIN], float2 (&a1)[C::WIN], float2 g0, float2 g1, float &d0,
+                                           float &d1) {
   static_assert(C::WIN <= 17, "z radius above 8");
   switch (phase) {
 #define HDOG_ZCASE(P)                                                         \
   case P:                                                                     \
-    if constexpr (P < C::WIN) z_step<C, ZA, ZB, P>(T, a0, a1, g0, g1, d0, d1); \
+    if constexpr (P < C::WIN) z_step<C, ZA, ZB, P>(T, K, a0, a1, g0, g1, d0, d1); \
     break;
     HDOG_ZCASE(0) HDOG_ZCASE(1) HDOG_ZCASE(2) HDOG_ZCASE(3) HDOG_ZCASE(4) HDOG_ZCASE(5)
     HDOG_ZCASE(6) HDOG_ZCASE(7) HDOG_ZCASE(8) HDOG_ZCASE(9) HDOG_ZCASE(10) HDOG_ZCASE(11)
@@ -481,6 +500,10 @@ __global__ void __launch_bounds__(DogT<RA, RB, ZA, ZB>::NT, 1)
   float2 acc0[C::WIN], acc1[C::WIN];
 #pragma unroll
   for (int s = 0; s < C::WIN; s++) { acc0[s] = make_float2(0.f, 0.f); acc1[s] = make_float2(0.f, 0.f); }
+  TapPairs<RA, RB> kxy;
+  TapPairs<ZA, ZB> kz;
+  kxy.load(T, 0, 2);
+  kz.load(T, 1, 3);
   const int nit = D + C::RZ + 1;
   for (int it = 0; it < nit; it++) {
     if (t == 0 && ok && it + 1 < D)
@@ -491,10 +514,10 @@ __global__ void __launch_bounds__(DogT<RA, RB, ZA, ZB>::NT, 1)
     if (zy >= 0) {
       float2 g0 = make_float2(0.f, 0.f), g1 = make_float2(0.f, 0.f);
       if (zy < D)
-        TapLoop<RA, RB, -C::RXY, 2 * C::RXY + 1>::template y2<kDTX>(T, xb + (zy & 1) * C::BH * kDTX + cy * kDTX + cx,
-                                                                     g0, g1);
+        TapLoop<RA, RB, -C::RXY, 2 * C::RXY + 1>::template y2<kDTX>(
+            T, kxy, xb + (zy & 1) * C::BH * kDTX + cy * kDTX + cx, g0, g1);
       float d0, d1;
-      z_dispatch<C, ZA, ZB>(zy % C::WIN, T, acc0, acc1, g0, g1, d0, d1);
+      z_dispatch<C, ZA, ZB>(zy % C::WIN, T, kz, acc0, acc1, g0, g1, d0, d1);
       const int zo = zy - C::RZ;
       if (zo >= 0) {
         if (w0) out0[zo * WH] = d0;
@@ -519,7 +542,7 @@ __global__ void __launch_bounds__(DogT<RA, RB, ZA, ZB>::NT, 1)
           w[i] = f.x; w[i + 1] = f.y; w[i + 2] = f.z; w[i + 3] = f.w;
         }
         float2 a[4] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
-        TapLoop<RA, RB, -C::RXY, 2 * C::RXY + 1>::x4(T, w, C::OFF + C::RXY, a);
+        TapLoop<RA, RB, -C::RXY, 2 * C::RXY + 1>::x4(T, kxy, w, C::OFF + C::RXY, a);
         float4 *o = reinterpret_cast<float4 *>(xo + row * kDTX + 4 * q);
         o[0] = make_float4(a[0].x, a[0].y, a[1].x, a[1].y);
         o[1] = make_float4(a[2].x, a[2].y, a[3].x, a[3].y);
@@ -535,25 +558,35 @@ __global__ void __launch_bounds__(DogT<RA, RB, ZA, ZB>::NT, 1)
 __device__ __forceinline__ float hdiff(float plus, float minus) { return __fmul_rn(__fsub_rn(plus, minus), 0.5f); }
 
 __global__ void __launch_bounds__(kHThreads, 3)
-    k_hess_sweep(const __grid_constant__ CUtensorMap map, const Sub *subs, const float *norm, uint8_t *mask, FgEntry *fg,
-                 unsigned long long *fg_count, int *status) {
+    k_hess_sweep(const __grid_constant__ CUtensorMap map, const __grid_constant__ CUtensorMap nmap, const Sub *subs,
+                 uint8_t *mask, FgEntry *fg, unsigned long long *fg_count, int *status) {
   extern __shared__ __align__(128) unsigned char smem[];
   constexpr int PL = kHPX * kHPY;
   constexpr uint32_t tma_bytes = (uint32_t)(PL * 4);
+  constexpr uint32_t ntma_bytes = (uint32_t)(kHTX * kHTY * 4);
   const Sub S = subs[blockIdx.y];
   const int ntx = (S.W + kHTX - 1) / kHTX, nty = (S.H + kHTY - 1) / kHTY;
   if ((int64_t)blockIdx.x >= (int64_t)ntx * nty) return;
   const int x0 = (int)(blockIdx.x % ntx) * kHTX, y0 = (int)(blockIdx.x / ntx) * kHTY;
   float *ring = reinterpret_cast<float *>(smem);
-  uint64_t *bar = reinterpret_cast<uint64_t *>(smem + (size_t)kHRing * PL * 4);
+  // normalized values of the tile's slice zh (the foreground list carries them), kNRing slots
+  float *nring = reinterpret_cast<float *>(smem + (size_t)kHRing * PL * 4);
+  uint64_t *bar = reinterpret_cast<uint64_t *>(smem + (size_t)kHRing * PL * 4 + (size_t)kNRing * kHTX * kHTY * 4);
+  uint64_t *nbar = bar + kHRing;
   const int t = threadIdx.x;
   const int D = S.D, W = S.W, H = S.H;
   const int32_t WH = W * H;
   if (t == 0) {
     for (int i = 0; i < kHRing; i++) mbar_init(&bar[i], 1);
+    for (int i = 0; i < kNRing; i++) mbar_init(&nbar[i], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
+  // normalized slice z -> slot z % kNRing, use z / kNRing; slices 0 .. 2 up front, then
+  // slice zh + 3 while slice zh is tested (its slot held slice zh - 1, read one barrier earlier)
+  if (t == 0)
+    for (int z = 0; z < 3 && z < D; z++)
+      tma_slice(&nmap, nring + (z % kNRing) * kHTX * kHTY, &nbar[z % kNRing], x0, y0, z, blockIdx.y, ntma_bytes);
   const int tx = x0 - 4, ty = y0 - 2;
   // ring slot of DoG slice z (z = -2 .. D+1; slices outside the volume arrive zero-filled)
   auto slot = [](int z) { return (z + 2 * kHRing) % kHRing; };
@@ -572,11 +605,13 @@ __global__ void __launch_bounds__(kHThreads, 3)
     }
   const int q = t % (kHTX / 4), ly = t / (kHTX / 4);
   const int X0 = x0 + 4 * q, Y = y0 + ly;
-  const bool interior = x0 >= 1 && x0 + kHTX < W && y0 >= 1 && y0 + kHTY < H;
   const int b = (ly + 2) * kHPX + 4 * q;   // ring index of column X0 - 4 on row Y
   for (int zh = 0; zh < D; zh++) {
     if (t == 0 && ok && zh + 5 <= D + 1)
       tma_slice(&map, ring + slot(zh + 5) * PL, &bar[slot(zh + 5)], tx, ty, zh + 5, blockIdx.y, tma_bytes);
+    if (t == 0 && ok && zh + 3 < D)
+      tma_slice(&nmap, nring + ((zh + 3) % kNRing) * kHTX * kHTY, &nbar[(zh + 3) % kNRing], x0, y0, zh + 3, blockIdx.y,
+                ntma_bytes);
     // slices zh-2 .. zh+1 were waited for already; zh+2 is new
     if (ok && !mbar_wait(&bar[slot(zh + 2)], use(zh + 2) & 1)) {
       ok = false;
@@ -589,7 +624,9 @@ __global__ void __launch_bounds__(kHThreads, 3)
     bool fgv[4] = {false, false, false, false};
     int nfg = 0;
     const int32_t i0 = zh * WH + Y * W + X0;
-    if (interior) {
+    // every in-plane gradient position of the quad inside the volume: the plain stencil
+    // (only the z neighbours can fall outside, handled by zup / zdn)
+    if (X0 >= 1 && X0 + 3 <= W - 2 && Y >= 1 && Y <= H - 2) {
       auto ld12 = [&](const float *src, float *dst) {   // columns X0-4 .. X0+7
 #pragma unroll
         for (int i = 0; i < 3; i++) {
@@ -686,6 +723,11 @@ __global__ void __launch_bounds__(kHThreads, 3)
       }
     }
     // warp-aggregated append to the foreground list (every lane of the block takes part)
+    if (ok && !mbar_wait(&nbar[zh % kNRing], (zh / kNRing) & 1)) {
+      ok = false;
+      atomicExch(status, HDOG_ERR_TIMEOUT);
+    }
+    const float *nslice = nring + (zh % kNRing) * kHTX * kHTY;
     const int lane = t & 31;
     int incl = nfg;
     for (int dd = 1; dd < 32; dd <<= 1) {
@@ -701,7 +743,7 @@ __global__ void __launch_bounds__(kHThreads, 3)
       if (!fgv[o]) continue;
       if ((int64_t)base < S.fg_cap) {
         float4 *dst = reinterpret_cast<float4 *>(fg + S.fg + base);
-        dst[0] = make_float4(__int_as_float(i0 + o), __ldcg(norm + S.vox + i0 + o), hv[o][0], hv[o][1]);
+        dst[0] = make_float4(__int_as_float(i0 + o), nslice[ly * kHTX + 4 * q + o], hv[o][0], hv[o][1]);
         dst[1] = make_float4(hv[o][2], hv[o][3], hv[o][4], hv[o][5]);
       }
       base++;
@@ -749,7 +791,8 @@ static const SweepInst *find_inst(const DogTaps &T) {
   return nullptr;
 }
 
-static constexpr size_t kHessSmem = (size_t)kHRing * kHPX * kHPY * 4 + kHRing * 8;
+static constexpr size_t kHessSmem =
+    (size_t)kHRing * kHPX * kHPY * 4 + (size_t)kNRing * kHTX * kHTY * 4 + (kHRing + kNRing) * 8;
 static_assert((kHPX * kHPY * 4) % 128 == 0, "TMA ring slots must start on 128-byte boundaries");
 
 // Whether the fused sweep handles these parameters (else the separate passes run).
@@ -793,9 +836,10 @@ int launch_dog_hess(const Sub *d_subs, int nsub, int W, int H, int D, const DogT
   cudaMemsetAsync(fg_count, 0, nsub * sizeof(unsigned long long), s);
   const SweepInst *si = find_inst(T);
   if (si) {
-    CUtensorMap map_n, map_d;
+    CUtensorMap map_n, map_d, map_t;
     if (encode_map(&map_n, norm, W, H, D, nsub, si->bw, si->bh) != CUDA_SUCCESS) return -1;
     if (encode_map(&map_d, dog, W, H, D, nsub, kHPX, kHPY) != CUDA_SUCCESS) return -1;
+    if (encode_map(&map_t, norm, W, H, D, nsub, kHTX, kHTY) != CUDA_SUCCESS) return -1;
     const unsigned tiles_d = ceil_div(W, kDTX) * ceil_div(H, kDTY);
     cudaFuncSetAttribute(si->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)si->smem);
     KLAUNCH("k_dog_sweep", s, (si->fn<<<dim3(tiles_d, nsub), si->threads, si->smem, s>>>(map_n, T, d_subs, dog,
@@ -803,7 +847,7 @@ int launch_dog_hess(const Sub *d_subs, int nsub, int W, int H, int D, const DogT
     const unsigned tiles_h = ceil_div(W, kHTX) * ceil_div(H, kHTY);
     cudaFuncSetAttribute(k_hess_sweep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kHessSmem);
     KLAUNCH("k_hess_sweep", s, (k_hess_sweep<<<dim3(tiles_h, nsub), kHThreads, kHessSmem, s>>>(
-                                   map_d, d_subs, norm, mask, fg, fg_count, d_status)));
+                                   map_d, map_t, d_subs, mask, fg, fg_count, d_status)));
     return 0;
   }
   CUtensorMap map;
