@@ -22,6 +22,8 @@
 // kernel finishes without further waits.
 #include <cuda.h>
 
+#include <type_traits>
+
 #include "kernels.cuh"
 
 namespace hdog {
@@ -447,23 +449,20 @@ __device__ __forceinline__ void z_step(const DogTaps &T, const TapPairs<ZA, ZB> 
   a1[se] = make_float2(0.f, 0.f);
 }
 
-// One switch (an indexed jump) over the WIN phases, WIN <= 17.
-template <class C, int ZA, int ZB>
-__device__ __forceinline__ void z_dispatch(int phase, const DogTaps &T, const TapPairs<ZA, ZB> &K,
-                                           float2 (&a0)[C::WIN], float2 (&a1)[C::WIN], float2 g0, float2 g1, float &d0,
-                                           float &d1) {
-  static_assert(C::WIN <= 17, "z radius above 8");
-  switch (phase) {
-#define HDOG_ZCASE(P)                                                         \
-  case P:                                                                     \
-    if constexpr (P < C::WIN) z_step<C, ZA, ZB, P>(T, K, a0, a1, g0, g1, d0, d1); \
-    break;
-    HDOG_ZCASE(0) HDOG_ZCASE(1) HDOG_ZCASE(2) HDOG_ZCASE(3) HDOG_ZCASE(4) HDOG_ZCASE(5)
-    HDOG_ZCASE(6) HDOG_ZCASE(7) HDOG_ZCASE(8) HDOG_ZCASE(9) HDOG_ZCASE(10) HDOG_ZCASE(11)
-    HDOG_ZCASE(12) HDOG_ZCASE(13) HDOG_ZCASE(14) HDOG_ZCASE(15) HDOG_ZCASE(16)
-#undef HDOG_ZCASE
-    default: break;
+// Calls f(base + P, integral_constant<P>) for P = 0 .. N-1 while base + P < limit (the
+// bound is uniform over the block, so every thread runs the same steps).
+template <int P, int N, class F>
+__device__ __forceinline__ void unroll_steps_from(F &f, int base, int limit) {
+  if constexpr (P < N) {
+    if (base + P < limit) {
+      f(base + P, std::integral_constant<int, P>{});
+      unroll_steps_from<P + 1, N>(f, base, limit);
+    }
   }
+}
+template <int N, class F>
+__device__ __forceinline__ void unroll_steps(F &f, int base, int limit) {
+  unroll_steps_from<0, N>(f, base, limit);
 }
 
 template <int RA, int RB, int ZA, int ZB>
@@ -505,7 +504,11 @@ __global__ void __launch_bounds__(DogT<RA, RB, ZA, ZB>::NT, 1)
   kxy.load(T, 0, 2);
   kz.load(T, 1, 3);
   const int nit = D + C::RZ + 1;
-  for (int it = 0; it < nit; it++) {
+  // One slice step; PC is the step's position inside a group of WIN steps, so the z phase
+  // of slice zy = it - 1 is the compile-time (PC - 1) mod WIN and every shift-register slot
+  // is a fixed register (the loop below runs WIN steps per trip).
+  auto step = [&](int it, auto PC) {
+    constexpr int PH = (decltype(PC)::value + C::WIN - 1) % C::WIN;
     if (t == 0 && ok && it + 1 < D)
       tma_slice(&map, inb + ((it + 1) & 1) * C::IN_FLOATS, &bar[(it + 1) & 1], tx, ty, it + 1, blockIdx.y, tma_bytes);
     // ---- B: y pass of slice zy (zero past the volume: the border taps still multiply),
@@ -517,7 +520,7 @@ __global__ void __launch_bounds__(DogT<RA, RB, ZA, ZB>::NT, 1)
         TapLoop<RA, RB, -C::RXY, 2 * C::RXY + 1>::template y2<kDTX>(
             T, kxy, xb + (zy & 1) * C::BH * kDTX + cy * kDTX + cx, g0, g1);
       float d0, d1;
-      z_dispatch<C, ZA, ZB>(zy % C::WIN, T, kz, acc0, acc1, g0, g1, d0, d1);
+      z_step<C, ZA, ZB, PH>(T, kz, acc0, acc1, g0, g1, d0, d1);
       const int zo = zy - C::RZ;
       if (zo >= 0) {
         if (w0) out0[zo * WH] = d0;
@@ -549,7 +552,9 @@ __global__ void __launch_bounds__(DogT<RA, RB, ZA, ZB>::NT, 1)
       }
     }
     __syncthreads();
-  }
+  };
+  for (int base = 0; base < nit; base += C::WIN)
+    unroll_steps<C::WIN>(step, base, nit);
 }
 
 // Central difference of the Hessian stage.  The reference writes ((0 + a) - b) * 0.5; the
