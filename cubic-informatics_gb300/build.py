@@ -19,6 +19,9 @@ NVFLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xco
 LIB = os.path.join(OUT, "libhdog.so")
 SYNTH = os.path.join(OUT, "libhdog_synth.so")
 MAIN = os.path.join(OUT, "hdog_main")
+STAGE = os.path.join(OUT, "hdog_stage_test")
+STAGE_DIR = os.path.join(OUT, "test")
+STAGE_NAMES = ["Normalize_test", "DoG_test", "Hessian_test", "CCL_test", "Regional_test"]
 
 
 def _mtime(p):
@@ -76,6 +79,15 @@ def build(verbose=False):
     main_src = os.path.join(CSRC, "hdog_main.cpp")
     if _stale(MAIN, [main_src, LIB]):
         _run(["g++", "-O2", "-std=c++17", "-o", MAIN, main_src, "-L" + OUT, "-lhdog", "-Wl,-rpath,$ORIGIN"])
+    # the reference's stage programs (test/*_test): one binary, linked under their names
+    stage_src = os.path.join(CSRC, "hdog_stage_test.cpp")
+    if _stale(STAGE, [stage_src, os.path.join(CSRC, "json_min.hpp"), LIB]):
+        _run(["g++", "-O2", "-std=c++17", "-o", STAGE, stage_src, "-L" + OUT, "-lhdog", "-Wl,-rpath,$ORIGIN:$ORIGIN/.."])
+    os.makedirs(STAGE_DIR, exist_ok=True)
+    for name in STAGE_NAMES:
+        link = os.path.join(STAGE_DIR, name)
+        if not os.path.lexists(link):
+            os.symlink(os.path.join("..", os.path.basename(STAGE)), link)
     return LIB
 
 

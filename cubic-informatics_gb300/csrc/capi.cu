@@ -442,18 +442,24 @@ static ScanSeg rseg_of(hdog_ctx *c) {
                  (c->reg_cap + kFinalizeBlock - 1) / kFinalizeBlock};
 }
 
-// Normalization of nsub substacks (descriptors already uploaded): src -> out_norm.
-static void enqueue_normalize(hdog_ctx *c, int nsub, float *out_norm, cudaStream_t st) {
+// Normalization of nsub substacks (descriptors already uploaded): src -> out_norm, and
+// the box means of the min and the max when ero_l / dil_l are given.
+static void enqueue_normalize(hdog_ctx *c, int nsub, float *out_norm, cudaStream_t st, float *ero_l = nullptr,
+                              float *dil_l = nullptr) {
   const hdog_params &p = c->p;
   if (p.radius_norm_xy == 0 || p.radius_norm_z == 0) {
     launch_copy_norm(c->d_subs, nsub, c->nvox, (float)p.min_intensity, out_norm, st);
+    if (ero_l) {   // no box means on the copy path: zero planes
+      cudaMemsetAsync(ero_l, 0, (size_t)nsub * c->nvox * sizeof(float), st);
+      cudaMemsetAsync(dil_l, 0, (size_t)nsub * c->nvox * sizeof(float), st);
+    }
     return;
   }
   // min/max (exact) z -> y -> x, box means x -> y -> z; packed u32 in fb's halves
   uint32_t *ma = reinterpret_cast<uint32_t *>(c->fb);
   uint32_t *mb = ma + (int64_t)c->max_sub * c->nvox;
   launch_normalize(c->d_subs, nsub, c->W, c->H, c->D, p.radius_norm_xy, p.radius_norm_z, (float)p.min_intensity,
-                   srcs_aligned8(c, nsub), ma, mb, c->fa, c->fb, out_norm, st);
+                   srcs_aligned8(c, nsub), ma, mb, c->fa, c->fb, out_norm, st, ero_l, dil_l);
 }
 
 // DoG volume: the radius-specialised z-sweep where it applies (bit-identical), else the
@@ -584,6 +590,17 @@ extern "C" int hdog_normalize(hdog_ctx *c, const uint16_t *d_img, float *d_norm,
   return HDOG_OK;
 }
 
+extern "C" int hdog_normalize_parts(hdog_ctx *c, const uint16_t *d_img, float *d_norm, float *d_ero_l, float *d_dil_l,
+                                    void *stream) {
+  CTX_GUARD(c);
+  if (!d_img || !d_norm || !d_ero_l || !d_dil_l) return fail(HDOG_ERR_ARG, "hdog_normalize_parts: null buffer");
+  cudaStream_t st = (cudaStream_t)stream;
+  TRY(single_sub(c, d_img, st));
+  enqueue_normalize(c, 1, d_norm, st, d_ero_l, d_dil_l);
+  HDOG_CUDA_TRY(cudaGetLastError());
+  return HDOG_OK;
+}
+
 extern "C" int hdog_dog(hdog_ctx *c, const float *d_norm, float *d_dog, void *stream) {
   CTX_GUARD(c);
   if (!d_norm || !d_dog) return fail(HDOG_ERR_ARG, "hdog_dog: null buffer");
@@ -649,6 +666,7 @@ extern "C" int hdog_regional_features(hdog_ctx *c, const int32_t *d_labels, cons
   out->centroid = c->out.centroid;
   out->hessian = c->out.hessian;
   out->eigen = c->out.eigen;
+  out->pitch = c->slots;
   return HDOG_OK;
 }
 

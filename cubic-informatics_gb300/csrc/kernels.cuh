@@ -61,9 +61,10 @@ inline unsigned ceil_div(int64_t a, int64_t b) { return (unsigned)((a + b - 1) /
 // ---- norm.cu ----
 // ma, mb: packed u32 volumes; fa, fb: float2 volumes (ma/mb may alias fb's two halves).
 // src_aligned8: every substack's src is 8-byte aligned (four-column z loads).
+// ero_l, dil_l (optional): also write the box means of the min and the max.
 void launch_normalize(const Sub *d_subs, int nsub, int W, int H, int D, int rxy, int rz, float min_intensity,
                       bool src_aligned8, uint32_t *ma, uint32_t *mb, float2 *fa, float2 *fb, float *norm,
-                      cudaStream_t s);
+                      cudaStream_t s, float *ero_l = nullptr, float *dil_l = nullptr);
 void launch_copy_norm(const Sub *d_subs, int nsub, int64_t max_n, float min_intensity,
                       float *norm, cudaStream_t s);
 // tmp: two packed u32 volumes of nsub substacks each; dst: uint16 (substack s at S.vox).

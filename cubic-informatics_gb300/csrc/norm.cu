@@ -334,7 +334,7 @@ __global__ void __launch_bounds__(128) k_box_y(const Sub *subs, int r, const flo
 constexpr int kBoxZK = 8;
 
 __global__ void __launch_bounds__(128) k_box_z_norm(const Sub *subs, int rz, float min_intensity, const float2 *in,
-                                                    float *norm) {
+                                                    float *norm, float *ero_l, float *dil_l) {
   const Sub S = subs[blockIdx.y];
   const int64_t plane = (int64_t)S.W * S.H;
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -352,6 +352,10 @@ __global__ void __launch_bounds__(128) k_box_z_norm(const Sub *subs, int rz, flo
         const float2 el = mul2(acc[k], make_float2(inv, inv));
         const float v = z < S.depth_valid ? (float)__ldg(S.src + z * plane + p) : 0.0f;
         norm[S.vox + z * plane + p] = (v >= min_intensity) ? (v - el.x) / (el.y - el.x) : 0.0f;
+        if (ero_l) {
+          ero_l[S.vox + z * plane + p] = el.x;
+          dil_l[S.vox + z * plane + p] = el.y;
+        }
       }
     }
   }
@@ -363,7 +367,7 @@ __global__ void __launch_bounds__(128) k_box_z_norm(const Sub *subs, int rz, flo
 // their overlapping inputs through L1.
 template <int RZ>
 __global__ void __launch_bounds__(128) k_box_z_norm_t(const Sub *subs, float min_intensity, const float2 *in,
-                                                      float *norm) {
+                                                      float *norm, float *ero_l, float *dil_l) {
   constexpr int L = 2 * RZ + 1, NW = kBoxZK + 2 * RZ;
   const Sub S = subs[blockIdx.z];
   const int64_t plane = (int64_t)S.W * S.H;
@@ -391,6 +395,10 @@ __global__ void __launch_bounds__(128) k_box_z_norm_t(const Sub *subs, float min
     if (z < D) {
       const float2 el = mul2(acc, make_float2(inv, inv));
       norm[S.vox + z * plane + p] = (v[k] >= min_intensity) ? (v[k] - el.x) / (el.y - el.x) : 0.0f;
+      if (ero_l) {   // the box means themselves, for stage dumps
+        ero_l[S.vox + z * plane + p] = el.x;
+        dil_l[S.vox + z * plane + p] = el.y;
+      }
     }
   }
 }
@@ -474,7 +482,7 @@ static void mm_x(const Sub *d_subs, int nsub, int W, int64_t rows, int r, const 
 
 void launch_normalize(const Sub *d_subs, int nsub, int W, int H, int D, int rxy, int rz, float min_intensity,
                       bool src_aligned8, uint32_t *ma, uint32_t *mb, float2 *fa, float2 *fb, float *norm,
-                      cudaStream_t s) {
+                      cudaStream_t s, float *ero_l, float *dil_l) {
   const int plane = W * H;
   const int64_t rows = (int64_t)H * D;
   mm_z<0>(d_subs, nsub, plane, rz, src_aligned8 && plane % 4 == 0, ma, s);
@@ -495,14 +503,14 @@ void launch_normalize(const Sub *d_subs, int nsub, int W, int H, int D, int rxy,
   switch (rz) {
 #define HDOG_BOXZ_CASE(R)                                                                                   \
   case R:                                                                                                   \
-    KLAUNCH("k_box_z_norm", s, (k_box_z_norm_t<R><<<gz, bz, 0, s>>>(d_subs, min_intensity, fb, norm)));     \
+    KLAUNCH("k_box_z_norm", s, (k_box_z_norm_t<R><<<gz, bz, 0, s>>>(d_subs, min_intensity, fb, norm, ero_l, dil_l))); \
     break;
     HDOG_BOXZ_CASE(1) HDOG_BOXZ_CASE(2) HDOG_BOXZ_CASE(3) HDOG_BOXZ_CASE(4)
     HDOG_BOXZ_CASE(5) HDOG_BOXZ_CASE(6) HDOG_BOXZ_CASE(7) HDOG_BOXZ_CASE(8)
 #undef HDOG_BOXZ_CASE
     default:
       KLAUNCH("k_box_z_norm", s, (k_box_z_norm<<<dim3(ceil_div(plane, 128), nsub), 128, 0, s>>>(
-                                     d_subs, rz, min_intensity, fb, norm)));
+                                     d_subs, rz, min_intensity, fb, norm, ero_l, dil_l)));
   }
 }
 

@@ -64,6 +64,7 @@ class hdog_regions(ctypes.Structure):
         ("num_regions", ctypes.c_int64),
         ("label", ctypes.c_void_p), ("count", ctypes.c_void_p), ("intensity", ctypes.c_void_p),
         ("centroid", ctypes.c_void_p), ("hessian", ctypes.c_void_p), ("eigen", ctypes.c_void_p),
+        ("pitch", ctypes.c_int64),
     ]
 
 
@@ -78,6 +79,7 @@ _SIGNATURES = {
     "hdog_ctx_destroy": (ctypes.c_int, [_P]),
     "hdog_ctx_bytes": (ctypes.c_int, [ctypes.POINTER(hdog_params), ctypes.c_int, ctypes.POINTER(ctypes.c_size_t)]),
     "hdog_normalize": (ctypes.c_int, [_P, _P, _P, _P]),
+    "hdog_normalize_parts": (ctypes.c_int, [_P, _P, _P, _P, _P, _P]),
     "hdog_dog": (ctypes.c_int, [_P, _P, _P, _P]),
     "hdog_hessian_pd": (ctypes.c_int, [_P, _P, _P, _P, _P]),
     "hdog_ccl": (ctypes.c_int, [_P, _P, _P, _P]),
@@ -279,6 +281,15 @@ class Context:
         check(lib().hdog_normalize(self._h, _ptr(img), _ptr(out), _stream(stream)))
         return out
 
+    def normalize_parts(self, img, stream=None):
+        """(norm, erosion_l, dilation_l): the normalized volume and the box means of the
+        min and the max it divides by (test/Normalize_test.cpp dumps all three)."""
+        import torch
+        assert img.dtype == torch.uint16 and img.is_cuda and img.is_contiguous()
+        norm, ero, dil = (self._empty(torch.float32) for _ in range(3))
+        check(lib().hdog_normalize_parts(self._h, _ptr(img), _ptr(norm), _ptr(ero), _ptr(dil), _stream(stream)))
+        return norm, ero, dil
+
     # DoG3DFilter (src/3D/DoG3DFilter.cu:431-437)
     def dog(self, norm, out=None, stream=None):
         import torch
@@ -311,7 +322,7 @@ class Context:
         check(lib().hdog_regional_features(self._h, _ptr(labels), _ptr(norm), _ptr(dog), ctypes.byref(r),
                                            _stream(stream)))
         n = int(r.num_regions)
-        cap = self._slots_stride()
+        cap = int(r.pitch)
 
         def fetch(ptr, dtype, rows=1):
             out = np.empty((rows, n), dtype)
@@ -329,11 +340,6 @@ class Context:
             "hessian": fetch(r.hessian, np.float32, 6),
             "eigen": fetch(r.eigen, np.float32, 2),
         }
-
-    def _slots_stride(self):
-        p = self.params
-        reg_cap = ((p.width + 1) // 2) * ((p.height + 1) // 2) * ((p.depth + 1) // 2) + 1
-        return reg_cap * self.max_substacks
 
     # Erosion3DFilter (src/3D/Erosion3DFilter.cu:260-268)
     def erosion(self, src, radius_xy, radius_z, stream=None):

@@ -38,7 +38,7 @@
 extern "C" {
 #endif
 
-#define HDOG_ABI_VERSION 1
+#define HDOG_ABI_VERSION 2
 
 enum {
   HDOG_OK = 0,
@@ -85,9 +85,10 @@ typedef struct hdog_regions {
   const int32_t *label;         /* [num_regions] */
   const uint32_t *count;        /* [num_regions] exact voxel count (records keep count & 0xFFFF) */
   const float *intensity;       /* [num_regions] max (or sum, is_ave_mode) of normalized intensity */
-  const float *centroid;        /* [3][num_regions] x, y, z (sum / (float)(uint16)count) */
-  const float *hessian;         /* [6][num_regions] sums of xx, xy, xz, yy, yz, zz */
-  const float *eigen;           /* [2][num_regions] structureness, blobness */
+  const float *centroid;        /* [3][pitch], first num_regions of each row: x, y, z (sum / (float)(uint16)count) */
+  const float *hessian;         /* [6][pitch]: sums of xx, xy, xz, yy, yz, zz */
+  const float *eigen;           /* [2][pitch]: structureness, blobness */
+  int64_t pitch;                /* elements between the rows of centroid, hessian and eigen */
 } hdog_regions;
 
 typedef struct hdog_ctx hdog_ctx;
@@ -112,6 +113,12 @@ int hdog_ctx_bytes(const hdog_params *p, int max_substacks, size_t *bytes);
 
 /* ---- stages (device pointers, one substack of width x height x depth, on `stream`) ---- */
 int hdog_normalize(hdog_ctx *ctx, const uint16_t *d_img, float *d_norm, void *stream);
+/* hdog_normalize plus the two box means it divides by: d_ero_l = box mean of the min,
+   d_dil_l = box mean of the max (the d_erosion_l / d_dilation_l of Normalize3DFilter,
+   src/3D/NormalizeFilter.cu:603-654, dumped by test/Normalize_test.cpp:95-118).  With a
+   normalization radius of 0 (the copy path, which computes no box means) both are zero. */
+int hdog_normalize_parts(hdog_ctx *ctx, const uint16_t *d_img, float *d_norm, float *d_ero_l, float *d_dil_l,
+                         void *stream);
 int hdog_dog(hdog_ctx *ctx, const float *d_norm, float *d_dog, void *stream);
 /* d_hessian may be NULL; when given it receives the six planes xx,xy,xz,yy,yz,zz (pitch N). */
 int hdog_hessian_pd(hdog_ctx *ctx, const float *d_dog, uint8_t *d_mask, float *d_hessian,

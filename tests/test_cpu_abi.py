@@ -32,7 +32,7 @@ def test_library_exports_every_declared_symbol():
 def test_struct_layouts():
     assert hdog.DT_LOCAL.itemsize == 28          # FeatureVector, src/3D/utils.h:188-197
     assert ctypes.sizeof(hdog.hdog_params) == 21 * 4
-    assert hdog.lib().hdog_abi_version() == 1
+    assert hdog.lib().hdog_abi_version() == 2
 
 
 @pytest.mark.parametrize("sigma", [0.0, 0.4, 1.5, 1.8, 2.0, 2.4, 2.7, 3.2, 4.0, 6.0, 12.3])
