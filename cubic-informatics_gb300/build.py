@@ -3,6 +3,7 @@ in-tree under _build/.  Run as a script or call build(); rebuilds only what chan
 import concurrent.futures as cf
 import os
 import platform
+import shutil
 import subprocess
 import sys
 
@@ -48,7 +49,11 @@ def _arch_guard():
     if os.path.exists(stamp) and open(stamp).read().strip() == here:
         return
     for f in os.listdir(OUT):
-        os.remove(os.path.join(OUT, f))
+        path = os.path.join(OUT, f)
+        if os.path.isdir(path) and not os.path.islink(path):
+            shutil.rmtree(path)
+        else:
+            os.remove(path)
     with open(stamp, "w") as fh:
         fh.write(here + "\n")
 
