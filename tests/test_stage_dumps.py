@@ -183,6 +183,9 @@ def test_dog_dump(case):
     assert rc == 0, out
     assert_bits_equal(load(d / "a.bin", np.float32, (D, H, W)), case["norm"], "normalized (named)")
     assert_bits_equal(load(d / "b.bin", np.float32, (D, H, W)), case["dog"], "dog (named)")
+    rc, out = run("DoG_test", [param, "c.bin"], str(d))
+    assert rc == 0, out
+    assert_bits_equal(load(d / "c.bin", np.float32, (D, H, W)), case["dog"], "dog (one name)")
 
 
 @pytest.mark.gpu
@@ -207,6 +210,11 @@ def test_hessian_dump_verbose(case):
     assert_bits_equal(load(d / "g.bin", np.float32, (D, H, W)), case["dog"], "dog")
     assert_bits_equal(load(d / "m.bin", np.uint8, (D, H, W)), case["mask"], "hessian_pd")
     assert_bits_equal(load(d / "hessian.bin", np.float32, (6, D, H, W)), case["hess"], "hessian planes")
+    # three names, as script/HDoG_intermediate.py passes them: dog, pd, the six planes
+    rc, out = run("Hessian_test", [param, "g3.bin", "m3.bin", "h3.bin"], str(d))
+    assert rc == 0, out
+    assert_bits_equal(load(d / "m3.bin", np.uint8, (D, H, W)), case["mask"], "hessian_pd (3 names)")
+    assert_bits_equal(load(d / "h3.bin", np.float32, (6, D, H, W)), case["hess"], "hessian planes (3 names)")
 
 
 @pytest.mark.gpu
