@@ -161,6 +161,31 @@ static int validate(const hdog_params *p) {
 }
 
 // ------------------------------------------------------------------ context
+// Host copy of a call's records in page-locked memory, so that the device-to-host copies
+// run at the link's speed; grows by doubling and keeps its size between calls.
+struct RecordBuf {
+  hdog_record *p = nullptr;
+  size_t n = 0, cap = 0;
+  bool reserve(size_t want) {
+    if (want <= cap) return true;
+    size_t nc = cap ? cap : (size_t)1 << 16;
+    while (nc < want) nc *= 2;
+    hdog_record *q = nullptr;
+    if (cudaMallocHost(&q, nc * sizeof(hdog_record)) != cudaSuccess) return false;
+    if (n) memcpy(q, p, n * sizeof(hdog_record));
+    if (p) cudaFreeHost(p);
+    p = q;
+    cap = nc;
+    return true;
+  }
+  void clear() { n = 0; }
+  void release() {
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    n = cap = 0;
+  }
+};
+
 struct hdog_ctx {
   hdog_params p;
   int dev = 0;
@@ -175,7 +200,7 @@ struct hdog_ctx {
   int num_sms = 152;
   int max_smem = 48 * 1024;
   bool use_sweep = true;   // fused DoG + Hessian sweep when the parameters allow it
-  std::vector<hdog_record> last;   // records of the last whole-chain call (hdog_last_records)
+  RecordBuf last;   // records of the last whole-chain call (hdog_last_records)
   int margin = 0;
   DogTaps taps;
   std::mutex mu;
@@ -301,6 +326,7 @@ extern "C" int hdog_ctx_destroy(hdog_ctx *ctx) {
   if (ctx->arena) cudaFree(ctx->arena);
   if (ctx->stack_buf) cudaFree(ctx->stack_buf);
   if (ctx->h_subs) cudaFreeHost(ctx->h_subs);
+  ctx->last.release();
   delete ctx->timer;
   delete ctx;
   return HDOG_OK;
@@ -546,25 +572,26 @@ static int run_batch(hdog_ctx *c, int nsub, cudaStream_t st) {
 }
 
 // Appends the records of substacks [0, nsub) to out, in substack order.
-static int collect_records(hdog_ctx *c, int nsub, std::vector<hdog_record> &out, cudaStream_t st) {
-  size_t n = out.size(), total = n;
+static int collect_records(hdog_ctx *c, int nsub, RecordBuf &out, cudaStream_t st) {
+  size_t n = out.n, total = n;
   for (int s = 0; s < nsub; s++) total += (size_t)c->h_counts[s];
-  out.resize(total);
+  if (!out.reserve(total)) return fail(HDOG_ERR_NOMEM, "page-locked host buffer for the records failed");
   for (int s = 0; s < nsub; s++) {
     const int64_t k = c->h_counts[s];
     if (k > 0)
-      HDOG_CUDA_TRY(cudaMemcpyAsync(out.data() + n, c->records + (int64_t)s * c->reg_cap, k * sizeof(hdog_record),
+      HDOG_CUDA_TRY(cudaMemcpyAsync(out.p + n, c->records + (int64_t)s * c->reg_cap, k * sizeof(hdog_record),
                                     cudaMemcpyDeviceToHost, st));
     n += (size_t)k;
   }
   HDOG_CUDA_TRY(cudaStreamSynchronize(st));
+  out.n = total;
   return HDOG_OK;
 }
 
-static int copy_out(const std::vector<hdog_record> &v, hdog_record *out, int64_t cap, int64_t *n) {
-  *n = (int64_t)v.size();
+static int copy_out(const RecordBuf &v, hdog_record *out, int64_t cap, int64_t *n) {
+  *n = (int64_t)v.n;
   if (*n > cap) return fail(HDOG_ERR_CAPACITY, "record buffer too small: " + std::to_string(*n) + " records");
-  if (*n > 0) memcpy(out, v.data(), v.size() * sizeof(hdog_record));
+  if (*n > 0) memcpy(out, v.p, v.n * sizeof(hdog_record));
   return HDOG_OK;
 }
 
@@ -714,8 +741,8 @@ static int schedule(int length, int D, int m, std::vector<int> &z0s) {
   return HDOG_OK;
 }
 
-static int run_stack_locked(hdog_ctx *c, const uint16_t *stack, int on_device, int length,
-                            std::vector<hdog_record> &out, cudaStream_t st) {
+static int run_stack_locked(hdog_ctx *c, const uint16_t *stack, int on_device, int length, RecordBuf &out,
+                            cudaStream_t st) {
   std::vector<int> z0s;
   TRY(schedule(length, c->D, c->margin, z0s));
   if (z0s.empty()) return HDOG_OK;
@@ -888,7 +915,7 @@ extern "C" int hdog_run_param_file(const char *param_path, int verbose) {
   const size_t plane = (size_t)p.width * p.height;
   uint16_t *h_stack = nullptr;
   size_t h_cap = 0;
-  std::vector<hdog_record> recs;
+  RecordBuf &recs = ctx->last;
   int rc = HDOG_OK;
   for (size_t i = 0; i < stacks.size() && rc == HDOG_OK; i++) {
     const StackSpec &sp = stacks[i];
@@ -916,10 +943,10 @@ extern "C" int hdog_run_param_file(const char *param_path, int verbose) {
       rc = run_stack_locked(ctx, h_stack, 0, last, recs, nullptr);
     }
     if (rc != HDOG_OK) break;
-    const int64_t n = (int64_t)recs.size();
+    const int64_t n = (int64_t)recs.n;
     FILE *f = fopen(sp.dst.c_str(), "ab");
     if (!f) { rc = fail(HDOG_ERR_IO, "Unable to open " + sp.dst); break; }
-    if (n > 0 && fwrite(recs.data(), sizeof(hdog_record), (size_t)n, f) != (size_t)n) {
+    if (n > 0 && fwrite(recs.p, sizeof(hdog_record), (size_t)n, f) != (size_t)n) {
       fclose(f);
       rc = fail(HDOG_ERR_IO, "Unable to write " + sp.dst);
       break;

@@ -240,6 +240,177 @@ __global__ void __launch_bounds__(256) k_mm_x(const Sub *subs, int r, int ry, in
   }
 }
 
+// ---------------------------------------------------------------- streaming y / x passes
+// Radius-specialised min/max passes (L = 2R+1 known at compile time).  Each thread walks
+// one line in blocks of L inputs and keeps, in registers, the suffix minima of the
+// previous block and the running prefix minimum of the current one (van Herk /
+// Gil-Werman): the window [t-R, t+R] starting at index i of block b is
+// min(suffix_b[i], prefix_{b+1}[i-1]).  The loops over a block are unrolled, so every
+// register index is a constant.  Nearest border (BORDER 0) clamps the line index; the
+// zero border (BORDER 1) reads the packed zero outside the line.
+
+// y pass: one thread per (column, segment of rows) of a slice; a warp reads 32
+// consecutive columns of a row per load.
+template <int R, int BORDER>
+__global__ void __launch_bounds__(128) k_mm_y_stream(const Sub *subs, int seg, const uint32_t *in, uint32_t *out) {
+  constexpr int L = 2 * R + 1;
+  const Sub S = subs[blockIdx.z];
+  const int W = S.W, H = S.H;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nseg = (H + seg - 1) / seg;
+  const int z = blockIdx.y / nseg, ys = (blockIdx.y % nseg) * seg;
+  if (x >= W || z >= S.D) return;
+  const int ye = min(ys + seg, H);
+  const int64_t plane = (int64_t)W * H;
+  const uint32_t *col = in + S.vox + z * plane + x;
+  uint32_t *oc = out + S.vox + z * plane + x;
+  auto ld = [&](int y) -> uint32_t {
+    if (BORDER == 1 && (y < 0 || y >= H)) return kZeroPacked;
+    return __ldg(col + (int64_t)clampi(y, 0, H - 1) * W);
+  };
+  uint32_t suf[L], cur[L];
+#pragma unroll
+  for (int j = 0; j < L; j++) suf[j] = ld(ys - R + j);
+#pragma unroll
+  for (int j = L - 2; j >= 0; j--) suf[j] = __vminu2(suf[j], suf[j + 1]);
+  for (int t0 = ys; t0 < ye; t0 += L) {
+#pragma unroll
+    for (int j = 0; j < L; j++) cur[j] = ld(t0 - R + L + j);
+    uint32_t pre = 0xFFFFFFFFu;
+#pragma unroll
+    for (int i = 0; i < L; i++) {
+      const uint32_t m = i == 0 ? suf[0] : __vminu2(suf[i], pre);
+      if (t0 + i < ye) oc[(int64_t)(t0 + i) * W] = m;
+      pre = __vminu2(pre, cur[i]);
+    }
+    suf[L - 1] = cur[L - 1];
+#pragma unroll
+    for (int j = L - 2; j >= 0; j--) suf[j] = __vminu2(cur[j], suf[j + 1]);
+  }
+}
+
+// x pass (nearest border) with the exact x box sum -> float2 (ero_x, dil_x): one warp per
+// 32 rows, one row per lane.  Each block of L inputs of the warp's rows is staged in
+// shared memory by cp.async, one block ahead of the one in use (two buffers), then read
+// one row per lane (L is odd, so the lanes' rows fall in distinct banks).  The box sum
+// over the window minima M slides one position per step as an exact integer sum; the box
+// output of u is formed when M(u + R) is, with M(0) standing for positions left of the
+// row and M(W-1) right of it.  Outputs return through a shared tile for row-wise
+// coalesced stores.
+constexpr int kXsWarps = 2;
+
+__device__ __forceinline__ void cp_async4(uint32_t *dst, const uint32_t *src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(static_cast<uint32_t>(__cvta_generic_to_shared(dst))),
+               "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+template <int R>
+__global__ void __launch_bounds__(32 * kXsWarps) k_mm_x_stream(const Sub *subs, const uint32_t *in, float2 *out) {
+  constexpr int L = 2 * R + 1;
+  static_assert(L <= 255, "the integer box sum needs 2R+1 <= 256");
+  __shared__ uint32_t sin_[kXsWarps][2][32 * L];
+  __shared__ float2 sout[kXsWarps][32 * L];
+  const Sub S = subs[blockIdx.y];
+  const int W = S.W;
+  const int64_t rows = (int64_t)S.H * S.D;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t row0 = ((int64_t)blockIdx.x * kXsWarps + w) * 32;
+  if (row0 >= rows) return;
+  const int nr = (int)min((int64_t)32, rows - row0);
+  float2 *tout = sout[w];
+  const uint32_t *lines = in + S.vox + row0 * W;
+  float2 *olines = out + S.vox + row0 * W;
+
+  // inputs [p, p + L) of the warp's rows (clamped to the row) -> buffer, asynchronously
+  auto issue = [&](int p, uint32_t *buf) {
+#pragma unroll 4
+    for (int k = 0; k < 32; k++) {
+      const uint32_t *line = lines + (int64_t)min(k, nr - 1) * W;
+#pragma unroll
+      for (int i = lane; i < L; i += 32) cp_async4(buf + k * L + i, line + clampi(p + i, 0, W - 1));
+    }
+    cp_async_commit();
+  };
+
+  const float inv = 1.0f / (float)L;
+  const uint32_t full = (uint32_t)L * 0xFFFFu;
+  uint32_t suf[L], cur[L], mp[L];
+  issue(-R, sin_[w][0]);
+  issue(-R + L, sin_[w][1]);
+  cp_async_wait<1>();
+  __syncwarp();
+#pragma unroll
+  for (int j = 0; j < L; j++) suf[j] = sin_[w][0][lane * L + j];
+#pragma unroll
+  for (int j = L - 2; j >= 0; j--) suf[j] = __vminu2(suf[j], suf[j + 1]);
+  uint32_t slo = 0, shi = 0, m0 = 0, mlast = 0;
+  int b = 0;
+  for (int t0 = 0; t0 < W + R; t0 += L, b ^= 1) {
+    __syncwarp();                                  // every lane is done with buffer b
+    issue(t0 - R + 2 * L, sin_[w][b]);            // block after next
+    cp_async_wait<1>();                            // block after this one has landed
+    __syncwarp();
+    const uint32_t *cb = sin_[w][b ^ 1];
+#pragma unroll
+    for (int j = 0; j < L; j++) cur[j] = cb[lane * L + j];
+    uint32_t pre = 0xFFFFFFFFu;
+    if (t0 >= L && t0 + L < W) {   // interior: every M(t - L) is in mp, no border
+#pragma unroll
+      for (int i = 0; i < L; i++) {
+        const uint32_t m = i == 0 ? suf[0] : __vminu2(suf[i], pre);
+        pre = __vminu2(pre, cur[i]);
+        const uint32_t o = mp[i];
+        slo += (m & 0xFFFFu) - (o & 0xFFFFu);
+        shi += (m >> 16) - (o >> 16);
+        mp[i] = m;
+        tout[lane * L + i] = make_float2((float)slo * inv, (float)(full - shi) * inv);
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < L; i++) {
+        const int t = t0 + i;
+        uint32_t m = i == 0 ? suf[0] : __vminu2(suf[i], pre);
+        pre = __vminu2(pre, cur[i]);
+        if (t == W - 1) mlast = m;
+        if (t >= W) m = mlast;
+        if (t == 0) {
+          m0 = m;
+          slo = (uint32_t)L * (m & 0xFFFFu);
+          shi = (uint32_t)L * (m >> 16);
+        } else {
+          const uint32_t o = t >= L ? mp[i] : m0;
+          slo += (m & 0xFFFFu) - (o & 0xFFFFu);
+          shi += (m >> 16) - (o >> 16);
+        }
+        mp[i] = m;
+        tout[lane * L + i] = make_float2((float)slo * inv, (float)(full - shi) * inv);
+      }
+    }
+    __syncwarp();
+    const int u0 = t0 - R;
+#pragma unroll 4
+    for (int k = 0; k < 32; k++) {
+      if (k >= nr) break;
+#pragma unroll
+      for (int i = lane; i < L; i += 32) {
+        const int u = u0 + i;
+        if (u >= 0 && u < W) olines[(int64_t)k * W + u] = tout[k * L + i];
+      }
+    }
+    __syncwarp();                                  // the tile is rewritten next block
+    suf[L - 1] = cur[L - 1];
+#pragma unroll
+    for (int j = L - 2; j >= 0; j--) suf[j] = __vminu2(cur[j], suf[j + 1]);
+  }
+  cp_async_wait<0>();                              // no copy outlives the block
+}
+
 // ---------------------------------------------------------------- x pass (box, float chain)
 // The literal float chain of the x box for windows wider than 256 (where the partial
 // sums stop being exact integers), over a packed min/max volume.
@@ -364,8 +535,8 @@ __global__ void __launch_bounds__(128) k_box_z_norm(const Sub *subs, int rz, flo
 // The same pass specialised on the z radius: one thread per (column, chunk of kBoxZK
 // slices), every window input loaded before the first add so that all loads of a thread
 // are in flight together; threadIdx.y picks the chunk, so the chunks of one column share
-// their overlapping inputs through L1.
-template <int RZ>
+// their overlapping inputs through L1.  PARTS also stores the box means (stage dumps).
+template <int RZ, bool PARTS>
 __global__ void __launch_bounds__(128) k_box_z_norm_t(const Sub *subs, float min_intensity, const float2 *in,
                                                       float *norm, float *ero_l, float *dil_l) {
   constexpr int L = 2 * RZ + 1, NW = kBoxZK + 2 * RZ;
@@ -395,7 +566,7 @@ __global__ void __launch_bounds__(128) k_box_z_norm_t(const Sub *subs, float min
     if (z < D) {
       const float2 el = mul2(acc, make_float2(inv, inv));
       norm[S.vox + z * plane + p] = (v[k] >= min_intensity) ? (v[k] - el.x) / (el.y - el.x) : 0.0f;
-      if (ero_l) {   // the box means themselves, for stage dumps
+      if (PARTS) {
         ero_l[S.vox + z * plane + p] = el.x;
         dil_l[S.vox + z * plane + p] = el.y;
       }
@@ -455,6 +626,34 @@ static void mm_y(const Sub *d_subs, int nsub, int W, int H, int D, int r, const 
   KLAUNCH("k_mm_y", s, (k_mm_y<BORDER><<<grid, 256, smem, s>>>(d_subs, r, ty, in, out)));
 }
 
+// The streaming passes where the radius has an instantiation (false: use the staged ones).
+template <int BORDER>
+static bool mm_y_stream(const Sub *d_subs, int nsub, int W, int H, int D, int r, const uint32_t *in, uint32_t *out,
+                        cudaStream_t s) {
+  const int L = 2 * r + 1;
+  const int seg = (ceil_div(H, 4) + L - 1) / L * L;   // about four segments a column, whole blocks
+  const dim3 grid(ceil_div(W, 128), ceil_div(H, seg) * D, nsub);
+  switch (r) {
+    case 20:
+      KLAUNCH("k_mm_y", s, (k_mm_y_stream<20, BORDER><<<grid, 128, 0, s>>>(d_subs, seg, in, out)));
+      return true;
+    default:
+      return false;
+  }
+}
+
+static bool mm_x_stream(const Sub *d_subs, int nsub, int64_t rows, int r, const uint32_t *in, float2 *out,
+                        cudaStream_t s) {
+  const dim3 grid(ceil_div(rows, 32 * kXsWarps), nsub);
+  switch (r) {
+    case 20:
+      KLAUNCH("k_mm_x", s, (k_mm_x_stream<20><<<grid, 32 * kXsWarps, 0, s>>>(d_subs, in, out)));
+      return true;
+    default:
+      return false;
+  }
+}
+
 static size_t mm_x_smem(int mode, int r, int ry, int tx) {
   const int hm = mode == 0 ? r : 0;
   const int stride = (tx + 2 * hm + 2 * r) | 1;
@@ -486,8 +685,9 @@ void launch_normalize(const Sub *d_subs, int nsub, int W, int H, int D, int rxy,
   const int plane = W * H;
   const int64_t rows = (int64_t)H * D;
   mm_z<0>(d_subs, nsub, plane, rz, src_aligned8 && plane % 4 == 0, ma, s);
-  mm_y<0>(d_subs, nsub, W, H, D, rxy, ma, mb, s);
-  if (2 * rxy + 1 <= 256) {
+  if (!mm_y_stream<0>(d_subs, nsub, W, H, D, rxy, ma, mb, s)) mm_y<0>(d_subs, nsub, W, H, D, rxy, ma, mb, s);
+  if (mm_x_stream(d_subs, nsub, rows, rxy, mb, fa, s)) {
+  } else if (2 * rxy + 1 <= 256) {
     mm_x<0, 0>(d_subs, nsub, W, rows, rxy, mb, fa, s);
   } else {
     mm_x<0, 2>(d_subs, nsub, W, rows, rxy, mb, ma, s);
@@ -503,7 +703,10 @@ void launch_normalize(const Sub *d_subs, int nsub, int W, int H, int D, int rxy,
   switch (rz) {
 #define HDOG_BOXZ_CASE(R)                                                                                   \
   case R:                                                                                                   \
-    KLAUNCH("k_box_z_norm", s, (k_box_z_norm_t<R><<<gz, bz, 0, s>>>(d_subs, min_intensity, fb, norm, ero_l, dil_l))); \
+    if (ero_l)                                                                                              \
+      KLAUNCH("k_box_z_norm", s, (k_box_z_norm_t<R, true><<<gz, bz, 0, s>>>(d_subs, min_intensity, fb, norm, ero_l, dil_l))); \
+    else                                                                                                    \
+      KLAUNCH("k_box_z_norm", s, (k_box_z_norm_t<R, false><<<gz, bz, 0, s>>>(d_subs, min_intensity, fb, norm, ero_l, dil_l))); \
     break;
     HDOG_BOXZ_CASE(1) HDOG_BOXZ_CASE(2) HDOG_BOXZ_CASE(3) HDOG_BOXZ_CASE(4)
     HDOG_BOXZ_CASE(5) HDOG_BOXZ_CASE(6) HDOG_BOXZ_CASE(7) HDOG_BOXZ_CASE(8)

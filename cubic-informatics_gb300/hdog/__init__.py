@@ -352,10 +352,9 @@ class Context:
     def run_substack(self, img, depth_valid, z0, cap=None, stream=None):
         """img: host numpy uint16 (depth_valid, H, W) or a CUDA tensor; -> dt_local records."""
         on_dev, ptr = _buffer(img)
-        cap = cap if cap is not None else 1 << 20
-        out = np.empty(cap, DT_LOCAL)
+        out = np.empty(cap or 0, DT_LOCAL)
         n = ctypes.c_int64()
-        rc = lib().hdog_run_substack(self._h, ptr, on_dev, int(depth_valid), int(z0), out.ctypes.data, cap,
+        rc = lib().hdog_run_substack(self._h, ptr, on_dev, int(depth_valid), int(z0), _out_ptr(out), len(out),
                                      ctypes.byref(n), _stream(stream) if on_dev else None)
         return self._finish(rc, out, n)
 
@@ -363,21 +362,26 @@ class Context:
         """All substacks of one stack (length, H, W) in the reference's schedule."""
         on_dev, ptr = _buffer(stack)
         length = int(stack.shape[0])
-        cap = cap if cap is not None else 1 << 20
-        out = np.empty(cap, DT_LOCAL)
+        out = np.empty(cap or 0, DT_LOCAL)
         n = ctypes.c_int64()
-        rc = lib().hdog_run_stack(self._h, ptr, on_dev, length, out.ctypes.data, cap, ctypes.byref(n),
+        rc = lib().hdog_run_stack(self._h, ptr, on_dev, length, _out_ptr(out), len(out), ctypes.byref(n),
                                   _stream(stream) if on_dev else None)
         return self._finish(rc, out, n)
 
     def _finish(self, rc, out, n):
-        """Records of a whole-chain call; a buffer that was too small is refilled from the
-        context's copy of the result, without running the chain again."""
+        """Records of a whole-chain call.  Without a capacity the call only counts them, and
+        one copy from the context's host copy of the result fills an array of exactly that
+        size; a buffer that was too small is refilled the same way, without running the chain
+        again."""
         if rc == HDOG_ERR_CAPACITY:
             out = np.empty(int(n.value), DT_LOCAL)
-            rc = lib().hdog_last_records(self._h, out.ctypes.data, len(out), ctypes.byref(n))
+            rc = lib().hdog_last_records(self._h, _out_ptr(out), len(out), ctypes.byref(n))
         check(rc)
-        return out[: n.value].copy()
+        return out if len(out) == n.value else out[: n.value].copy()
+
+
+def _out_ptr(a):
+    return a.ctypes.data if len(a) else None
 
 
 def _buffer(a):

@@ -23,6 +23,10 @@ CASES = {
     "copy_path_r0": (64, 48, 16, dict(radius_norm_xy=0, min_intensity=120)),
     "tiny5x3x2": (5, 3, 2, dict(radius_norm_xy=2, radius_norm_z=1)),
     "wide_x_box_r140": (300, 40, 8, dict(radius_norm_xy=140, radius_norm_z=2)),
+    # the radius-specialised normalize passes (r_xy 20, r_z 5) on ragged tiles and a
+    # substack shallower than the z window
+    "ragged_r20_203x150x19": (203, 150, 19, {}),
+    "shallow_r20_64x40x6": (64, 40, 6, {}),
 }
 
 
