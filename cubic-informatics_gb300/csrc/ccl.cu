@@ -247,6 +247,41 @@ __device__ __forceinline__ void cell_occ8(const Sub &S, const uint8_t *m, int64_
   }
 }
 
+// Drops links that other links of the tile already imply.  Every tile edge is linked by
+// the later of its two cells, so with cell c linked to B (a backward neighbour) and B
+// touching A (another backward neighbour of c), the edge B-A is linked too and c-A adds
+// nothing.  Links kept unconditionally: k = 4 (dz -1), 10 (dy -1), 12 (dx -1).  Pruned:
+//   via k = 4  (the cell below):  the other eight cells of the layer below, through the
+//              in-plane edges of that layer;
+//   via k = 10 (the cell behind): k = 9, 11 through that row's x edges (kept by rule) and
+//              k = 1 through its own link k = 4 (kept);
+//   via k = 12 (the cell left):   k = 9 through its link k = 10 and k = 3 through its
+//              link k = 4 (both kept).
+// Each pruned link rests on links that are kept or pruned only by the rules for
+// in-layer edges, which rest on kept links: the implied connectivity is exact.
+// The component minima are unchanged (they come from the final trees, not the links).
+__device__ __forceinline__ bool touches(uint32_t a, uint32_t b, CellNb e) { return (a & e.self) && (b & e.other); }
+
+__device__ __forceinline__ uint32_t prune_links(uint32_t todo, const uint32_t (&on)[13]) {
+  if (todo & (1u << 4)) {
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+      if (k == 4) continue;
+      if (touches(on[4], on[k], cell_nb(0, k / 3 - 1, k % 3 - 1))) todo &= ~(1u << k);
+    }
+  }
+  if (todo & (1u << 10)) {
+    if (touches(on[10], on[9], cell_nb(0, 0, -1))) todo &= ~(1u << 9);
+    if (touches(on[10], on[11], cell_nb(0, 0, 1))) todo &= ~(1u << 11);
+    if (touches(on[10], on[1], cell_nb(-1, 0, 0))) todo &= ~(1u << 1);
+  }
+  if (todo & (1u << 12)) {
+    if (touches(on[12], on[9], cell_nb(0, -1, 0))) todo &= ~(1u << 9);
+    if (touches(on[12], on[3], cell_nb(-1, 0, 0))) todo &= ~(1u << 3);
+  }
+  return todo;
+}
+
 __global__ void __launch_bounds__(kCclThreads) k_ccl_local(const Sub *subs, const uint8_t *mask, int32_t *labels,
                                                           int2 *edges, unsigned long long *edge_count) {
   __shared__ uint32_t par[kCells];
@@ -332,13 +367,15 @@ __global__ void __launch_bounds__(kCclThreads) k_ccl_local(const Sub *subs, cons
     const uint32_t oc = occ[halo_of(cx, cy, cz)];
     uint32_t todo = 0;
     if (oc) {
+      uint32_t on[13];   // occupancy of the backward neighbours inside the tile (0 outside)
 #pragma unroll
       for (int k = 0; k < 13; k++) {
         const CellNb nb = kCellNb[k];
         const int nx = cx + nb.dx, ny = cy + nb.dy, nz = cz + nb.dz;
-        if (nx < 0 || nx >= kCX || ny < 0 || ny >= kCY || nz < 0) continue;
-        if ((oc & nb.self) && (occ[halo_of(nx, ny, nz)] & nb.other)) todo |= 1u << k;
+        on[k] = (nx < 0 || nx >= kCX || ny < 0 || ny >= kCY || nz < 0) ? 0u : occ[halo_of(nx, ny, nz)];
+        if ((oc & nb.self) && (on[k] & nb.other)) todo |= 1u << k;
       }
+      todo = prune_links(todo, on);
     }
     while (__any_sync(0xFFFFFFFFu, todo != 0)) {
       if (todo) {
