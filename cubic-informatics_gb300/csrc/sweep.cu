@@ -374,9 +374,21 @@ template <int RA, int RB>
 struct TapPairs {
   static constexpr int RS = RA < RB ? RA : RB;
   float2 k[2 * RS + 1];
+  static constexpr int N = 2 * RS + 1;
   __device__ __forceinline__ void load(const DogTaps &T, int ka, int kb) {
 #pragma unroll
     for (int j = -RS; j <= RS; j++) k[j + RS] = make_float2(T.k[ka][RA - j], T.k[kb][RB - j]);
+  }
+  // The pairs as written by stage(): read back from shared memory, they are per-thread
+  // registers, so the f32x2 FMAs use them directly instead of copying each pair out of
+  // the uniform registers a kernel-parameter value would live in.
+  __device__ __forceinline__ static void stage(const DogTaps &T, int ka, int kb, float2 *sh) {
+#pragma unroll
+    for (int j = -RS; j <= RS; j++) sh[j + RS] = make_float2(T.k[ka][RA - j], T.k[kb][RB - j]);
+  }
+  __device__ __forceinline__ void load_shared(const float2 *sh) {
+#pragma unroll
+    for (int i = 0; i < N; i++) k[i] = sh[i];
   }
 };
 
@@ -480,10 +492,13 @@ __global__ void __launch_bounds__(DogT<RA, RB, ZA, ZB>::NT, 1)
   uint64_t *bar = reinterpret_cast<uint64_t *>(smem + (size_t)2 * C::IN_FLOATS * 4 + (size_t)2 * C::BH * kDTX * 8);
   const int t = threadIdx.x;
   const int D = S.D, W = S.W, H = S.H;
+  __shared__ float2 tap_sh[TapPairs<RA, RB>::N + TapPairs<ZA, ZB>::N];
   if (t == 0) {
     mbar_init(&bar[0], 1);
     mbar_init(&bar[1], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    TapPairs<RA, RB>::stage(T, 0, 2, tap_sh);
+    TapPairs<ZA, ZB>::stage(T, 1, 3, tap_sh + TapPairs<RA, RB>::N);
   }
   __syncthreads();
   constexpr uint32_t tma_bytes = (uint32_t)(C::BW * C::BH * 4);
@@ -501,8 +516,8 @@ __global__ void __launch_bounds__(DogT<RA, RB, ZA, ZB>::NT, 1)
   for (int s = 0; s < C::WIN; s++) { acc0[s] = make_float2(0.f, 0.f); acc1[s] = make_float2(0.f, 0.f); }
   TapPairs<RA, RB> kxy;
   TapPairs<ZA, ZB> kz;
-  kxy.load(T, 0, 2);
-  kz.load(T, 1, 3);
+  kxy.load_shared(tap_sh);
+  kz.load_shared(tap_sh + TapPairs<RA, RB>::N);
   const int nit = D + C::RZ + 1;
   // One slice step; PC is the step's position inside a group of WIN steps, so the z phase
   // of slice zy = it - 1 is the compile-time (PC - 1) mod WIN and every shift-register slot

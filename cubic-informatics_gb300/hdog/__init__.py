@@ -349,20 +349,24 @@ class Context:
         return out
 
     # processSubstack + saveFeatureVector
-    def run_substack(self, img, depth_valid, z0, cap=None, stream=None):
-        """img: host numpy uint16 (depth_valid, H, W) or a CUDA tensor; -> dt_local records."""
+    def run_substack(self, img, depth_valid, z0, cap=None, stream=None, out=None):
+        """img: host numpy uint16 (depth_valid, H, W) or a CUDA tensor; -> dt_local records.
+        out: an optional dt_local array to fill (the result is then a view of it, or a
+        new array when it is too small)."""
         on_dev, ptr = _buffer(img)
-        out = np.empty(cap or 0, DT_LOCAL)
+        out = _out_array(out, cap)
         n = ctypes.c_int64()
         rc = lib().hdog_run_substack(self._h, ptr, on_dev, int(depth_valid), int(z0), _out_ptr(out), len(out),
                                      ctypes.byref(n), _stream(stream) if on_dev else None)
         return self._finish(rc, out, n)
 
-    def run_stack(self, stack, cap=None, stream=None):
-        """All substacks of one stack (length, H, W) in the reference's schedule."""
+    def run_stack(self, stack, cap=None, stream=None, out=None):
+        """All substacks of one stack (length, H, W) in the reference's schedule.  out: an
+        optional dt_local array to fill, as for run_substack (reusing one array across calls
+        saves mapping fresh pages for every result)."""
         on_dev, ptr = _buffer(stack)
         length = int(stack.shape[0])
-        out = np.empty(cap or 0, DT_LOCAL)
+        out = _out_array(out, cap)
         n = ctypes.c_int64()
         rc = lib().hdog_run_stack(self._h, ptr, on_dev, length, _out_ptr(out), len(out), ctypes.byref(n),
                                   _stream(stream) if on_dev else None)
@@ -377,11 +381,18 @@ class Context:
             out = np.empty(int(n.value), DT_LOCAL)
             rc = lib().hdog_last_records(self._h, _out_ptr(out), len(out), ctypes.byref(n))
         check(rc)
-        return out if len(out) == n.value else out[: n.value].copy()
+        return out[: n.value]
 
 
 def _out_ptr(a):
     return a.ctypes.data if len(a) else None
+
+
+def _out_array(out, cap):
+    if out is None:
+        return np.empty(cap or 0, DT_LOCAL)
+    assert out.dtype == DT_LOCAL and out.ndim == 1 and out.flags["C_CONTIGUOUS"]
+    return out
 
 
 def _buffer(a):
