@@ -132,6 +132,44 @@ struct DogTaps {
   float normalizer;
 };
 
+// ---- mbarrier / TMA helpers (sm_90+ PTX).  Every wait is bounded: after kWaitLimit
+// polls it gives up and the caller records HDOG_ERR_TIMEOUT.
+constexpr long long kWaitLimit = 1ll << 26;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+  uint32_t done = 0;
+  for (long long it = 0; it < kWaitLimit && !done; it++) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+  }
+  return done != 0;
+}
+
+// One box of a 4-D tensor map (x, y, z, substack) into shared memory, completing on bar.
+__device__ __forceinline__ void tma_load_4d(const void *map, void *dst, uint64_t *bar, int x, int y, int z, int s,
+                                            uint32_t bytes) {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+      "[%6];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(s), "r"(smem_u32(bar))
+      : "memory");
+}
+
 // Optional per-kernel timing: when a context enables it, each kernel launch is
 // bracketed by CUDA events recorded on the launching stream.
 struct KernelTimer {

@@ -32,7 +32,6 @@ constexpr int kSX = 64, kSY = 16;                 // mask tile
 constexpr int kEX = kSX + 4, kEY = kSY + 4;       // DoG tile with the Hessian halo
 constexpr int kSweepThreads = 704;                // 22 warps
 constexpr int kXQuads = kEX / 4;                  // 17 four-wide x-pass items per row
-constexpr long long kWaitLimit = 1ll << 26;       // bounded mbarrier spin
 
 __host__ __device__ inline int sweep_hx(int rxy) { return ((rxy + 2 + 3) / 4) * 4; }   // aligned x halo
 __host__ __device__ inline int sweep_bw(int rxy) { return kSX + 2 * sweep_hx(rxy); }
@@ -45,38 +44,10 @@ size_t sweep_smem_bytes(int rxy) {
   return 2 * in + xb + ring + 64;
 }
 
-__device__ __forceinline__ uint32_t smem_u32(const void *p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
-}
-
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
-  uint32_t done = 0;
-  for (long long it = 0; it < kWaitLimit && !done; it++) {
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(done)
-        : "r"(smem_u32(bar)), "r"(parity)
-        : "memory");
-  }
-  return done != 0;
-}
-
 // One normalized slice (box bw x bh at (x, y, z, s)) into shared memory.
 __device__ __forceinline__ void tma_slice(const CUtensorMap *map, float *dst, uint64_t *bar, int x, int y, int z, int s,
                                           uint32_t bytes) {
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
-  asm volatile(
-      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
-      "[%6];" ::"r"(smem_u32(dst)),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(s), "r"(smem_u32(bar))
-      : "memory");
+  tma_load_4d(map, dst, bar, x, y, z, s, bytes);
 }
 
 template <int RZ>
