@@ -782,6 +782,35 @@ extern "C" int hdog_run_stack(hdog_ctx *c, const uint16_t *stack, int stack_on_d
   return copy_out(c->last, out, cap, n_records);
 }
 
+// ------------------------------------------------------------------ after the records
+extern "C" int hdog_records_to_global(const hdog_record *d_records, int64_t n, const hdog_global_params *p,
+                                      hdog_global *d_out, void *stream) {
+  if (!p || n < 0 || (n > 0 && (!d_records || !d_out))) return fail(HDOG_ERR_ARG, "hdog_records_to_global: bad argument");
+  if (p->promote != HDOG_PROMOTE_F32 && p->promote != HDOG_PROMOTE_F64)
+    return fail(HDOG_ERR_ARG, "hdog_records_to_global: promote must be HDOG_PROMOTE_F32 or HDOG_PROMOTE_F64");
+  launch_to_global(d_records, n, *p, d_out, (cudaStream_t)stream);
+  HDOG_CUDA_TRY(cudaGetLastError());
+  return HDOG_OK;
+}
+
+extern "C" int hdog_scale_merge(const hdog_global *d_in, int64_t n, const hdog_scalemerge_params *p,
+                                hdog_scalemerged *d_out, void *stream) {
+  if (!p || n < 0 || (n > 0 && (!d_in || !d_out))) return fail(HDOG_ERR_ARG, "hdog_scale_merge: bad argument");
+  if (p->promote != HDOG_PROMOTE_F32 && p->promote != HDOG_PROMOTE_F64)
+    return fail(HDOG_ERR_ARG, "hdog_scale_merge: promote must be HDOG_PROMOTE_F32 or HDOG_PROMOTE_F64");
+  launch_scale_merge(d_in, n, *p, d_out, (cudaStream_t)stream);
+  HDOG_CUDA_TRY(cudaGetLastError());
+  return HDOG_OK;
+}
+
+extern "C" int hdog_classifier_features(const hdog_record *d_records, int64_t n, const hdog_clf_params *p, double *d_X,
+                                        void *stream) {
+  if (!p || n < 0 || (n > 0 && (!d_records || !d_X))) return fail(HDOG_ERR_ARG, "hdog_classifier_features: bad argument");
+  launch_clf_features(d_records, n, *p, d_X, (cudaStream_t)stream);
+  HDOG_CUDA_TRY(cudaGetLastError());
+  return HDOG_OK;
+}
+
 extern "C" int hdog_last_records(hdog_ctx *c, hdog_record *out, int64_t cap, int64_t *n_records) {
   if (!c || !n_records || (cap > 0 && !out)) return fail(HDOG_ERR_ARG, "hdog_last_records: bad argument");
   std::lock_guard<std::mutex> lock(c->mu);

@@ -81,6 +81,13 @@ size_t sweep_smem_bytes(int rxy);
 bool sweep_supported(const DogTaps &T, int W, int max_smem);
 // DoG volume by the radius-specialised z-sweep; false (nothing launched) when the radii
 // have no instantiation or the buffers do not suit TMA.
+// records.cu: per-record steps after the records (host-side NumPy in the reference)
+void launch_to_global(const hdog_record *rec, int64_t n, const hdog_global_params &p, hdog_global *out,
+                      cudaStream_t s);
+void launch_scale_merge(const hdog_global *in, int64_t n, const hdog_scalemerge_params &p, hdog_scalemerged *out,
+                        cudaStream_t s);
+void launch_clf_features(const hdog_record *rec, int64_t n, const hdog_clf_params &p, double *X, cudaStream_t s);
+
 bool launch_dog_sweep(const Sub *d_subs, int nsub, int W, int H, int D, const DogTaps &T, const float *norm,
                       float *dog, int *d_status, int max_smem, cudaStream_t s);
 // DoG + Hessian + PD: the radius-specialised pair (norm -> dog -> mask + list) when the tap

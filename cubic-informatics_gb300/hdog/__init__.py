@@ -69,6 +69,34 @@ class hdog_regions(ctypes.Structure):
 
 
 _P = ctypes.c_void_p
+HDOG_PROMOTE_F32, HDOG_PROMOTE_F64 = 0, 1
+
+# dt_global (script/HalfBrainCells.py:16-20) and dt_scalemerged (script/MergeBrain.py:32-35)
+DT_GLOBAL = np.dtype([("merged_x", "f4"), ("merged_y", "f4"), ("merged_z", "f4"),
+                      ("i_x", "u1"), ("i_y", "u1"), ("FWRV", "u1")])
+DT_SCALEMERGED = np.dtype([("scaled_x", "f4"), ("scaled_y", "f4"), ("scaled_z", "f4"), ("is_valid", "bool")])
+
+
+class hdog_global_params(ctypes.Structure):
+    _fields_ = [("offset_x", ctypes.c_double), ("offset_y", ctypes.c_double), ("offset_z", ctypes.c_double),
+                ("scale_x", ctypes.c_double), ("scale_y", ctypes.c_double), ("scale_z", ctypes.c_double),
+                ("width", ctypes.c_int), ("height", ctypes.c_int), ("is_fw", ctypes.c_int),
+                ("i_x", ctypes.c_int), ("i_y", ctypes.c_int), ("promote", ctypes.c_int)]
+
+
+class hdog_scalemerge_params(ctypes.Structure):
+    _fields_ = [("bound_z0", ctypes.c_double), ("bound_z1", ctypes.c_double),
+                ("offset_x", ctypes.c_double), ("offset_y", ctypes.c_double), ("offset_z", ctypes.c_double),
+                ("coeff_x", ctypes.c_double), ("coeff_y", ctypes.c_double), ("coeff_z", ctypes.c_double),
+                ("margin_left", ctypes.c_double), ("margin_top", ctypes.c_double),
+                ("A", ctypes.c_double * 9), ("b", ctypes.c_double * 3), ("promote", ctypes.c_int)]
+
+
+class hdog_clf_params(ctypes.Structure):
+    _fields_ = [("bias", ctypes.c_double * 3), ("scale", ctypes.c_double * 3),
+                ("bias_before_log", ctypes.c_double * 3), ("is_ave", ctypes.c_int)]
+
+
 _SIGNATURES = {
     "hdog_last_error": (ctypes.c_char_p, []),
     "hdog_abi_version": (ctypes.c_int, []),
@@ -95,6 +123,9 @@ _SIGNATURES = {
     "hdog_ccl_noalloc": (ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P]),
     "hdog_timing_enable": (ctypes.c_int, [_P, ctypes.c_int]),
     "hdog_timing_read": (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_size_t]),
+    "hdog_records_to_global": (ctypes.c_int, [_P, ctypes.c_int64, ctypes.POINTER(hdog_global_params), _P, _P]),
+    "hdog_scale_merge": (ctypes.c_int, [_P, ctypes.c_int64, ctypes.POINTER(hdog_scalemerge_params), _P, _P]),
+    "hdog_classifier_features": (ctypes.c_int, [_P, ctypes.c_int64, ctypes.POINTER(hdog_clf_params), _P, _P]),
     "hdog_memcpy": (ctypes.c_int, [_P, _P, ctypes.c_size_t, _P]),
     "hdog_stream_sync": (ctypes.c_int, [_P]),
     "hdog_device_alloc": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.c_size_t]),
@@ -404,3 +435,4 @@ def _buffer(a):
 
 
 from . import synth  # noqa: E402,F401
+from .postprocess import records_to_global, scale_merge, classifier_features  # noqa: E402,F401

@@ -28,6 +28,9 @@
  *                                                            src/3D/HDoG3D_main.cpp:134-257,
  *                                                            src/3D/utils.h:204-250
  *   hdog_run_stack          the substack loop of main        src/3D/HDoG3D_main.cpp:294-315
+ *   hdog_records_to_global  HDoGResultStack                  script/HalfBrainCells.py:44-56
+ *   hdog_scale_merge        process_stack (scale merge)      script/MergeBrain.py:546-570
+ *   hdog_classifier_features get_X_3d                        script/HDoG_classifier.py:158-176
  */
 #ifndef HDOG_H
 #define HDOG_H
@@ -38,7 +41,7 @@
 extern "C" {
 #endif
 
-#define HDOG_ABI_VERSION 2
+#define HDOG_ABI_VERSION 3
 
 enum {
   HDOG_OK = 0,
@@ -165,6 +168,75 @@ int hdog_run_param_file(const char *param_path, int verbose);
    that device current.  Synchronizes `stream` before returning. */
 int hdog_ccl_noalloc(const uint8_t *d_mask, int32_t *d_labels, int width, int height, int depth,
                      void *stream);
+
+/* ---- after the records: global coordinates, scale-merge validity, classifier features ----
+   Per-record passes over record arrays in device memory (n may be 0), on `stream`
+   (no synchronization).  The reference does these steps in NumPy on the host.
+
+   Where a float64 scalar (a stack offset, a z bound) meets the float32 record fields the
+   reference leaves the rounding to NumPy's promotion rules, which changed in NumPy 2: */
+enum {
+  HDOG_PROMOTE_F32 = 0,   /* NumPy 1.x value-based casting: the scalar is rounded to float32
+                             and the arithmetic or comparison runs in float32 */
+  HDOG_PROMOTE_F64 = 1    /* NumPy >= 2: float64 arithmetic or comparison, rounded to
+                             float32 when stored into a float32 field */
+};
+
+/* dt_global of script/HalfBrainCells.py:16-20 and dt_scalemerged of script/MergeBrain.py:32-35,
+   both packed (15 and 13 bytes), as NumPy lays them out. */
+#pragma pack(push, 1)
+typedef struct hdog_global {
+  float merged_x, merged_y, merged_z;
+  uint8_t i_x, i_y;
+  uint8_t fwrv;                          /* 0 FW, 1 RV */
+} hdog_global;
+typedef struct hdog_scalemerged {
+  float scaled_x, scaled_y, scaled_z;
+  uint8_t is_valid;
+} hdog_scalemerged;
+#pragma pack(pop)
+
+/* HDoGResultStack (script/HalfBrainCells.py:44-56): merged = offset + local * scale per axis
+   (the scale a Python float, so the product is float32), and for a negative x (y) scale
+   merged -= width * scale (height * scale).  i_x, i_y, fwrv are copied to every record. */
+typedef struct hdog_global_params {
+  double offset_x, offset_y, offset_z;   /* imagestack.offset_{x,y,z} (NumPy float64 scalars) */
+  double scale_x, scale_y, scale_z;      /* coordinate_info.scale_{x,y,z} */
+  int width, height;                     /* the stack's image size */
+  int is_fw;                             /* 1: FW (fwrv 0), 0: RV (fwrv 1) */
+  int i_x, i_y;                          /* stack grid position (stored as uint8) */
+  int promote;                           /* HDOG_PROMOTE_* for offset + product */
+} hdog_global_params;
+int hdog_records_to_global(const hdog_record *d_records, int64_t n, const hdog_global_params *p,
+                           hdog_global *d_out, void *stream);
+
+/* process_stack of the scale-merge step (script/MergeBrain.py:546-570): is_valid = z inside
+   bound_z (either order, infinities allowed); scaled = A . ((merged - offset) * coeff -
+   margin) + b, the inner expression stored as float32 and the affine step in float64. */
+typedef struct hdog_scalemerge_params {
+  double bound_z0, bound_z1;             /* bound_z (NumPy float64 scalars or +-inf) */
+  double offset_x, offset_y, offset_z;   /* NumPy float64 scalars */
+  double coeff_x, coeff_y, coeff_z;      /* downscale ratio / original scale (Python floats) */
+  double margin_left, margin_top;        /* merged margins (Python ints) */
+  double A[9];                           /* flip / axis permutation, row-major, entries 0 or +-1 */
+  double b[3];
+  int promote;                           /* HDOG_PROMOTE_* for merged - offset and the z test */
+} hdog_scalemerge_params;
+int hdog_scale_merge(const hdog_global *d_in, int64_t n, const hdog_scalemerge_params *p,
+                     hdog_scalemerged *d_out, void *stream);
+
+/* get_X_3d (script/HDoG_classifier.py:158-176): X = nan_to_num((log10(F + bias_before_log) +
+   bias) * scale) in float64, F = (intensity, structureness, blobness) of each record
+   (intensity / size when is_ave).  X is n x 3, row-major.  log10 is CUDA's (at most 1 ulp
+   from the correctly rounded value, as the host libm's is within its own bound). */
+typedef struct hdog_clf_params {
+  double bias[3];                        /* default 0 */
+  double scale[3];                       /* default 1 */
+  double bias_before_log[3];             /* default 0 */
+  int is_ave;
+} hdog_clf_params;
+int hdog_classifier_features(const hdog_record *d_records, int64_t n, const hdog_clf_params *p, double *d_X,
+                             void *stream);
 
 /* ---- context options ---- */
 enum {

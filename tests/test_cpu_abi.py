@@ -32,7 +32,12 @@ def test_library_exports_every_declared_symbol():
 def test_struct_layouts():
     assert hdog.DT_LOCAL.itemsize == 28          # FeatureVector, src/3D/utils.h:188-197
     assert ctypes.sizeof(hdog.hdog_params) == 21 * 4
-    assert hdog.lib().hdog_abi_version() == 2
+    assert hdog.lib().hdog_abi_version() == 3
+    # the record post-processing types: packed NumPy records, plain parameter blocks
+    assert hdog.DT_GLOBAL.itemsize == 15 and hdog.DT_SCALEMERGED.itemsize == 13
+    assert ctypes.sizeof(hdog.hdog_global_params) == 6 * 8 + 6 * 4
+    assert ctypes.sizeof(hdog.hdog_scalemerge_params) == 22 * 8 + 8
+    assert ctypes.sizeof(hdog.hdog_clf_params) == 9 * 8 + 8
 
 
 @pytest.mark.parametrize("sigma", [0.0, 0.4, 1.5, 1.8, 2.0, 2.4, 2.7, 3.2, 4.0, 6.0, 12.3])
