@@ -230,9 +230,14 @@ struct hdog_ctx {
   Sub *h_subs = nullptr;
   int64_t *h_seg = nullptr;
   int64_t *h_counts = nullptr;   // [3*max_sub + 2]: records, regions, foreground counts per substack; status
-  // device copy of a whole stack for hdog_run_stack with host input
+  // device copy of a whole stack for hdog_run_stack with host input, copied in chunks on
+  // copy_st (one event per batch) so that later chunks land while earlier batches run
   uint16_t *stack_buf = nullptr;
   size_t stack_bytes = 0;
+  cudaStream_t copy_st = nullptr;
+  std::vector<cudaEvent_t> chunk_ev;
+  cudaEvent_t start_ev = nullptr;
+  int host_batch = 1;   // substacks in the first batch of a host-input stack (0: max_sub)
   EventTimer *timer = nullptr;
 };
 
@@ -325,6 +330,9 @@ extern "C" int hdog_ctx_destroy(hdog_ctx *ctx) {
   cudaSetDevice(ctx->dev);
   if (ctx->arena) cudaFree(ctx->arena);
   if (ctx->stack_buf) cudaFree(ctx->stack_buf);
+  for (cudaEvent_t e : ctx->chunk_ev) cudaEventDestroy(e);
+  if (ctx->start_ev) cudaEventDestroy(ctx->start_ev);
+  if (ctx->copy_st) cudaStreamDestroy(ctx->copy_st);
   if (ctx->h_subs) cudaFreeHost(ctx->h_subs);
   ctx->last.release();
   delete ctx->timer;
@@ -451,8 +459,31 @@ static bool srcs_aligned8(const hdog_ctx *c, int nsub) {
   return true;
 }
 
+// Descriptors of up to kParamSubs substacks travel as a kernel parameter and a one-block
+// kernel stores them: no host-to-device copy on the compute stream, where it would queue on
+// the copy engine behind a stack chunk that hdog_run_stack is copying on its copy stream.
+constexpr int kParamSubs = 16;
+struct SubsParam {
+  Sub subs[kParamSubs];
+  int64_t seg[6 * kParamSubs];
+};
+
+__global__ void k_store_subs(const __grid_constant__ SubsParam P, int nsub, int ms, Sub *subs, int64_t *seg) {
+  const int t = threadIdx.x;
+  if (t < nsub) subs[t] = P.subs[t];
+  if (t < 6 * ms) seg[t] = P.seg[t];
+}
+
 static int upload_subs(hdog_ctx *c, int nsub, cudaStream_t st) {
   const int ms = c->max_sub;
+  if (ms <= kParamSubs) {
+    SubsParam P;
+    memcpy(P.subs, c->h_subs, nsub * sizeof(Sub));
+    memcpy(P.seg, c->h_seg, 6 * ms * sizeof(int64_t));
+    KLAUNCH("k_store_subs", st, (k_store_subs<<<1, 6 * kParamSubs, 0, st>>>(P, nsub, ms, c->d_subs, c->d_seg)));
+    HDOG_CUDA_TRY(cudaGetLastError());
+    return HDOG_OK;
+  }
   HDOG_CUDA_TRY(cudaMemcpyAsync(c->d_subs, c->h_subs, nsub * sizeof(Sub), cudaMemcpyHostToDevice, st));
   HDOG_CUDA_TRY(cudaMemcpyAsync(c->d_seg, c->h_seg, 6 * ms * sizeof(int64_t), cudaMemcpyHostToDevice, st));
   return HDOG_OK;
@@ -748,6 +779,18 @@ static int run_stack_locked(hdog_ctx *c, const uint16_t *stack, int on_device, i
   if (z0s.empty()) return HDOG_OK;
   const size_t plane = (size_t)c->W * c->H;
   const uint16_t *dev = stack;
+  // batches of as many substacks as the context holds; with host input the first batch
+  // holds host_batch substacks, so that only its slices are copied before work starts and
+  // the copy of the rest overlaps it
+  std::vector<size_t> starts;   // first substack of each batch, then the end
+  {
+    const size_t full = (size_t)c->max_sub;
+    size_t first = full;
+    if (!on_device && c->host_batch > 0) first = std::min(full, (size_t)c->host_batch);
+    for (size_t b0 = 0; b0 < z0s.size(); b0 += (b0 == 0 ? first : full)) starts.push_back(b0);
+    starts.push_back(z0s.size());
+  }
+  const size_t nbatch = starts.size() - 1;
   if (!on_device) {
     const size_t bytes = (size_t)length * plane * sizeof(uint16_t);
     if (bytes > c->stack_bytes) {
@@ -758,13 +801,38 @@ static int run_stack_locked(hdog_ctx *c, const uint16_t *stack, int on_device, i
         return fail(HDOG_ERR_NOMEM, "hdog_run_stack: no device memory for the stack");
       c->stack_bytes = bytes;
     }
-    HDOG_CUDA_TRY(cudaMemcpyAsync(c->stack_buf, stack, bytes, cudaMemcpyHostToDevice, st));
+    if (!c->copy_st) {
+      HDOG_CUDA_TRY(cudaStreamCreateWithFlags(&c->copy_st, cudaStreamNonBlocking));
+      HDOG_CUDA_TRY(cudaEventCreateWithFlags(&c->start_ev, cudaEventDisableTiming));
+    }
+    while (c->chunk_ev.size() < nbatch) {
+      cudaEvent_t e;
+      HDOG_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+      c->chunk_ev.push_back(e);
+    }
+    // the copies start after the work already queued on st (which may still read stack_buf)
+    HDOG_CUDA_TRY(cudaEventRecord(c->start_ev, st));
+    HDOG_CUDA_TRY(cudaStreamWaitEvent(c->copy_st, c->start_ev, 0));
+    size_t z_done = 0;
+    for (size_t b = 0; b < nbatch; b++) {
+      const size_t last = starts[b + 1] - 1;
+      const size_t z_end = std::min((size_t)length, (size_t)z0s[last] + (size_t)c->D);
+      if (z_end > z_done) {
+        HDOG_CUDA_TRY(cudaMemcpyAsync(c->stack_buf + z_done * plane, stack + z_done * plane,
+                                      (z_end - z_done) * plane * sizeof(uint16_t), cudaMemcpyHostToDevice,
+                                      c->copy_st));
+        z_done = z_end;
+      }
+      HDOG_CUDA_TRY(cudaEventRecord(c->chunk_ev[b], c->copy_st));
+    }
     dev = c->stack_buf;
   }
-  for (size_t b = 0; b < z0s.size(); b += (size_t)c->max_sub) {
-    const int nsub = (int)std::min<size_t>((size_t)c->max_sub, z0s.size() - b);
+  for (size_t b = 0; b < nbatch; b++) {
+    const size_t first = starts[b];
+    const int nsub = (int)(starts[b + 1] - first);
+    if (!on_device) HDOG_CUDA_TRY(cudaStreamWaitEvent(st, c->chunk_ev[b], 0));
     for (int s = 0; s < nsub; s++) {
-      const int z0 = z0s[b + s];
+      const int z0 = z0s[first + s];
       set_sub(c, s, dev + (size_t)z0 * plane, std::min(c->D, length - z0), z0);
     }
     TRY(run_batch(c, nsub, st));
@@ -994,6 +1062,10 @@ extern "C" int hdog_ctx_set_option(hdog_ctx *c, int option, int value) {
   std::lock_guard<std::mutex> lock(c->mu);
   switch (option) {
     case HDOG_OPT_FUSED_SWEEP: c->use_sweep = value != 0; return HDOG_OK;
+    case HDOG_OPT_HOST_BATCH:
+      if (value < 0) return fail(HDOG_ERR_ARG, "HDOG_OPT_HOST_BATCH must be >= 0");
+      c->host_batch = value;
+      return HDOG_OK;
     default: return fail(HDOG_ERR_ARG, "unknown option");
   }
 }

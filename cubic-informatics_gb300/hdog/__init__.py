@@ -23,7 +23,7 @@ MAIN_PATH = os.path.join(BUILD_DIR, "hdog_main")
 
 HDOG_OK, HDOG_ERR_ARG, HDOG_ERR_SHAPE, HDOG_ERR_CUDA, HDOG_ERR_IO = 0, 1, 2, 3, 4
 HDOG_ERR_PARAM, HDOG_ERR_CAPACITY, HDOG_ERR_TIMEOUT, HDOG_ERR_NOMEM = 5, 6, 7, 8
-HDOG_OPT_FUSED_SWEEP = 1
+HDOG_OPT_FUSED_SWEEP, HDOG_OPT_HOST_BATCH = 1, 2
 
 # The 28-byte candidate record (FeatureVector, src/3D/utils.h:188-197).
 DT_LOCAL = np.dtype([
@@ -289,6 +289,11 @@ class Context:
     def set_fused_sweep(self, on):
         """DoG + Hessian + PD in one z-sweep kernel (default) or as separate passes."""
         check(lib().hdog_ctx_set_option(self._h, HDOG_OPT_FUSED_SWEEP, int(bool(on))))
+
+    def set_host_batch(self, n):
+        """Substacks in the first batch of run_stack with a host-memory stack (0: the
+        context's max_substacks); the copy of the later slices overlaps that batch."""
+        check(lib().hdog_ctx_set_option(self._h, HDOG_OPT_HOST_BATCH, int(n)))
 
     def timing(self, on=True):
         """Per-kernel CUDA-event timing of this context's launches."""
