@@ -618,58 +618,85 @@ __global__ void __launch_bounds__(kHThreads, 3)
     // every in-plane gradient position of the quad inside the volume: the plain stencil
     // (only the z neighbours can fall outside, handled by zup / zdn)
     if (X0 >= 1 && X0 + 3 <= W - 2 && Y >= 1 && Y <= H - 2) {
-      auto ld12 = [&](const float *src, float *dst) {   // columns X0-4 .. X0+7
+      // Voxels o = 2p, 2p+1 of the quad go as one pair through f32x2 subtract and multiply
+      // (each lane rounds as the scalar operation does): every stencil operand that sits
+      // at the same offset from both voxels comes from one 8-byte-aligned pair of a
+      // 128-bit ring load.  The x gradients of the xy and xz elements are taken at odd
+      // offsets, so they stay scalar and only their outer difference is paired.
+      auto ld12 = [&](const float *src, float2 *dst) {   // columns X0-4 .. X0+7 as 6 pairs
 #pragma unroll
         for (int i = 0; i < 3; i++) {
           const float4 f = *reinterpret_cast<const float4 *>(src + 4 * i);
-          dst[4 * i] = f.x; dst[4 * i + 1] = f.y; dst[4 * i + 2] = f.z; dst[4 * i + 3] = f.w;
+          dst[2 * i] = make_float2(f.x, f.y);
+          dst[2 * i + 1] = make_float2(f.z, f.w);
         }
       };
-      auto ld4 = [&](const float *src, float *dst) {    // columns X0 .. X0+3
+      auto ld4 = [&](const float *src, float2 *dst) {    // columns X0 .. X0+3 as 2 pairs
         const float4 f = *reinterpret_cast<const float4 *>(src + 4);
-        dst[0] = f.x; dst[1] = f.y; dst[2] = f.z; dst[3] = f.w;
+        dst[0] = make_float2(f.x, f.y);
+        dst[1] = make_float2(f.z, f.w);
       };
-      // voxel o sits at index o + 4 of a 12-column row
+      const float2 half = make_float2(0.5f, 0.5f), zero2 = make_float2(0.0f, 0.0f);
+      auto hd2 = [&](float2 plus, float2 minus) { return mul2(sub2(plus, minus), half); };
+      float2 h2[2][6];   // [pair][element]
       {
-        float a[12], v[4], w[4], p2[4], m2[4];
+        float2 a[6], v[2], w[2], p2[2], m2[2];
         ld12(P0 + b, a);
         ld4(P0 + b - 2 * kHPX, v);
         ld4(P0 + b + 2 * kHPX, w);
         ld4(P2 + b, p2);
         ld4(M2 + b, m2);
 #pragma unroll
-        for (int o = 0; o < 4; o++) {
-          const float c = a[o + 4];
-          hv[o][0] = hdiff(hdiff(a[o + 6], c), hdiff(c, a[o + 2]));
-          hv[o][3] = hdiff(hdiff(w[o], c), hdiff(c, v[o]));
-          hv[o][5] = hdiff(zup ? hdiff(p2[o], c) : 0.0f, zdn ? hdiff(c, m2[o]) : 0.0f);
+        for (int p = 0; p < 2; p++) {
+          const float2 c = a[2 + p];   // voxels 2p, 2p+1 at row index 4 + 2p
+          h2[p][0] = hd2(hd2(a[3 + p], c), hd2(c, a[1 + p]));
+          h2[p][3] = hd2(hd2(w[p], c), hd2(c, v[p]));
+          h2[p][5] = hd2(zup ? hd2(p2[p], c) : zero2, zdn ? hd2(c, m2[p]) : zero2);
         }
       }
       {
-        float u[12], dn[12];
+        float2 u[6], dn[6];
         ld12(P0 + b - kHPX, u);
         ld12(P0 + b + kHPX, dn);
+        const float *uf = reinterpret_cast<const float *>(u), *df = reinterpret_cast<const float *>(dn);
 #pragma unroll
-        for (int o = 0; o < 4; o++) hv[o][1] = hdiff(hdiff(dn[o + 5], dn[o + 3]), hdiff(u[o + 5], u[o + 3]));
+        for (int p = 0; p < 2; p++) {
+          const int o = 2 * p;
+          const float2 gd = make_float2(hdiff(df[o + 5], df[o + 3]), hdiff(df[o + 6], df[o + 4]));
+          const float2 gu = make_float2(hdiff(uf[o + 5], uf[o + 3]), hdiff(uf[o + 6], uf[o + 4]));
+          h2[p][1] = hd2(gd, gu);
+        }
       }
       {
-        float p[12], m[12];
-        ld12(P1 + b, p);
-        ld12(M1 + b, m);
+        float2 pp[6], mm[6];
+        ld12(P1 + b, pp);
+        ld12(M1 + b, mm);
+        const float *pf = reinterpret_cast<const float *>(pp), *mf = reinterpret_cast<const float *>(mm);
 #pragma unroll
-        for (int o = 0; o < 4; o++)
-          hv[o][2] = hdiff(zup ? hdiff(p[o + 5], p[o + 3]) : 0.0f, zdn ? hdiff(m[o + 5], m[o + 3]) : 0.0f);
+        for (int p = 0; p < 2; p++) {
+          const int o = 2 * p;
+          const float2 gp = zup ? make_float2(hdiff(pf[o + 5], pf[o + 3]), hdiff(pf[o + 6], pf[o + 4])) : zero2;
+          const float2 gm = zdn ? make_float2(hdiff(mf[o + 5], mf[o + 3]), hdiff(mf[o + 6], mf[o + 4])) : zero2;
+          h2[p][2] = hd2(gp, gm);
+        }
       }
       {
-        float pu[4], pd[4], mu[4], md[4];
+        float2 pu[2], pd[2], mu[2], md[2];
         ld4(P1 + b - kHPX, pu);
         ld4(P1 + b + kHPX, pd);
         ld4(M1 + b - kHPX, mu);
         ld4(M1 + b + kHPX, md);
 #pragma unroll
-        for (int o = 0; o < 4; o++)
-          hv[o][4] = hdiff(zup ? hdiff(pd[o], pu[o]) : 0.0f, zdn ? hdiff(md[o], mu[o]) : 0.0f);
+        for (int p = 0; p < 2; p++)
+          h2[p][4] = hd2(zup ? hd2(pd[p], pu[p]) : zero2, zdn ? hd2(md[p], mu[p]) : zero2);
       }
+#pragma unroll
+      for (int p = 0; p < 2; p++)
+#pragma unroll
+        for (int k = 0; k < 6; k++) {
+          hv[2 * p][k] = h2[p][k].x;
+          hv[2 * p + 1][k] = h2[p][k].y;
+        }
       uint32_t mword = 0;
 #pragma unroll
       for (int o = 0; o < 4; o++) {
