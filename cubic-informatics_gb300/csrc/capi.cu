@@ -850,6 +850,60 @@ extern "C" int hdog_run_stack(hdog_ctx *c, const uint16_t *stack, int stack_on_d
   return copy_out(c->last, out, cap, n_records);
 }
 
+extern "C" int hdog_run_stacks(hdog_ctx *c, const hdog_stack_in *stacks, int n_stacks, hdog_record *out,
+                               int64_t cap, int64_t *n_records, int64_t *stack_counts, void *stream) {
+  CTX_GUARD(c);
+  if (!n_records || n_stacks < 0 || (n_stacks > 0 && !stacks) || (cap > 0 && !out))
+    return fail(HDOG_ERR_ARG, "hdog_run_stacks: bad argument");
+  for (int i = 0; i < n_stacks; i++)
+    if ((!stacks[i].data && stacks[i].length > 0) || stacks[i].length < 0)
+      return fail(HDOG_ERR_ARG, "hdog_run_stacks: bad stack");
+  cudaStream_t st = (cudaStream_t)stream;
+  c->last.clear();
+  if (stack_counts)
+    for (int i = 0; i < n_stacks; i++) stack_counts[i] = 0;
+  const size_t plane = (size_t)c->W * c->H;
+  // every stack's substacks, stack by stack
+  struct Item { int stack, z0; };
+  std::vector<Item> items;
+  std::vector<int> z0s;
+  for (int i = 0; i < n_stacks; i++) {
+    TRY(schedule(stacks[i].length, c->D, c->margin, z0s));
+    for (int z0 : z0s) items.push_back({i, z0});
+  }
+  // host stacks go to device buffers of this call
+  std::vector<uint16_t *> dev(n_stacks, nullptr), owned;
+  struct Free {
+    std::vector<uint16_t *> &v;
+    ~Free() { for (uint16_t *p : v) cudaFree(p); }
+  } free_owned{owned};
+  for (int i = 0; i < n_stacks; i++) {
+    if (stacks[i].on_device) {
+      dev[i] = const_cast<uint16_t *>(stacks[i].data);
+      continue;
+    }
+    const size_t bytes = (size_t)stacks[i].length * plane * sizeof(uint16_t);
+    if (!bytes) continue;
+    uint16_t *d = nullptr;
+    if (cudaMalloc(&d, bytes) != cudaSuccess) return fail(HDOG_ERR_NOMEM, "hdog_run_stacks: no device memory for a stack");
+    owned.push_back(d);
+    HDOG_CUDA_TRY(cudaMemcpyAsync(d, stacks[i].data, bytes, cudaMemcpyHostToDevice, st));
+    dev[i] = d;
+  }
+  for (size_t b = 0; b < items.size(); b += (size_t)c->max_sub) {
+    const int nsub = (int)std::min(items.size() - b, (size_t)c->max_sub);
+    for (int s = 0; s < nsub; s++) {
+      const Item &it = items[b + s];
+      set_sub(c, s, dev[it.stack] + (size_t)it.z0 * plane, std::min(c->D, stacks[it.stack].length - it.z0), it.z0);
+    }
+    TRY(run_batch(c, nsub, st));
+    if (stack_counts)
+      for (int s = 0; s < nsub; s++) stack_counts[items[b + s].stack] += c->h_counts[s];
+    TRY(collect_records(c, nsub, c->last, st));
+  }
+  return copy_out(c->last, out, cap, n_records);
+}
+
 // ------------------------------------------------------------------ after the records
 extern "C" int hdog_records_to_global(const hdog_record *d_records, int64_t n, const hdog_global_params *p,
                                       hdog_global *d_out, void *stream) {

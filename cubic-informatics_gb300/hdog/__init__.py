@@ -97,6 +97,10 @@ class hdog_clf_params(ctypes.Structure):
                 ("bias_before_log", ctypes.c_double * 3), ("is_ave", ctypes.c_int)]
 
 
+class hdog_stack_in(ctypes.Structure):
+    _fields_ = [("data", ctypes.c_void_p), ("on_device", ctypes.c_int), ("length", ctypes.c_int)]
+
+
 _SIGNATURES = {
     "hdog_last_error": (ctypes.c_char_p, []),
     "hdog_abi_version": (ctypes.c_int, []),
@@ -118,6 +122,8 @@ _SIGNATURES = {
     "hdog_run_stack": (ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.c_int, _P, ctypes.c_int64,
                                       ctypes.POINTER(ctypes.c_int64), _P]),
     "hdog_last_records": (ctypes.c_int, [_P, _P, ctypes.c_int64, ctypes.POINTER(ctypes.c_int64)]),
+    "hdog_run_stacks": (ctypes.c_int, [_P, ctypes.POINTER(hdog_stack_in), ctypes.c_int, _P, ctypes.c_int64,
+                                       ctypes.POINTER(ctypes.c_int64), _P, _P]),
     "hdog_run_param_file": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int]),
     "hdog_ctx_set_option": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int]),
     "hdog_ccl_noalloc": (ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P]),
@@ -407,6 +413,23 @@ class Context:
         rc = lib().hdog_run_stack(self._h, ptr, on_dev, length, _out_ptr(out), len(out), ctypes.byref(n),
                                   _stream(stream) if on_dev else None)
         return self._finish(rc, out, n)
+
+    def run_stacks(self, stacks, cap=None, stream=None, out=None):
+        """Many stacks (each (length, H, W): numpy uint16 or CUDA tensor) with their
+        substacks packed into full batches across stacks -> (records, per-stack counts);
+        the records are stack by stack, as run_stack gives each stack's."""
+        descs = (hdog_stack_in * max(1, len(stacks)))()
+        for i, a in enumerate(stacks):
+            on_dev, ptr = _buffer(a)
+            descs[i].data = ptr.value
+            descs[i].on_device = on_dev
+            descs[i].length = int(a.shape[0])
+        counts = np.zeros(max(1, len(stacks)), np.int64)
+        out = _out_array(out, cap)
+        n = ctypes.c_int64()
+        rc = lib().hdog_run_stacks(self._h, descs, len(stacks), _out_ptr(out), len(out), ctypes.byref(n),
+                                   ctypes.c_void_p(counts.ctypes.data), _stream(stream))
+        return self._finish(rc, out, n), counts[:len(stacks)]
 
     def _finish(self, rc, out, n):
         """Records of a whole-chain call.  Without a capacity the call only counts them, and

@@ -28,6 +28,8 @@
  *                                                            src/3D/HDoG3D_main.cpp:134-257,
  *                                                            src/3D/utils.h:204-250
  *   hdog_run_stack          the substack loop of main        src/3D/HDoG3D_main.cpp:294-315
+ *   hdog_run_stacks         main's loop over the stacks of a parameter file
+ *                                                            src/3D/HDoG3D_main.cpp:287-316
  *   hdog_records_to_global  HDoGResultStack                  script/HalfBrainCells.py:44-56
  *   hdog_scale_merge        process_stack (scale merge)      script/MergeBrain.py:546-570
  *   hdog_classifier_features get_X_3d                        script/HDoG_classifier.py:158-176
@@ -146,7 +148,20 @@ int hdog_run_substack(hdog_ctx *ctx, const uint16_t *img, int img_on_device, int
    context has room, records appended in substack order. */
 int hdog_run_stack(hdog_ctx *ctx, const uint16_t *stack, int stack_on_device, int length,
                    hdog_record *out, int64_t cap, int64_t *n_records, void *stream);
-/* The records of the context's last hdog_run_substack / hdog_run_stack call, kept by the
+/* Many stacks of the context's width and height in one call: the substacks of all stacks
+   (each stack in its own HDoG3D_main schedule) are packed into batches of as many as the
+   context holds, across stack boundaries, so uneven stack lengths leave no partial batches
+   but the last.  Records come out stack by stack, each stack's in substack order, exactly as
+   hdog_run_stack gives them; stack_counts[i] (may be NULL) receives stack i's count.  Host
+   stacks are copied to device memory the call allocates and frees. */
+typedef struct hdog_stack_in {
+  const uint16_t *data;   /* length slices of width * height uint16, x fastest */
+  int on_device;          /* 1: device memory, 0: host memory */
+  int length;             /* slices */
+} hdog_stack_in;
+int hdog_run_stacks(hdog_ctx *ctx, const hdog_stack_in *stacks, int n_stacks, hdog_record *out, int64_t cap,
+                    int64_t *n_records, int64_t *stack_counts, void *stream);
+/* The records of the context's last hdog_run_substack / hdog_run_stack / hdog_run_stacks call, kept by the
    context (also after that call returned HDOG_ERR_CAPACITY): a caller whose buffer was
    too small sizes a new one from *n_records and fetches them here instead of running
    the chain again.  No counterpart in the reference (HDoG3D_main writes records to a

@@ -151,3 +151,22 @@ def test_fused_sweep_equals_separate_passes(W, H, D, dv, sigmas):
     assert fused.tobytes() == plain.tobytes()
     ref = orc.substack(orc.params_from(p), padded(vol, D, dv), dv, 3)[0]
     assert_records_match(fused, ref, "fused %dx%dx%d %s" % (W, H, D, sigmas))
+
+
+@pytest.mark.gpu
+def test_run_stacks_packs_across_stacks_like_per_stack_runs():
+    """hdog_run_stacks (substacks of several stacks packed into shared batches) gives each
+    stack's records exactly as hdog_run_stack does, stack by stack, with the counts."""
+    import torch
+    W, H, D = 256, 192, 32
+    p = params(W, H, D, margins=6)
+    lengths = [40, 75, 9, 0, 33]
+    stacks = [volume(W, H, max(L, 1), n_nuclei=max(1, L * 8), seed=9000 + i)[:L] for i, L in enumerate(lengths)]
+    with hdog.Context(p, max_substacks=3) as ctx:
+        per = [ctx.run_stack(np.ascontiguousarray(s)) if len(s) else np.zeros(0, hdog.DT_LOCAL) for s in stacks]
+        inputs = [torch.from_numpy(np.ascontiguousarray(s)).cuda() if i % 2 == 0 else np.ascontiguousarray(s)
+                  for i, s in enumerate(stacks)]
+        recs, counts = ctx.run_stacks(inputs)
+    assert list(counts) == [len(r) for r in per]
+    assert recs.tobytes() == np.concatenate(per).tobytes()
+    assert sum(len(r) for r in per) > 50
