@@ -295,6 +295,83 @@ def uneven_workload(args):
     return 0
 
 
+STREAM = ("dense stack uint16 2560x2160x1536 (17 GB) in pinned host memory, 1.5M nuclei, 30% of them in "
+          "touching clusters of 2-6; HDoG depth 32 (96 overlapping substacks), sigma_dog (2,1.5,3.2,2.4), "
+          "radius_norm (20,5); per-substack labels as the reference")
+
+
+def stream_nuclei(w, h, d, total, seed):
+    """total nuclei, 30% of them in clusters of 2-6: each cluster's extra members touch its
+    first one, at centre distance 0.8 (sigma_a + sigma_b) along a random direction."""
+    from hdog import synth
+    rng = np.random.default_rng(seed)
+    sizes = rng.integers(2, 7, size=int(0.3 * total) // 2 + 1)
+    sizes = sizes[: np.searchsorted(np.cumsum(sizes), int(0.3 * total)) + 1]
+    n_seed = total - int(sizes.sum()) + len(sizes)
+    base = synth.nuclei(synth.spec(w, h, d, n_seed, seed))   # (x, y, z, sigma_xy, sigma_z, peak)
+    first = np.repeat(np.arange(len(sizes)), sizes - 1)       # the cluster each extra member joins
+    extra = base[rng.integers(len(base), size=len(first))].copy()
+    v = rng.normal(size=(len(first), 3))
+    v /= np.linalg.norm(v, axis=1, keepdims=True)
+    a = base[first]
+    dist = 0.8 * (a[:, 3] + extra[:, 3])
+    extra[:, :3] = a[:, :3] + v * np.stack([dist, dist, dist * a[:, 4] / a[:, 3]], axis=1)
+    keep = (extra[:, 0] >= 0) & (extra[:, 0] < w) & (extra[:, 1] >= 0) & (extra[:, 1] < h) & \
+           (extra[:, 2] >= 0) & (extra[:, 2] < d)
+    return np.concatenate([base, extra[keep]])
+
+
+def stream_workload(args):
+    """The 17 GB stack from pinned host memory through hdog_run_stack: its chunks are copied
+    on a second stream while the first batches run.  Batched (8 substacks per launch) and
+    plain (one per launch) forms, records compared."""
+    import torch
+    import hdog
+    from hdog import synth
+    torch.cuda.set_device(0)
+    w, h, d = 2560, 2160, 1536
+    t0 = time.time()
+    nuc = stream_nuclei(w, h, d, 1_500_000, synth.SEED_BASE + 4)
+    spec = synth.spec(w, h, d, len(nuc), synth.SEED_BASE + 4)
+    host = torch.empty((d, h, w), dtype=torch.uint16).pin_memory()
+    hn = host.numpy()
+    for z0 in range(0, d, 128):
+        hn[z0:z0 + 128] = synth.volume(spec, z0, min(d, z0 + 128), nuc=nuc)
+    gen_s = time.time() - t0
+    p = hdog.make_params(**PARAMS)
+    unique = w * h * d
+    res = {}
+    for name, max_sub, steps in (("batched", 8, args.steps), ("plain", 1, max(1, min(args.steps, 2)))):
+        with hdog.Context(p, max_substacks=max_sub) as ctx:
+            out = np.empty(0, hdog.DT_LOCAL)
+            for _ in range(max(1, args.warmup)):
+                r = ctx.run_stack(hn, out=out)
+                if len(r) > len(out):
+                    out = np.empty(len(r), hdog.DT_LOCAL)
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            for _ in range(steps):
+                r = ctx.run_stack(hn, out=out)
+            torch.cuda.synchronize()
+            res[name] = ((time.perf_counter() - t) * 1e3 / steps, r.copy())
+    assert res["batched"][1].tobytes() == res["plain"][1].tobytes(), "batched and plain records differ"
+    bms, pms = res["batched"][0], res["plain"][0]
+    nsub = len(hdog.substack_schedule(d, DEPTH, hdog.depth_margin(p)))
+    line = {"metric": METRIC, "value": unique / (bms * 1e-3) / 1e9, "unit": "Gvox/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": bms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": STREAM, "substacks": nsub, "nuclei": int(len(nuc)),
+                       "unique_voxels_per_step": unique, "records_per_step": int(len(res["batched"][1])),
+                       "mode": "end to end: pinned host stack, chunked H2D overlapping the batches, records D2H",
+                       "generator_s": round(gen_s, 1)},
+            "plain": {"value": unique / (pms * 1e-3) / 1e9, "ms_per_step": pms, "mode": "one substack per launch"},
+            "batched_over_plain": pms / bms,
+            "e2e": {"value": unique / (bms * 1e-3) / 1e9, "unit": "Gvox/s", "h2d_bytes_per_step": unique * 2,
+                    "d2h_bytes_per_step": int(len(res["batched"][1])) * 28}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -302,8 +379,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="camera", choices=["camera", "uneven"],
-                    help="camera: the 2560x2160x128 stack (default); uneven: the 40-stack mix")
+    ap.add_argument("--workload", default="camera", choices=["camera", "uneven", "stream"],
+                    help="camera: the 2560x2160x128 stack (default); uneven: the 40-stack mix; "
+                         "stream: the 17 GB stack from host memory")
     ap.add_argument("--profile-case", action="store_true",
                     help="run one 1280x1080x32 substack twice (the small case the ncu summaries capture)")
     args = ap.parse_args()
@@ -313,6 +391,8 @@ def main():
         return profile_case()
     if args.workload == "uneven":
         return uneven_workload(args)
+    if args.workload == "stream":
+        return stream_workload(args)
 
     import torch
     import hdog
