@@ -904,6 +904,29 @@ extern "C" int hdog_run_stacks(hdog_ctx *c, const hdog_stack_in *stacks, int n_s
   return copy_out(c->last, out, cap, n_records);
 }
 
+// ------------------------------------------------------------------ differentiable chain
+extern "C" size_t hdog_soft_workspace_bytes(const hdog_soft_params *p) { return p ? soft_workspace_bytes(*p) : 0; }
+
+extern "C" int hdog_soft_forward(const hdog_soft_params *p, const float *d_volume, const int32_t *d_pos, int n_pos,
+                                 const int32_t *d_neg, int n_neg, float *d_loss, float *d_scores, void *d_workspace,
+                                 void *stream) {
+  const int rc = soft_forward(p, d_volume, d_pos, n_pos, d_neg, n_neg, d_loss, d_scores, d_workspace,
+                              (cudaStream_t)stream);
+  if (rc != HDOG_OK) return fail(rc, "hdog_soft_forward: bad argument, parameter or sigma");
+  HDOG_CUDA_TRY(cudaGetLastError());
+  return HDOG_OK;
+}
+
+extern "C" int hdog_soft_backward(const hdog_soft_params *p, const float *d_volume, const int32_t *d_pos, int n_pos,
+                                  const int32_t *d_neg, int n_neg, float grad_loss, float *d_grad_volume,
+                                  float *d_grad_sigma, void *d_workspace, void *stream) {
+  const int rc = soft_backward(p, d_volume, d_pos, n_pos, d_neg, n_neg, grad_loss, d_grad_volume, d_grad_sigma,
+                               d_workspace, (cudaStream_t)stream);
+  if (rc != HDOG_OK) return fail(rc, "hdog_soft_backward: bad argument, parameter or sigma");
+  HDOG_CUDA_TRY(cudaGetLastError());
+  return HDOG_OK;
+}
+
 // ------------------------------------------------------------------ after the records
 extern "C" int hdog_records_to_global(const hdog_record *d_records, int64_t n, const hdog_global_params *p,
                                       hdog_global *d_out, void *stream) {

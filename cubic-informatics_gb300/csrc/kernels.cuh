@@ -88,6 +88,13 @@ void launch_scale_merge(const hdog_global *in, int64_t n, const hdog_scalemerge_
                         cudaStream_t s);
 void launch_clf_features(const hdog_record *rec, int64_t n, const hdog_clf_params &p, double *X, cudaStream_t s);
 
+// soft.cu: the differentiable chain (hdog_soft_*); status codes as the C ABI
+size_t soft_workspace_bytes(const hdog_soft_params &p);
+int soft_forward(const hdog_soft_params *p, const float *vol, const int32_t *pos, int n_pos, const int32_t *neg,
+                 int n_neg, float *loss, float *scores, void *work, cudaStream_t st);
+int soft_backward(const hdog_soft_params *p, const float *vol, const int32_t *pos, int n_pos, const int32_t *neg,
+                  int n_neg, float grad_loss, float *grad_vol, float *grad_sigma, void *work, cudaStream_t st);
+
 bool launch_dog_sweep(const Sub *d_subs, int nsub, int W, int H, int D, const DogTaps &T, const float *norm,
                       float *dog, int *d_status, int max_smem, cudaStream_t s);
 // DoG + Hessian + PD: the radius-specialised pair (norm -> dog -> mask + list) when the tap

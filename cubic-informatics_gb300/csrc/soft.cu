@@ -1,0 +1,482 @@
+// soft.cu -- the differentiable HDoG chain, sm_103a: forward and hand-written adjoint of
+// normalize -> DoG -> Hessian -> relaxed positive-definiteness score at sample points.
+//
+// Forward stages follow the reference's (NormalizeFilter.cu:537-654, DoG3DFilter.cu:70-437,
+// Hessian3DFilter_element.cu:22-388) with its borders, in float32 without the bit-exact
+// summation orders of the detection path: min / max and box means with nearest borders,
+// separable Gaussians with zero borders (one sigma per axis and scale), central
+// differences of central differences with zeros outside the volume, and the mask test
+// xx < 0, xx yy - xy^2 > 0, det < 0 relaxed to a product of sigmoids of the minors scaled
+// by tau, tau^2, tau^3.  Loss = mean score at the positive points - mean score at the
+// negative points.
+//
+// Backward recomputes every intermediate from the input (nothing is kept between the two
+// calls) and runs the adjoints in reverse: the score's derivative scattered through the
+// Hessian stencil into a DoG-shaped gradient; for the sigmas, the derivative-of-Gaussian
+// taps (d t_k / d sigma = t_k (k^2 - sum_j t_j j^2) / sigma^3 for the normalized taps) on
+// one axis and the plain taps on the others, dotted with that gradient, plus the
+// normalizer's term; for the input, the transposed separable Gaussians (the taps are
+// symmetric and the borders zero, so the transpose is the same correlation), the
+// normalization's quotient rule, the transposed box means (a gather that counts how often
+// the nearest border repeats each edge value) and the transposed min / max filters (each
+// window's gradient goes to its first extreme, recomputed from the filter's input).
+// Tap radii are (int)(2 sigma + 0.5), held fixed for the derivatives.
+#include <cmath>
+
+#include "kernels.cuh"
+
+namespace hdog {
+
+constexpr int kSoftMaxRadius = 31;
+constexpr int kSoftMaxTaps = 2 * kSoftMaxRadius + 1;
+struct SoftTaps {
+  float k[kSoftMaxTaps];
+  int r;
+};
+enum { kMin = 0, kMax = 1, kBox = 2, kConv = 3 };
+struct SoftGeom {
+  int W, H, D;
+};
+
+__device__ __forceinline__ void soft_axis(const SoftGeom &g, int axis, int64_t i, int &c, int64_t &stride, int &n) {
+  const int x = (int)(i % g.W), y = (int)((i / g.W) % g.H), z = (int)(i / ((int64_t)g.W * g.H));
+  if (axis == 0) { c = x; stride = 1; n = g.W; }
+  else if (axis == 1) { c = y; stride = g.W; n = g.H; }
+  else { c = z; stride = (int64_t)g.W * g.H; n = g.D; }
+}
+
+// One separable pass along `axis` (0 x, 1 y, 2 z): min / max / box mean with nearest
+// borders, or the correlation with T (zero border).
+__global__ void k_soft_pass(const float *in, float *out, SoftGeom g, int axis, int mode, int r, SoftTaps T, int64_t N) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  int c, n;
+  int64_t s;
+  soft_axis(g, axis, i, c, s, n);
+  const float *line = in + (i - (int64_t)c * s);
+  float acc;
+  if (mode == kConv) {
+    acc = 0.0f;
+    for (int j = -T.r; j <= T.r; j++) {
+      const int p = c + j;
+      if (p >= 0 && p < n) acc = __fmaf_rn(T.k[j + T.r], line[(int64_t)p * s], acc);
+    }
+  } else if (mode == kBox) {
+    acc = 0.0f;
+    for (int j = -r; j <= r; j++) acc += line[(int64_t)clampi(c + j, 0, n - 1) * s];
+    acc = acc / (float)(2 * r + 1);
+  } else {
+    acc = line[(int64_t)clampi(c - r, 0, n - 1) * s];
+    for (int j = -r + 1; j <= r; j++) {
+      const float v = line[(int64_t)clampi(c + j, 0, n - 1) * s];
+      acc = mode == kMin ? fminf(acc, v) : fmaxf(acc, v);
+    }
+  }
+  out[i] = acc;
+}
+
+// Transposed min / max pass: the output gradient of each window goes to the window's first
+// extreme (the index the forward filter took it from).  g_in must start at zero.
+__global__ void k_soft_minmax_adj(const float *in, const float *g_out, float *g_in, SoftGeom g, int axis, int r,
+                                  int is_max, int64_t N) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  const float go = g_out[i];
+  if (go == 0.0f) return;
+  int c, n;
+  int64_t s;
+  soft_axis(g, axis, i, c, s, n);
+  const int64_t base = i - (int64_t)c * s;
+  int arg = clampi(c - r, 0, n - 1);
+  float best = in[base + (int64_t)arg * s];
+  for (int j = -r + 1; j <= r; j++) {
+    const int p = clampi(c + j, 0, n - 1);
+    const float v = in[base + (int64_t)p * s];
+    if (is_max ? v > best : v < best) {
+      best = v;
+      arg = p;
+    }
+  }
+  atomicAdd(g_in + base + (int64_t)arg * s, go);
+}
+
+// Transposed box mean (nearest border), as a gather: input i receives every output t within
+// r of it, and an edge input additionally receives each output whose window ran past that
+// edge once per clamped tap.
+__global__ void k_soft_box_adj(const float *g_out, float *g_in, SoftGeom g, int axis, int r, int64_t N) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  int c, n;
+  int64_t s;
+  soft_axis(g, axis, i, c, s, n);
+  const float *line = g_out + (i - (int64_t)c * s);
+  float acc = 0.0f;
+  for (int t = max(0, c - r); t <= min(n - 1, c + r); t++) acc += line[(int64_t)t * s];
+  if (c == 0)
+    for (int t = 0; t < min(n, r); t++) acc += (float)(r - t) * line[(int64_t)t * s];
+  if (c == n - 1)
+    for (int t = max(0, n - 1 - r + 1); t < n; t++) acc += (float)(t + r - (n - 1)) * line[(int64_t)t * s];
+  g_in[i] = acc / (float)(2 * r + 1);
+}
+
+__global__ void k_soft_norm(const float *I, const float *e, const float *d, float *norm, float min_intensity, int64_t N) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  norm[i] = I[i] >= min_intensity ? (I[i] - e[i]) / (d[i] - e[i]) : 0.0f;
+}
+
+// Quotient rule of the normalization: g_I (direct term, written), g_e, g_d.
+__global__ void k_soft_norm_adj(const float *I, const float *e, const float *d, const float *g_norm, float *g_I,
+                                float *g_e, float *g_d, float min_intensity, int64_t N) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  const float g = g_norm[i];
+  if (I[i] >= min_intensity) {
+    const float den = d[i] - e[i], inv = 1.0f / den, inv2 = inv * inv;
+    g_I[i] = g * inv;
+    g_e[i] = g * (I[i] - d[i]) * inv2;
+    g_d[i] = -g * (I[i] - e[i]) * inv2;
+  } else {
+    g_I[i] = 0.0f;
+    g_e[i] = 0.0f;
+    g_d[i] = 0.0f;
+  }
+}
+
+// out = scale * (a - b)
+__global__ void k_soft_diff(const float *a, const float *b, float *out, float scale, int64_t N) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < N) out[i] = scale * (a[i] - b[i]);
+}
+
+__global__ void k_soft_add(float *a, const float *b, int64_t N) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < N) a[i] += b[i];
+}
+
+// sum_i a[i] * b[i] into *out (double; out must start at zero)
+__global__ void k_soft_dot(const float *a, const float *b, int64_t N, double *out) {
+  __shared__ double part[8];
+  double acc = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x)
+    acc += (double)a[i] * (double)b[i];
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xFFFFFFFFu, acc, o);
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += part[w];
+    atomicAdd(out, t);
+  }
+}
+
+// ---- Hessian at a point and its adjoint (element order xx, xy, xz, yy, yz, zz)
+__device__ __forceinline__ int h_inner(int e) { return e < 3 ? 0 : (e < 5 ? 1 : 2); }   // xx xy xz | yy yz | zz
+__device__ __forceinline__ int h_outer(int e) { return e == 0 ? 0 : (e == 1 || e == 3 ? 1 : 2); }
+
+struct SoftPoint {
+  int x, y, z;
+};
+__device__ __forceinline__ bool soft_in(const SoftGeom &g, int x, int y, int z) {
+  return x >= 0 && y >= 0 && z >= 0 && x < g.W && y < g.H && z < g.D;
+}
+__device__ __forceinline__ void soft_step(int axis, int s, int &x, int &y, int &z) {
+  if (axis == 0) x += s;
+  else if (axis == 1) y += s;
+  else z += s;
+}
+__device__ __forceinline__ float soft_f(const float *f, const SoftGeom &g, int x, int y, int z) {
+  return soft_in(g, x, y, z) ? f[((int64_t)z * g.H + y) * g.W + x] : 0.0f;
+}
+
+__device__ void soft_hessian(const float *f, const SoftGeom &g, SoftPoint p, float h[6]) {
+  for (int e = 0; e < 6; e++) {
+    float v = 0.0f;
+    for (int sb = -1; sb <= 1; sb += 2) {
+      int qx = p.x, qy = p.y, qz = p.z;
+      soft_step(h_outer(e), sb, qx, qy, qz);
+      if (!soft_in(g, qx, qy, qz)) continue;   // a first derivative outside the volume is 0
+      int ax = qx, ay = qy, az = qz, bx = qx, by = qy, bz = qz;
+      soft_step(h_inner(e), 1, ax, ay, az);
+      soft_step(h_inner(e), -1, bx, by, bz);
+      const float ga = 0.5f * (soft_f(f, g, ax, ay, az) - soft_f(f, g, bx, by, bz));
+      v += sb > 0 ? ga : -ga;
+    }
+    h[e] = 0.5f * v;
+  }
+}
+
+__device__ void soft_hessian_adj(float *gf, const SoftGeom &g, SoftPoint p, const float gh[6]) {
+  for (int e = 0; e < 6; e++) {
+    for (int sb = -1; sb <= 1; sb += 2) {
+      int qx = p.x, qy = p.y, qz = p.z;
+      soft_step(h_outer(e), sb, qx, qy, qz);
+      if (!soft_in(g, qx, qy, qz)) continue;
+      const float c = 0.25f * (float)sb * gh[e];
+      int ax = qx, ay = qy, az = qz, bx = qx, by = qy, bz = qz;
+      soft_step(h_inner(e), 1, ax, ay, az);
+      soft_step(h_inner(e), -1, bx, by, bz);
+      if (soft_in(g, ax, ay, az)) atomicAdd(gf + ((int64_t)az * g.H + ay) * g.W + ax, c);
+      if (soft_in(g, bx, by, bz)) atomicAdd(gf + ((int64_t)bz * g.H + by) * g.W + bx, -c);
+    }
+  }
+}
+
+__device__ __forceinline__ float sigm(float v) { return 1.0f / (1.0f + expf(-v)); }
+
+// Score of Hessian h and, when ds is given, its derivative in h.
+__device__ float soft_score(const float h[6], float tau, float *ds) {
+  const float xx = h[0], xy = h[1], xz = h[2], yy = h[3], yz = h[4], zz = h[5];
+  const float t2 = tau * tau, t3 = t2 * tau;
+  const float m2 = xx * yy - xy * xy;
+  const float det = xx * yy * zz + 2.0f * xy * yz * xz - xx * yz * yz - yy * xz * xz - zz * xy * xy;
+  const float A = sigm(-xx / tau), B = sigm(m2 / t2), C = sigm(-det / t3);
+  const float s = A * B * C;
+  if (ds) {
+    const float ca = -(1.0f - A) / tau, cb = (1.0f - B) / t2, cc = -(1.0f - C) / t3;
+    // d det / d (xx, xy, xz, yy, yz, zz)
+    const float dd[6] = {yy * zz - yz * yz, 2.0f * yz * xz - 2.0f * zz * xy, 2.0f * xy * yz - 2.0f * yy * xz,
+                         xx * zz - xz * xz, 2.0f * xy * xz - 2.0f * xx * yz, xx * yy - xy * xy};
+    const float dm2[6] = {yy, -2.0f * xy, 0.0f, xx, 0.0f, 0.0f};
+    for (int k = 0; k < 6; k++) ds[k] = s * ((k == 0 ? ca : 0.0f) + cb * dm2[k] + cc * dd[k]);
+  }
+  return s;
+}
+
+// Forward at the points: scores (optional) and the loss (double, out must start at zero).
+__global__ void k_soft_points(const float *dog, SoftGeom g, const int32_t *pos, int n_pos, const int32_t *neg,
+                              int n_neg, float tau, float *scores, double *loss) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_pos + n_neg) return;
+  const int32_t *q = i < n_pos ? pos + 3 * i : neg + 3 * (i - n_pos);
+  const SoftPoint p{q[2], q[1], q[0]};
+  float h[6];
+  soft_hessian(dog, g, p, h);
+  const float s = soft_score(h, tau, nullptr);
+  if (scores) scores[i] = s;
+  atomicAdd(loss, i < n_pos ? (double)s / n_pos : -(double)s / n_neg);
+}
+
+// Backward at the points: d loss / d dog scattered into gdog (which must start at zero).
+__global__ void k_soft_points_adj(const float *dog, SoftGeom g, const int32_t *pos, int n_pos, const int32_t *neg,
+                                  int n_neg, float tau, float grad_loss, float *gdog) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_pos + n_neg) return;
+  const int32_t *q = i < n_pos ? pos + 3 * i : neg + 3 * (i - n_pos);
+  const SoftPoint p{q[2], q[1], q[0]};
+  float h[6], ds[6];
+  soft_hessian(dog, g, p, h);
+  soft_score(h, tau, ds);
+  const float w = i < n_pos ? grad_loss / (float)n_pos : -grad_loss / (float)n_neg;
+  for (int k = 0; k < 6; k++) ds[k] *= w;
+  soft_hessian_adj(gdog, g, p, ds);
+}
+
+__global__ void k_soft_to_float(const double *in, float *out, int n) {
+  const int i = threadIdx.x;
+  if (i < n) out[i] = (float)in[i];
+}
+
+// ------------------------------------------------------------------ host side
+namespace {
+
+struct SoftRun {
+  const hdog_soft_params &p;
+  SoftGeom g;
+  int64_t N;
+  cudaStream_t st;
+  float *w;      // workspace slots of N floats (after the accumulators)
+  double *acc;   // 8 doubles at the start of the workspace
+  unsigned blocks() const { return ceil_div(N, 256); }
+  float *slot(int k) const { return w + (int64_t)k * N; }
+};
+
+enum { S_MN1, S_MN2, S_MN, S_MX1, S_MX2, S_MX, S_E, S_D, S_NORM, S_DOG, S_T1, S_T2, S_T3, S_GDOG, S_GA, S_GB, S_GC,
+       kSoftSlots };
+
+SoftTaps no_taps() {
+  SoftTaps t;
+  memset(&t, 0, sizeof(t));
+  return t;
+}
+
+// Normalized Gaussian taps of sigma (or their derivative in sigma), radius (int)(2 sigma + 0.5).
+SoftTaps gauss_taps_f(double sigma, bool derivative) {
+  SoftTaps t = no_taps();
+  const int r = (int)(2.0 * sigma + 0.5);
+  t.r = r;
+  double e[kSoftMaxTaps], sum = 0.0, m2 = 0.0;
+  for (int k = -r; k <= r; k++) {
+    e[k + r] = exp(-0.5 * k * k / (sigma * sigma));
+    sum += e[k + r];
+  }
+  for (int k = -r; k <= r; k++) m2 += e[k + r] / sum * (double)k * k;
+  for (int k = -r; k <= r; k++) {
+    const double tk = e[k + r] / sum;
+    t.k[k + r] = (float)(derivative ? tk * ((double)k * k - m2) / (sigma * sigma * sigma) : tk);
+  }
+  return t;
+}
+
+void pass(const SoftRun &R, const float *in, float *out, int axis, int mode, int r, const SoftTaps &T) {
+  KLAUNCH("k_soft_pass", R.st, (k_soft_pass<<<R.blocks(), 256, 0, R.st>>>(in, out, R.g, axis, mode, r, T, R.N)));
+}
+
+// conv of `in` with taps (tx, ty, tz) along x, y, z -> out (t1, t2 as temporaries)
+void conv3(const SoftRun &R, const float *in, float *out, const SoftTaps &tx, const SoftTaps &ty, const SoftTaps &tz,
+           float *t1, float *t2) {
+  pass(R, in, t1, 0, kConv, 0, tx);
+  pass(R, t1, t2, 1, kConv, 0, ty);
+  pass(R, t2, out, 2, kConv, 0, tz);
+}
+
+// The forward chain into the workspace: min/max chains, box means, norm, dog.
+void forward_chain(const SoftRun &R, const float *vol) {
+  const hdog_soft_params &p = R.p;
+  const SoftTaps none = no_taps();
+  const int rr[3] = {p.radius_norm_xy, p.radius_norm_xy, p.radius_norm_z};
+  const float *src_mn = vol, *src_mx = vol;
+  const int smn[3] = {S_MN1, S_MN2, S_MN}, smx[3] = {S_MX1, S_MX2, S_MX};
+  for (int a = 0; a < 3; a++) {
+    pass(R, src_mn, R.slot(smn[a]), a, kMin, rr[a], none);
+    pass(R, src_mx, R.slot(smx[a]), a, kMax, rr[a], none);
+    src_mn = R.slot(smn[a]);
+    src_mx = R.slot(smx[a]);
+  }
+  pass(R, R.slot(S_MN), R.slot(S_T1), 0, kBox, rr[0], none);
+  pass(R, R.slot(S_T1), R.slot(S_T2), 1, kBox, rr[1], none);
+  pass(R, R.slot(S_T2), R.slot(S_E), 2, kBox, rr[2], none);
+  pass(R, R.slot(S_MX), R.slot(S_T1), 0, kBox, rr[0], none);
+  pass(R, R.slot(S_T1), R.slot(S_T2), 1, kBox, rr[1], none);
+  pass(R, R.slot(S_T2), R.slot(S_D), 2, kBox, rr[2], none);
+  KLAUNCH("k_soft_norm", R.st, (k_soft_norm<<<R.blocks(), 256, 0, R.st>>>(vol, R.slot(S_E), R.slot(S_D), R.slot(S_NORM),
+                                                                        p.min_intensity, R.N)));
+  const float *s = p.sigma;
+  conv3(R, R.slot(S_NORM), R.slot(S_T3), gauss_taps_f(s[0], false), gauss_taps_f(s[1], false), gauss_taps_f(s[2], false),
+        R.slot(S_T1), R.slot(S_T2));
+  conv3(R, R.slot(S_NORM), R.slot(S_GA), gauss_taps_f(s[3], false), gauss_taps_f(s[4], false), gauss_taps_f(s[5], false),
+        R.slot(S_T1), R.slot(S_T2));
+  const float nrm = (float)pow((double)s[0] * s[1] * s[2], (double)p.gamma);
+  KLAUNCH("k_soft_diff", R.st, (k_soft_diff<<<R.blocks(), 256, 0, R.st>>>(R.slot(S_T3), R.slot(S_GA), R.slot(S_DOG),
+                                                                        nrm, R.N)));
+}
+
+int check_params(const hdog_soft_params *p, const float *vol, const int32_t *pos, int n_pos, const int32_t *neg,
+                 int n_neg, void *work) {
+  if (!p || !vol || !work || n_pos < 0 || n_neg < 0 || (n_pos && !pos) || (n_neg && !neg))
+    return HDOG_ERR_ARG;
+  if (p->width < 1 || p->height < 1 || p->depth < 1 || p->radius_norm_xy < 0 || p->radius_norm_z < 0 ||
+      p->radius_norm_xy > 1000 || p->radius_norm_z > 1000 || !(p->tau > 0.0f))
+    return HDOG_ERR_PARAM;
+  for (int k = 0; k < 6; k++)
+    if (!(p->sigma[k] > 0.0f) || (int)(2.0 * p->sigma[k] + 0.5) > kSoftMaxRadius) return HDOG_ERR_SHAPE;
+  return HDOG_OK;
+}
+
+}  // namespace
+
+size_t soft_workspace_bytes(const hdog_soft_params &p) {
+  return 8 * sizeof(double) + (size_t)kSoftSlots * p.width * p.height * p.depth * sizeof(float);
+}
+
+int soft_forward(const hdog_soft_params *p, const float *vol, const int32_t *pos, int n_pos, const int32_t *neg,
+                 int n_neg, float *loss, float *scores, void *work, cudaStream_t st) {
+  const int rc = check_params(p, vol, pos, n_pos, neg, n_neg, work);
+  if (rc != HDOG_OK || !loss) return rc != HDOG_OK ? rc : HDOG_ERR_ARG;
+  SoftRun R{*p, SoftGeom{p->width, p->height, p->depth}, (int64_t)p->width * p->height * p->depth, st,
+            static_cast<float *>(work), nullptr};
+  R.acc = static_cast<double *>(work);
+  R.w = reinterpret_cast<float *>(R.acc + 8);
+  forward_chain(R, vol);
+  cudaMemsetAsync(R.acc, 0, sizeof(double), st);
+  if (n_pos + n_neg > 0)
+    KLAUNCH("k_soft_points", st, (k_soft_points<<<ceil_div(n_pos + n_neg, 128), 128, 0, st>>>(
+                                     R.slot(S_DOG), R.g, pos, n_pos, neg, n_neg, p->tau, scores, R.acc)));
+  k_soft_to_float<<<1, 32, 0, st>>>(R.acc, loss, 1);
+  return HDOG_OK;
+}
+
+int soft_backward(const hdog_soft_params *p, const float *vol, const int32_t *pos, int n_pos, const int32_t *neg,
+                  int n_neg, float grad_loss, float *grad_vol, float *grad_sigma, void *work, cudaStream_t st) {
+  const int rc = check_params(p, vol, pos, n_pos, neg, n_neg, work);
+  if (rc != HDOG_OK) return rc;
+  SoftRun R{*p, SoftGeom{p->width, p->height, p->depth}, (int64_t)p->width * p->height * p->depth, st,
+            static_cast<float *>(work), nullptr};
+  R.acc = static_cast<double *>(work);
+  R.w = reinterpret_cast<float *>(R.acc + 8);
+  const unsigned nb = R.blocks();
+  forward_chain(R, vol);
+  float *gdog = R.slot(S_GDOG);
+  cudaMemsetAsync(gdog, 0, R.N * sizeof(float), st);
+  if (n_pos + n_neg > 0)
+    KLAUNCH("k_soft_points_adj", st, (k_soft_points_adj<<<ceil_div(n_pos + n_neg, 128), 128, 0, st>>>(
+                                         R.slot(S_DOG), R.g, pos, n_pos, neg, n_neg, p->tau, grad_loss, gdog)));
+  const float *s = p->sigma;
+  const float nrm = (float)pow((double)s[0] * s[1] * s[2], (double)p->gamma);
+  if (grad_sigma) {
+    // acc[0..5]: <gdog, d dog / d sigma_k> without the normalizer term; acc[6]: <gdog, dog>
+    cudaMemsetAsync(R.acc, 0, 8 * sizeof(double), st);
+    const unsigned db = 152 * 4;
+    for (int k = 0; k < 6; k++) {
+      const int sc = k / 3, ax = k % 3;
+      SoftTaps t[3];
+      for (int a = 0; a < 3; a++) t[a] = gauss_taps_f(s[3 * sc + a], a == ax);
+      conv3(R, R.slot(S_NORM), R.slot(S_T3), t[0], t[1], t[2], R.slot(S_T1), R.slot(S_T2));
+      KLAUNCH("k_soft_dot", st, (k_soft_dot<<<db, 256, 0, st>>>(gdog, R.slot(S_T3), R.N, R.acc + k)));
+    }
+    KLAUNCH("k_soft_dot", st, (k_soft_dot<<<db, 256, 0, st>>>(gdog, R.slot(S_DOG), R.N, R.acc + 6)));
+    double h[8];
+    HDOG_CUDA_TRY(cudaMemcpyAsync(h, R.acc, sizeof(h), cudaMemcpyDeviceToHost, st));
+    HDOG_CUDA_TRY(cudaStreamSynchronize(st));
+    float gs[6];
+    for (int k = 0; k < 6; k++) {
+      double v = (k < 3 ? nrm : -nrm) * h[k];
+      if (k < 3) v += (double)p->gamma / s[k] * h[6];   // d normalizer / d sigma = gamma normalizer / sigma
+      gs[k] = (float)v;
+    }
+    HDOG_CUDA_TRY(cudaMemcpyAsync(grad_sigma, gs, sizeof(gs), cudaMemcpyHostToDevice, st));
+    HDOG_CUDA_TRY(cudaStreamSynchronize(st));
+  }
+  if (grad_vol) {
+    // g_norm = normalizer (G1 - G2)^T gdog = normalizer (G1 gdog - G2 gdog)
+    conv3(R, gdog, R.slot(S_T3), gauss_taps_f(s[0], false), gauss_taps_f(s[1], false), gauss_taps_f(s[2], false),
+          R.slot(S_T1), R.slot(S_T2));
+    conv3(R, gdog, R.slot(S_GA), gauss_taps_f(s[3], false), gauss_taps_f(s[4], false), gauss_taps_f(s[5], false),
+          R.slot(S_T1), R.slot(S_T2));
+    KLAUNCH("k_soft_diff", st, (k_soft_diff<<<nb, 256, 0, st>>>(R.slot(S_T3), R.slot(S_GA), R.slot(S_GB), nrm, R.N)));
+    // quotient rule: direct term into grad_vol, g_e -> S_T1, g_d -> S_T2
+    KLAUNCH("k_soft_norm_adj", st, (k_soft_norm_adj<<<nb, 256, 0, st>>>(vol, R.slot(S_E), R.slot(S_D), R.slot(S_GB),
+                                                                       grad_vol, R.slot(S_T1), R.slot(S_T2),
+                                                                       p->min_intensity, R.N)));
+    const int rr[3] = {p->radius_norm_xy, p->radius_norm_xy, p->radius_norm_z};
+    // min side then max side: box means transposed z -> y -> x, then the min / max filters
+    // transposed z -> y -> x, each scattering into a zeroed buffer
+    for (int side = 0; side < 2; side++) {
+      float *g = R.slot(side == 0 ? S_T1 : S_T2);
+      float *ping = R.slot(S_GA), *pong = R.slot(S_GC);
+      const float *cur = g;
+      for (int a = 2; a >= 0; a--) {
+        float *dst = (cur == ping) ? pong : ping;
+        if (rr[a] == 0) continue;
+        KLAUNCH("k_soft_box_adj", st, (k_soft_box_adj<<<nb, 256, 0, st>>>(cur, dst, R.g, a, rr[a], R.N)));
+        cur = dst;
+      }
+      // filter inputs of the forward passes x, y, z: vol, *1, *2
+      const float *fin[3] = {vol, R.slot(side == 0 ? S_MN1 : S_MX1), R.slot(side == 0 ? S_MN2 : S_MX2)};
+      for (int a = 2; a >= 0; a--) {
+        if (rr[a] == 0) continue;
+        float *dst = (cur == ping) ? pong : ping;
+        if (dst == g) dst = R.slot(S_GB);
+        cudaMemsetAsync(dst, 0, R.N * sizeof(float), st);
+        KLAUNCH("k_soft_minmax_adj", st, (k_soft_minmax_adj<<<nb, 256, 0, st>>>(fin[a], cur, dst, R.g, a, rr[a],
+                                                                               side, R.N)));
+        cur = dst;
+      }
+      KLAUNCH("k_soft_add", st, (k_soft_add<<<nb, 256, 0, st>>>(grad_vol, cur, R.N)));
+    }
+  }
+  HDOG_CUDA_TRY(cudaGetLastError());
+  return HDOG_OK;
+}
+
+}  // namespace hdog

@@ -101,6 +101,13 @@ class hdog_stack_in(ctypes.Structure):
     _fields_ = [("data", ctypes.c_void_p), ("on_device", ctypes.c_int), ("length", ctypes.c_int)]
 
 
+class hdog_soft_params(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_int), ("height", ctypes.c_int), ("depth", ctypes.c_int),
+                ("radius_norm_xy", ctypes.c_int), ("radius_norm_z", ctypes.c_int),
+                ("min_intensity", ctypes.c_float), ("sigma", ctypes.c_float * 6), ("gamma", ctypes.c_float),
+                ("tau", ctypes.c_float)]
+
+
 _SIGNATURES = {
     "hdog_last_error": (ctypes.c_char_p, []),
     "hdog_abi_version": (ctypes.c_int, []),
@@ -132,6 +139,11 @@ _SIGNATURES = {
     "hdog_records_to_global": (ctypes.c_int, [_P, ctypes.c_int64, ctypes.POINTER(hdog_global_params), _P, _P]),
     "hdog_scale_merge": (ctypes.c_int, [_P, ctypes.c_int64, ctypes.POINTER(hdog_scalemerge_params), _P, _P]),
     "hdog_classifier_features": (ctypes.c_int, [_P, ctypes.c_int64, ctypes.POINTER(hdog_clf_params), _P, _P]),
+    "hdog_soft_workspace_bytes": (ctypes.c_size_t, [ctypes.POINTER(hdog_soft_params)]),
+    "hdog_soft_forward": (ctypes.c_int, [ctypes.POINTER(hdog_soft_params), _P, _P, ctypes.c_int, _P, ctypes.c_int,
+                                         _P, _P, _P, _P]),
+    "hdog_soft_backward": (ctypes.c_int, [ctypes.POINTER(hdog_soft_params), _P, _P, ctypes.c_int, _P, ctypes.c_int,
+                                          ctypes.c_float, _P, _P, _P, _P]),
     "hdog_memcpy": (ctypes.c_int, [_P, _P, ctypes.c_size_t, _P]),
     "hdog_stream_sync": (ctypes.c_int, [_P]),
     "hdog_device_alloc": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.c_size_t]),
@@ -464,3 +476,4 @@ def _buffer(a):
 
 from . import synth  # noqa: E402,F401
 from .postprocess import records_to_global, scale_merge, classifier_features  # noqa: E402,F401
+from . import soft  # noqa: E402,F401
