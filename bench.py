@@ -372,6 +372,64 @@ def stream_workload(args):
     return 0
 
 
+SOFT = ("differentiable chain: 4 volumes uint16 128x512x512 (cast to float32), 3200 nuclei each; loss = mean "
+        "relaxed mask score at 2000 nucleus centroids (jittered +-0.5 voxel) - mean at 2000 random voxels; "
+        "gradients w.r.t. the 6 DoG sigmas and the input volume; radius_norm (20,5), tau 0.02")
+
+
+def soft_workload(args):
+    """Forward + hand-written backward of the differentiable chain on four volumes; a step
+    is one loss and both gradients for every volume."""
+    import torch
+    import hdog
+    from hdog import synth
+    torch.cuda.set_device(0)
+    rng = np.random.default_rng(synth.SEED_BASE + 3)
+    d, h, w = 128, 512, 512
+    cases = []
+    for i in range(4):
+        spec = synth.spec(w, h, d, 3200, synth.SEED_BASE + 300 + i)
+        nuc = synth.nuclei(spec)
+        vol = torch.from_numpy(synth.volume(spec, nuc=nuc).astype(np.float32)).cuda()
+        c = nuc[rng.choice(len(nuc), 2000, replace=len(nuc) < 2000)][:, [2, 1, 0]] + rng.uniform(-0.5, 0.5, (2000, 3))
+        lim = np.array([d - 1, h - 1, w - 1])
+        pos = np.clip(np.rint(c), 0, lim).astype(np.int32)
+        neg = np.stack([rng.integers(0, d, 2000), rng.integers(0, h, 2000), rng.integers(0, w, 2000)], 1).astype(np.int32)
+        cases.append((vol, torch.from_numpy(pos).cuda(), torch.from_numpy(neg).cuda()))
+    sig0 = [2.0, 2.0, 1.5, 3.2, 3.2, 2.4]
+    kw = dict(radius_norm_xy=20, radius_norm_z=5, min_intensity=50.0, tau=0.02)
+
+    def step():
+        out = []
+        for vol, pos, neg in cases:
+            v = vol.clone().requires_grad_(True)
+            s = torch.tensor(sig0, dtype=torch.float32, requires_grad=True)
+            loss = hdog.soft.soft_loss(v, s, pos, neg, **kw)
+            loss.backward()
+            out.append((float(loss.detach()), s.grad.tolist(), float(v.grad.abs().max())))
+        return out
+
+    for _ in range(max(1, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        res = step()
+    torch.cuda.synchronize()
+    ms = (time.perf_counter() - t) * 1e3 / args.steps
+    vox = 4 * d * h * w
+    line = {"metric": METRIC, "value": vox / (ms * 1e-3) / 1e9, "unit": "Gvox/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": SOFT, "voxels_per_step": vox, "sigma": sig0,
+                       "mode": "forward + backward (recomputed intermediates) per volume"},
+            "volumes": [{"loss": r[0], "grad_sigma": r[1], "max_abs_grad_volume": r[2]} for r in res],
+            "checks": "gradients checked against an FP64 reference and FP64 central differences in tests/test_soft.py "
+                      "(14x40x44 volumes); not at this size"}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -379,9 +437,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="camera", choices=["camera", "uneven", "stream"],
+    ap.add_argument("--workload", default="camera", choices=["camera", "uneven", "stream", "soft"],
                     help="camera: the 2560x2160x128 stack (default); uneven: the 40-stack mix; "
-                         "stream: the 17 GB stack from host memory")
+                         "stream: the 17 GB stack from host memory; soft: the differentiable chain")
     ap.add_argument("--profile-case", action="store_true",
                     help="run one 1280x1080x32 substack twice (the small case the ncu summaries capture)")
     args = ap.parse_args()
@@ -393,6 +451,8 @@ def main():
         return uneven_workload(args)
     if args.workload == "stream":
         return stream_workload(args)
+    if args.workload == "soft":
+        return soft_workload(args)
 
     import torch
     import hdog
