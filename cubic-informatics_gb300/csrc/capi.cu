@@ -538,7 +538,8 @@ static void enqueue_after_norm(hdog_ctx *c, int nsub, bool fused, cudaStream_t s
     launch_hessian_pd(c->d_subs, nsub, c->W, c->H, c->D, c->dog, c->mask, nullptr, st);
   }
   launch_ccl(c->d_subs, nsub, c->W, c->H, c->D, c->nvox, c->mask, c->labels, c->edges, c->edge_count, c->root_bits,
-             c->blk_counts, c->status, c->num_sms, st);
+             c->blk_counts, c->status, c->num_sms, st, fused ? c->fg : nullptr, fused ? c->fg_count : nullptr,
+             c->fg_cap, c->nblk);
   int32_t *rank = reinterpret_cast<int32_t *>(c->fa);
   if (fused)
     launch_regions_fg(c->d_subs, nsub, c->nvox, c->fg_cap, vseg_of(c), c->labels, c->root_bits, c->fg, c->fg_count, rank,

@@ -635,10 +635,52 @@ __global__ void __launch_bounds__(256) k_ccl_flatten(const Sub *subs, uint8_t *m
   }
 }
 
+// The same pass over the fused sweep's foreground list instead of the whole volume (the list
+// holds every foreground voxel but voxel 0): root bits and block counts start at zero and
+// each root sets its own bit and counts itself.  A substack whose list overflowed is
+// skipped; its batch is redone with the separate passes.
+constexpr int kFlatFgPerThread = 8;
+
+__global__ void __launch_bounds__(256) k_ccl_flatten_fg(const Sub *subs, const FgEntry *fg,
+                                                       const unsigned long long *fg_count, int32_t *labels,
+                                                       uint32_t *root_bits, uint32_t *blk_counts, int *status) {
+  const Sub S = subs[blockIdx.y];
+  const int64_t cnt = (int64_t)fg_count[blockIdx.y];
+  if (cnt > S.fg_cap) return;
+  const int64_t n = (int64_t)S.W * S.H * S.D;
+  int32_t *L = labels + S.vox;
+  const int32_t *ent = reinterpret_cast<const int32_t *>(fg + S.fg);   // idx is each entry's first word
+  constexpr int kWords = (int)(sizeof(FgEntry) / sizeof(int32_t));
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x * kFlatFgPerThread;
+  for (int64_t e0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * kFlatFgPerThread; e0 < cnt; e0 += stride) {
+    // level by level: the entries' voxels, their labels, the labels' parents
+    int32_t idx[kFlatFgPerThread], l[kFlatFgPerThread], p[kFlatFgPerThread];
+#pragma unroll
+    for (int k = 0; k < kFlatFgPerThread; k++) idx[k] = e0 + k < cnt ? __ldg(ent + (e0 + k) * kWords) : -1;
+#pragma unroll
+    for (int k = 0; k < kFlatFgPerThread; k++) l[k] = idx[k] >= 0 ? __ldcg(L + idx[k]) : -1;
+#pragma unroll
+    for (int k = 0; k < kFlatFgPerThread; k++) p[k] = l[k] >= 0 ? __ldcg(L + l[k]) : -1;
+#pragma unroll
+    for (int k = 0; k < kFlatFgPerThread; k++) {
+      if (l[k] < 0) continue;
+      const int32_t r = p[k] == l[k] ? l[k] : uf_root(L, p[k], n, status);
+      if (r != l[k]) L[idx[k]] = r;
+      if (r == idx[k]) {
+        const int64_t b = idx[k] / kScanBlock;
+        const int o = (int)(idx[k] % kScanBlock);
+        atomicOr(root_bits + (S.blk + b) * (kScanBlock / 32) + o / 32, 1u << (o % 32));
+        atomicAdd(blk_counts + S.blk + b, 1u);
+      }
+    }
+  }
+}
+
 // ------------------------------------------------------------------ launchers
 void launch_ccl(const Sub *d_subs, int nsub, int max_w, int max_h, int max_d, int64_t max_n, const uint8_t *mask,
                 int32_t *labels, int2 *edges, unsigned long long *edge_count, uint32_t *root_bits,
-                uint32_t *blk_counts, int *d_status, int num_sms, cudaStream_t s) {
+                uint32_t *blk_counts, int *d_status, int num_sms, cudaStream_t s, const FgEntry *fg,
+                const unsigned long long *fg_count, int64_t max_fg, int64_t nblk) {
   const int64_t tiles = (int64_t)ceil_div(max_w, kTX) * ceil_div(max_h, kTY) * ceil_div(max_d, kTZ);
   cudaMemsetAsync(edge_count, 0, nsub * sizeof(unsigned long long), s);
   KLAUNCH("k_ccl_local", s, (k_ccl_local<<<dim3((unsigned)tiles, nsub), kCclThreads, 0, s>>>(
@@ -648,8 +690,17 @@ void launch_ccl(const Sub *d_subs, int nsub, int max_w, int max_h, int max_d, in
                                                                         d_status)));
   KLAUNCH("k_ccl_cross_direct", s, (k_ccl_cross_direct<<<dim3((unsigned)tiles, nsub), kCclThreads, 0, s>>>(
                                        d_subs, mask, edge_count, labels, d_status)));
-  KLAUNCH("k_ccl_flatten", s, (k_ccl_flatten<false><<<dim3(ceil_div(max_n, kScanBlock), nsub), 256, 0, s>>>(
-                                  d_subs, const_cast<uint8_t *>(mask), labels, root_bits, blk_counts, d_status)));
+  if (fg) {
+    cudaMemsetAsync(root_bits, 0, (size_t)nsub * nblk * (kScanBlock / 32) * sizeof(uint32_t), s);
+    cudaMemsetAsync(blk_counts, 0, (size_t)nsub * nblk * sizeof(uint32_t), s);
+    const int64_t want = std::min((int64_t)ceil_div(max_fg, 256 * kFlatFgPerThread),
+                                  (int64_t)(8 * num_sms / (nsub > 0 ? nsub : 1) + 1));
+    KLAUNCH("k_ccl_flatten", s, (k_ccl_flatten_fg<<<dim3((unsigned)std::max<int64_t>(want, 1), nsub), 256, 0, s>>>(
+                                    d_subs, fg, fg_count, labels, root_bits, blk_counts, d_status)));
+  } else {
+    KLAUNCH("k_ccl_flatten", s, (k_ccl_flatten<false><<<dim3(ceil_div(max_n, kScanBlock), nsub), 256, 0, s>>>(
+                                    d_subs, const_cast<uint8_t *>(mask), labels, root_bits, blk_counts, d_status)));
+  }
 }
 
 void launch_roots_from_labels(const Sub *d_subs, int nsub, int64_t max_n, const int32_t *labels, uint8_t *mask,

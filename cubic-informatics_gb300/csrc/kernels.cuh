@@ -113,7 +113,8 @@ void launch_scan(const ScanSeg &sg, int nsub, const uint32_t *in, uint32_t *out,
                  int64_t *totals, int64_t add, cudaStream_t s);
 void launch_ccl(const Sub *d_subs, int nsub, int max_w, int max_h, int max_d, int64_t max_n, const uint8_t *mask,
                 int32_t *labels, int2 *edges, unsigned long long *edge_count, uint32_t *root_bits,
-                uint32_t *blk_counts, int *d_status, int num_sms, cudaStream_t s);
+                uint32_t *blk_counts, int *d_status, int num_sms, cudaStream_t s, const FgEntry *fg = nullptr,
+                const unsigned long long *fg_count = nullptr, int64_t max_fg = 0, int64_t nblk = 0);
 // Foreground mask (label != 0), root bitmap and per-block root counts from labels alone.
 void launch_roots_from_labels(const Sub *d_subs, int nsub, int64_t max_n, const int32_t *labels, uint8_t *mask,
                               uint32_t *root_bits, uint32_t *blk_counts, cudaStream_t s);
