@@ -507,8 +507,8 @@ static void enqueue_normalize(hdog_ctx *c, int nsub, float *out_norm, cudaStream
   if (p.radius_norm_xy == 0 || p.radius_norm_z == 0) {
     launch_copy_norm(c->d_subs, nsub, c->nvox, (float)p.min_intensity, out_norm, st);
     if (ero_l) {   // no box means on the copy path: zero planes
-      cudaMemsetAsync(ero_l, 0, (size_t)nsub * c->nvox * sizeof(float), st);
-      cudaMemsetAsync(dil_l, 0, (size_t)nsub * c->nvox * sizeof(float), st);
+      zero_async(ero_l, (size_t)nsub * c->nvox * sizeof(float), st);
+      zero_async(dil_l, (size_t)nsub * c->nvox * sizeof(float), st);
     }
     return;
   }
@@ -549,7 +549,7 @@ static void enqueue_after_norm(hdog_ctx *c, int nsub, bool fused, cudaStream_t s
     launch_regions(c->d_subs, nsub, c->nvox, vseg_of(c), c->mask, c->labels, c->root_bits, c->norm, c->dog, rank,
                    c->blk_counts, c->blk_offsets, c->chunk, c->num_regions, c->acc, c->slots, c->status, st);
   launch_finalize(c->d_subs, nsub, c->reg_cap, rseg_of(c), c->num_regions, c->acc, c->slots, c->out, filter_of(c->p),
-                  c->blk_counts, c->blk_offsets, c->chunk, c->num_records, c->records, st);
+                  c->blk_counts, c->blk_offsets, c->chunk, c->num_records, c->records, c->nblk, st);
 }
 
 static bool fused_ok(hdog_ctx *c) { return c->use_sweep && sweep_supported(c->taps, c->W, c->max_smem); }
@@ -573,7 +573,7 @@ static int readback(hdog_ctx *c, int nsub, cudaStream_t st) {
 // counts, region counts and the status word in c->h_counts after a stream sync.
 static int run_batch(hdog_ctx *c, int nsub, cudaStream_t st) {
   TRY(upload_subs(c, nsub, st));
-  HDOG_CUDA_TRY(cudaMemsetAsync(c->status, 0, sizeof(int), st));
+  zero_async(c->status, sizeof(int), st);
   if (c->p.erosion_radius_xy > 0 || c->p.erosion_radius_z > 0) {
     // opt-in regional erosion of the input (the reference compiles Erosion3DFilter but
     // never calls it); the eroded substacks replace the inputs in c->img
@@ -587,7 +587,7 @@ static int run_batch(hdog_ctx *c, int nsub, cudaStream_t st) {
   }
   enqueue_normalize(c, nsub, c->norm, st);
   const bool fused = fused_ok(c);
-  if (fused) HDOG_CUDA_TRY(cudaMemsetAsync(c->fg_count, 0, nsub * sizeof(unsigned long long), st));
+  if (fused) zero_async(c->fg_count, nsub * sizeof(unsigned long long), st);
   enqueue_after_norm(c, nsub, fused, st);
   TRY(readback(c, nsub, st));
   if (fused) {
@@ -595,7 +595,7 @@ static int run_batch(hdog_ctx *c, int nsub, cudaStream_t st) {
     for (int s = 0; s < nsub; s++) over |= c->h_counts[2 * c->max_sub + s] > c->fg_cap;
     if (over) {
       // more foreground than the list holds: redo this batch with the separate passes
-      HDOG_CUDA_TRY(cudaMemsetAsync(c->status, 0, sizeof(int), st));
+      zero_async(c->status, sizeof(int), st);
       enqueue_after_norm(c, nsub, false, st);
       TRY(readback(c, nsub, st));
     }
@@ -685,7 +685,7 @@ extern "C" int hdog_ccl(hdog_ctx *c, const uint8_t *d_mask, int32_t *d_labels, v
   if (!d_mask || !d_labels) return fail(HDOG_ERR_ARG, "hdog_ccl: null buffer");
   cudaStream_t st = (cudaStream_t)stream;
   TRY(single_sub(c, nullptr, st));
-  HDOG_CUDA_TRY(cudaMemsetAsync(c->status, 0, sizeof(int), st));
+  zero_async(c->status, sizeof(int), st);
   launch_ccl(c->d_subs, 1, c->W, c->H, c->D, c->nvox, d_mask, d_labels, c->edges, c->edge_count, c->root_bits,
              c->blk_counts, c->status, c->num_sms, st);
   HDOG_CUDA_TRY(cudaGetLastError());
@@ -702,14 +702,14 @@ extern "C" int hdog_regional_features(hdog_ctx *c, const int32_t *d_labels, cons
   if (!d_labels || !d_norm || !d_dog || !out) return fail(HDOG_ERR_ARG, "hdog_regional_features: null argument");
   cudaStream_t st = (cudaStream_t)stream;
   TRY(single_sub(c, nullptr, st));
-  HDOG_CUDA_TRY(cudaMemsetAsync(c->status, 0, sizeof(int), st));
+  zero_async(c->status, sizeof(int), st);
   // foreground = nonzero label; roots = voxels labelled with their own index
   launch_roots_from_labels(c->d_subs, 1, c->nvox, d_labels, c->mask, c->root_bits, c->blk_counts, st);
   int32_t *rank = reinterpret_cast<int32_t *>(c->fa);
   launch_regions(c->d_subs, 1, c->nvox, vseg_of(c), c->mask, d_labels, c->root_bits, d_norm, d_dog, rank,
                  c->blk_counts, c->blk_offsets, c->chunk, c->num_regions, c->acc, c->slots, c->status, st);
   launch_finalize(c->d_subs, 1, c->reg_cap, rseg_of(c), c->num_regions, c->acc, c->slots, c->out,
-                  filter_of(c->p, true), c->blk_counts, c->blk_offsets, c->chunk, c->num_records, c->records, st);
+                  filter_of(c->p, true), c->blk_counts, c->blk_offsets, c->chunk, c->num_records, c->records, c->nblk, st);
   HDOG_CUDA_TRY(cudaGetLastError());
   int64_t nr = 0;
   int status = 0;

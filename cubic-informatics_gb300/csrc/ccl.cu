@@ -682,7 +682,7 @@ void launch_ccl(const Sub *d_subs, int nsub, int max_w, int max_h, int max_d, in
                 uint32_t *blk_counts, int *d_status, int num_sms, cudaStream_t s, const FgEntry *fg,
                 const unsigned long long *fg_count, int64_t max_fg, int64_t nblk) {
   const int64_t tiles = (int64_t)ceil_div(max_w, kTX) * ceil_div(max_h, kTY) * ceil_div(max_d, kTZ);
-  cudaMemsetAsync(edge_count, 0, nsub * sizeof(unsigned long long), s);
+  zero_async(edge_count, nsub * sizeof(unsigned long long), s);
   KLAUNCH("k_ccl_local", s, (k_ccl_local<<<dim3((unsigned)tiles, nsub), kCclThreads, 0, s>>>(
                                 d_subs, mask, labels, edges, edge_count)));
   const unsigned eb = (unsigned)max(1, (8 * num_sms + nsub - 1) / nsub);
@@ -691,8 +691,8 @@ void launch_ccl(const Sub *d_subs, int nsub, int max_w, int max_h, int max_d, in
   KLAUNCH("k_ccl_cross_direct", s, (k_ccl_cross_direct<<<dim3((unsigned)tiles, nsub), kCclThreads, 0, s>>>(
                                        d_subs, mask, edge_count, labels, d_status)));
   if (fg) {
-    cudaMemsetAsync(root_bits, 0, (size_t)nsub * nblk * (kScanBlock / 32) * sizeof(uint32_t), s);
-    cudaMemsetAsync(blk_counts, 0, (size_t)nsub * nblk * sizeof(uint32_t), s);
+    zero_async(root_bits, (size_t)nsub * nblk * (kScanBlock / 32) * sizeof(uint32_t), s);
+    zero_async(blk_counts, (size_t)nsub * nblk * sizeof(uint32_t), s);
     const int64_t want = std::min((int64_t)ceil_div(max_fg, 256 * kFlatFgPerThread),
                                   (int64_t)(8 * num_sms / (nsub > 0 ? nsub : 1) + 1));
     KLAUNCH("k_ccl_flatten", s, (k_ccl_flatten_fg<<<dim3((unsigned)std::max<int64_t>(want, 1), nsub), 256, 0, s>>>(

@@ -95,6 +95,9 @@ int soft_forward(const hdog_soft_params *p, const float *vol, const int32_t *pos
 int soft_backward(const hdog_soft_params *p, const float *vol, const int32_t *pos, int n_pos, const int32_t *neg,
                   int n_neg, float grad_loss, float *grad_vol, float *grad_sigma, void *work, cudaStream_t st);
 
+// Zero `bytes` (a multiple of 4) of device memory on stream s with a kernel.
+void zero_async(void *p, size_t bytes, cudaStream_t s);
+
 bool launch_dog_sweep(const Sub *d_subs, int nsub, int W, int H, int D, const DogTaps &T, const float *norm,
                       float *dog, int *d_status, int max_smem, cudaStream_t s);
 // DoG + Hessian + PD: the radius-specialised pair (norm -> dog -> mask + list) when the tap
@@ -131,7 +134,7 @@ void launch_regions_fg(const Sub *d_subs, int nsub, int64_t max_n, int64_t max_f
 void launch_finalize(const Sub *d_subs, int nsub, int64_t max_reg_cap, const ScanSeg &rseg,
                      const int64_t *d_num_regions, RegionAcc acc, int64_t slots, RegionOut out,
                      FilterParams fp, uint32_t *blk_counts, uint32_t *blk_offsets, uint32_t *chunk,
-                     int64_t *d_num_records, hdog_record *records, cudaStream_t s);
+                     int64_t *d_num_records, hdog_record *records, int64_t blk_stride, cudaStream_t s);
 
 constexpr int kMaxRadiusXY = 421;    // shared-memory bound of the min/max x and y passes
 constexpr int kScanBlock = 4096;     // voxels per block in the region scans (16 per thread)

@@ -108,24 +108,32 @@ __device__ __forceinline__ void init_slot(RegionAcc acc, int64_t slots, int64_t 
 }
 
 // 4096 voxels per block, 16 per thread; the thread's root bits are one half-word.
-__global__ void __launch_bounds__(256) k_rank(const Sub *subs, const uint32_t *root_bits, const uint32_t *blk_offsets,
-                                              int32_t *rank, RegionAcc acc, int64_t slots, int *status) {
+// One block of kRankThreads threads per kScanBlock voxels, 64 voxels (two root-bit words)
+// per thread: roots numbered in voxel order after the block's offset.
+constexpr int kRankThreads = kScanBlock / 64;
+
+__global__ void __launch_bounds__(kRankThreads) k_rank(const Sub *subs, const uint32_t *root_bits,
+                                                       const uint32_t *blk_offsets, int32_t *rank, RegionAcc acc,
+                                                       int64_t slots, int *status) {
   const Sub S = subs[blockIdx.y];
   const int64_t n = (int64_t)S.W * S.H * S.D;
   const int64_t base = (int64_t)blockIdx.x * kScanBlock;
   if (base >= n) return;
-  const uint32_t word = root_bits[(S.blk + blockIdx.x) * (kScanBlock / 32) + threadIdx.x / 2];
-  const uint32_t bits = (threadIdx.x & 1) ? (word >> 16) : (word & 0xFFFFu);
-  const uint32_t pre = block_excl_scan(__popc(bits), nullptr);
+  const uint2 w = reinterpret_cast<const uint2 *>(root_bits + (S.blk + blockIdx.x) * (kScanBlock / 32))[threadIdx.x];
+  const uint32_t pre = block_excl_scan(__popc(w.x) + __popc(w.y), nullptr);
   if (blockIdx.x == 0 && threadIdx.x == 0) init_slot(acc, slots, S.reg, 0);
   int64_t r = 1 + (int64_t)blk_offsets[S.blk + blockIdx.x] + pre;
-  for (int k = 0; k < 16; k++) {
-    if (!((bits >> k) & 1u)) continue;
-    if (r >= S.reg_cap) { atomicExch(status, HDOG_ERR_CAPACITY); return; }
-    const int64_t i = base + threadIdx.x * 16 + k;
-    rank[S.vox + i] = (int32_t)r;
-    init_slot(acc, slots, S.reg + r, (int32_t)i);
-    r++;
+  for (int half = 0; half < 2; half++) {
+    uint32_t bits = half ? w.y : w.x;
+    while (bits) {
+      const int k = __ffs(bits) - 1;
+      bits &= bits - 1;
+      if (r >= S.reg_cap) { atomicExch(status, HDOG_ERR_CAPACITY); return; }
+      const int64_t i = base + threadIdx.x * 64 + half * 32 + k;
+      rank[S.vox + i] = (int32_t)r;
+      init_slot(acc, slots, S.reg + r, (int32_t)i);
+      r++;
+    }
   }
 }
 
@@ -304,10 +312,11 @@ __global__ void __launch_bounds__(kFinalizeBlock) k_finalize(const Sub *subs, co
                                                             RegionAcc acc, int64_t slots, RegionOut out,
                                                             FilterParams fp, uint32_t *blk_counts) {
   const Sub S = subs[blockIdx.y];
-  const int64_t nblk = (S.reg_cap + kFinalizeBlock - 1) / kFinalizeBlock;
-  if ((int64_t)blockIdx.x >= nblk) return;
-  const int64_t R = num_regions[blockIdx.y];
-  const int64_t r = (int64_t)blockIdx.x * kFinalizeBlock + threadIdx.x;
+  const int64_t R = min(num_regions[blockIdx.y], S.reg_cap);
+  __shared__ uint32_t wc[kFinalizeBlock / 32];
+  // only the blocks that hold regions (the counts of the others were zeroed)
+  for (int64_t blk = blockIdx.x; blk * kFinalizeBlock < R; blk += gridDim.x) {
+  const int64_t r = blk * kFinalizeBlock + threadIdx.x;
   bool keep = false;
   if (r < R) {
     const int64_t g = S.reg + r;
@@ -340,13 +349,14 @@ __global__ void __launch_bounds__(kFinalizeBlock) k_finalize(const Sub *subs, co
     out.keep[g] = keep ? 1 : 0;
   }
   const uint32_t b = __ballot_sync(0xFFFFFFFFu, keep);
-  __shared__ uint32_t wc[kFinalizeBlock / 32];
   if ((threadIdx.x & 31) == 0) wc[threadIdx.x >> 5] = __popc(b);
   __syncthreads();
   if (threadIdx.x == 0) {
     uint32_t t = 0;
     for (int k = 0; k < kFinalizeBlock / 32; k++) t += wc[k];
-    blk_counts[S.blk + blockIdx.x] = t;
+    blk_counts[S.blk + blk] = t;
+  }
+  __syncthreads();   // wc is rewritten by the next block
   }
 }
 
@@ -356,15 +366,14 @@ __global__ void __launch_bounds__(kFinalizeBlock) k_records(const Sub *subs, con
                                                            int64_t slots, const uint32_t *blk_offsets,
                                                            hdog_record *rec) {
   const Sub S = subs[blockIdx.y];
-  const int64_t nblk = (S.reg_cap + kFinalizeBlock - 1) / kFinalizeBlock;
-  if ((int64_t)blockIdx.x >= nblk) return;
-  const int64_t R = num_regions[blockIdx.y];
-  const int64_t r = (int64_t)blockIdx.x * kFinalizeBlock + threadIdx.x;
+  const int64_t R = min(num_regions[blockIdx.y], S.reg_cap);
+  __shared__ uint32_t wp[kFinalizeBlock / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int64_t blk = blockIdx.x; blk * kFinalizeBlock < R; blk += gridDim.x) {
+  const int64_t r = blk * kFinalizeBlock + threadIdx.x;
   const int64_t g = S.reg + r;
   const bool keep = r < R && out.keep[g];
   const uint32_t b = __ballot_sync(0xFFFFFFFFu, keep);
-  __shared__ uint32_t wp[kFinalizeBlock / 32];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   if (lane == 0) wp[w] = __popc(b);
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -372,8 +381,8 @@ __global__ void __launch_bounds__(kFinalizeBlock) k_records(const Sub *subs, con
     for (int k = 0; k < kFinalizeBlock / 32; k++) { const uint32_t c = wp[k]; wp[k] = t; t += c; }
   }
   __syncthreads();
-  if (!keep) return;
-  const int64_t o = S.reg + blk_offsets[S.blk + blockIdx.x] + wp[w] + __popc(b & ((1u << lane) - 1u));
+  if (keep) {
+  const int64_t o = S.reg + blk_offsets[S.blk + blk] + wp[w] + __popc(b & ((1u << lane) - 1u));
   hdog_record q;
   q.centroid_x = out.centroid[g];
   q.centroid_y = out.centroid[slots + g];
@@ -384,8 +393,26 @@ __global__ void __launch_bounds__(kFinalizeBlock) k_records(const Sub *subs, con
   q.size = (uint16_t)(count[g] & 0xFFFFu);
   q.padding = 0;
   rec[o] = q;
+  }
+  __syncthreads();   // wp is rewritten by the next block
+  }
 }
 
+
+// ------------------------------------------------------------------ zero fill
+// Clearing by a kernel rather than cudaMemsetAsync: a memset can go to a copy engine, where
+// it would queue behind the chunks of a host stack being copied on the copy stream.
+__global__ void k_zero32(uint32_t *p, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    p[i] = 0u;
+}
+
+void zero_async(void *p, size_t bytes, cudaStream_t s) {
+  const int64_t n = (int64_t)(bytes / 4);
+  if (n > 0)
+    KLAUNCH("k_zero32", s, (k_zero32<<<(unsigned)std::min<int64_t>(ceil_div(n, 256), 4096), 256, 0, s>>>(
+                               static_cast<uint32_t *>(p), n)));
+}
 
 // ------------------------------------------------------------------ launchers
 void launch_scan(const ScanSeg &sg, int nsub, const uint32_t *in, uint32_t *out, uint32_t *chunk,
@@ -401,7 +428,7 @@ void launch_regions(const Sub *d_subs, int nsub, int64_t max_n, const ScanSeg &v
                     int32_t *rank, uint32_t *blk_counts, uint32_t *blk_offsets, uint32_t *chunk,
                     int64_t *d_num_regions, RegionAcc acc, int64_t slots, int *d_status, cudaStream_t s) {
   launch_scan(vseg, nsub, blk_counts, blk_offsets, chunk, d_num_regions, 1, s);
-  KLAUNCH("k_rank", s, (k_rank<<<dim3(ceil_div(max_n, kScanBlock), nsub), 256, 0, s>>>(d_subs, root_bits, blk_offsets, rank,
+  KLAUNCH("k_rank", s, (k_rank<<<dim3(ceil_div(max_n, kScanBlock), nsub), kRankThreads, 0, s>>>(d_subs, root_bits, blk_offsets, rank,
                                                                         acc, slots, d_status)));
   KLAUNCH("k_accumulate", s, (k_accumulate<<<dim3(ceil_div(max_n, kScanBlock), nsub), 256, 0, s>>>(d_subs, mask, labels, rank, norm, dog, acc,
                                                                 slots)));
@@ -413,7 +440,7 @@ void launch_regions_fg(const Sub *d_subs, int nsub, int64_t max_n, int64_t max_f
                        uint32_t *blk_offsets, uint32_t *chunk, int64_t *d_num_regions, RegionAcc acc, int64_t slots,
                        int *d_status, int num_sms, cudaStream_t s) {
   launch_scan(vseg, nsub, blk_counts, blk_offsets, chunk, d_num_regions, 1, s);
-  KLAUNCH("k_rank", s, (k_rank<<<dim3(ceil_div(max_n, kScanBlock), nsub), 256, 0, s>>>(d_subs, root_bits, blk_offsets,
+  KLAUNCH("k_rank", s, (k_rank<<<dim3(ceil_div(max_n, kScanBlock), nsub), kRankThreads, 0, s>>>(d_subs, root_bits, blk_offsets,
                                                                                       rank, acc, slots, d_status)));
   int64_t want = (int64_t)ceil_div(max_fg, 256 * kFgChunk);
   const int64_t cap = (int64_t)8 * num_sms / (nsub > 0 ? nsub : 1) + 1;
@@ -427,11 +454,15 @@ void launch_regions_fg(const Sub *d_subs, int nsub, int64_t max_n, int64_t max_f
 void launch_finalize(const Sub *d_subs, int nsub, int64_t max_reg_cap, const ScanSeg &rseg,
                      const int64_t *d_num_regions, RegionAcc acc, int64_t slots, RegionOut out,
                      FilterParams fp, uint32_t *blk_counts, uint32_t *blk_offsets, uint32_t *chunk,
-                     int64_t *d_num_records, hdog_record *records, cudaStream_t s) {
-  const unsigned nb = ceil_div(max_reg_cap, kFinalizeBlock);
-  KLAUNCH("k_finalize", s, (k_finalize<<<dim3(nb, nsub), kFinalizeBlock, 0, s>>>(d_subs, d_num_regions, acc, slots, out, fp, blk_counts)));
+                     int64_t *d_num_records, hdog_record *records, int64_t blk_stride, cudaStream_t s) {
+  // the kernels visit only the blocks that hold regions (the count is on the device): the
+  // other blocks' counts are zero for the record scan
+  const int64_t nb = ceil_div(max_reg_cap, kFinalizeBlock);
+  zero_async(blk_counts, (size_t)((nsub - 1) * blk_stride + nb) * sizeof(uint32_t), s);
+  const unsigned grid = (unsigned)std::min<int64_t>(nb, 2048);
+  KLAUNCH("k_finalize", s, (k_finalize<<<dim3(grid, nsub), kFinalizeBlock, 0, s>>>(d_subs, d_num_regions, acc, slots, out, fp, blk_counts)));
   launch_scan(rseg, nsub, blk_counts, blk_offsets, chunk, d_num_records, 0, s);
-  KLAUNCH("k_records", s, (k_records<<<dim3(nb, nsub), kFinalizeBlock, 0, s>>>(d_subs, d_num_regions, out, acc.count, slots, blk_offsets,
+  KLAUNCH("k_records", s, (k_records<<<dim3(grid, nsub), kFinalizeBlock, 0, s>>>(d_subs, d_num_regions, out, acc.count, slots, blk_offsets,
                                                       records)));
 }
 

@@ -851,7 +851,7 @@ int launch_dog_hess(const Sub *d_subs, int nsub, int W, int H, int D, const DogT
                     float *dog, uint8_t *mask, FgEntry *fg, unsigned long long *fg_count, int *d_status,
                     cudaStream_t s) {
   const int rxy = max(T.r[0], T.r[2]), rz = max(T.r[1], T.r[3]);
-  cudaMemsetAsync(fg_count, 0, nsub * sizeof(unsigned long long), s);
+  zero_async(fg_count, nsub * sizeof(unsigned long long), s);
   const SweepInst *si = find_inst(T);
   if (si) {
     CUtensorMap map_n, map_d, map_t;
