@@ -537,12 +537,15 @@ static void enqueue_after_norm(hdog_ctx *c, int nsub, bool fused, cudaStream_t s
     enqueue_dog(c, nsub, c->norm, c->dog, st);
     launch_hessian_pd(c->d_subs, nsub, c->W, c->H, c->D, c->dog, c->mask, nullptr, st);
   }
+  // each foreground entry's root, per entry beside the list (fb is free after the
+  // normalization)
+  int32_t *fg_root = reinterpret_cast<int32_t *>(c->fb);
   launch_ccl(c->d_subs, nsub, c->W, c->H, c->D, c->nvox, c->mask, c->labels, c->edges, c->edge_count, c->root_bits,
              c->blk_counts, c->status, c->num_sms, st, fused ? c->fg : nullptr, fused ? c->fg_count : nullptr,
-             c->fg_cap, c->nblk);
+             c->fg_cap, c->nblk, fg_root);
   int32_t *rank = reinterpret_cast<int32_t *>(c->fa);
   if (fused)
-    launch_regions_fg(c->d_subs, nsub, c->nvox, c->fg_cap, vseg_of(c), c->labels, c->root_bits, c->fg, c->fg_count, rank,
+    launch_regions_fg(c->d_subs, nsub, c->nvox, c->fg_cap, vseg_of(c), fg_root, c->root_bits, c->fg, c->fg_count, rank,
                       c->blk_counts, c->blk_offsets, c->chunk, c->num_regions, c->acc, c->slots, c->status, c->num_sms,
                       st);
   else

@@ -643,7 +643,8 @@ constexpr int kFlatFgPerThread = 8;
 
 __global__ void __launch_bounds__(256) k_ccl_flatten_fg(const Sub *subs, const FgEntry *fg,
                                                        const unsigned long long *fg_count, int32_t *labels,
-                                                       uint32_t *root_bits, uint32_t *blk_counts, int *status) {
+                                                       uint32_t *root_bits, uint32_t *blk_counts, int32_t *fg_root,
+                                                       int *status) {
   const Sub S = subs[blockIdx.y];
   const int64_t cnt = (int64_t)fg_count[blockIdx.y];
   if (cnt > S.fg_cap) return;
@@ -666,6 +667,7 @@ __global__ void __launch_bounds__(256) k_ccl_flatten_fg(const Sub *subs, const F
       if (l[k] < 0) continue;
       const int32_t r = p[k] == l[k] ? l[k] : uf_root(L, p[k], n, status);
       if (r != l[k]) L[idx[k]] = r;
+      fg_root[S.fg + e0 + k] = r;   // the entry's root, read by the region accumulation
       if (r == idx[k]) {
         const int64_t b = idx[k] / kScanBlock;
         const int o = (int)(idx[k] % kScanBlock);
@@ -680,7 +682,7 @@ __global__ void __launch_bounds__(256) k_ccl_flatten_fg(const Sub *subs, const F
 void launch_ccl(const Sub *d_subs, int nsub, int max_w, int max_h, int max_d, int64_t max_n, const uint8_t *mask,
                 int32_t *labels, int2 *edges, unsigned long long *edge_count, uint32_t *root_bits,
                 uint32_t *blk_counts, int *d_status, int num_sms, cudaStream_t s, const FgEntry *fg,
-                const unsigned long long *fg_count, int64_t max_fg, int64_t nblk) {
+                const unsigned long long *fg_count, int64_t max_fg, int64_t nblk, int32_t *fg_root) {
   const int64_t tiles = (int64_t)ceil_div(max_w, kTX) * ceil_div(max_h, kTY) * ceil_div(max_d, kTZ);
   zero_async(edge_count, nsub * sizeof(unsigned long long), s);
   KLAUNCH("k_ccl_local", s, (k_ccl_local<<<dim3((unsigned)tiles, nsub), kCclThreads, 0, s>>>(
@@ -696,7 +698,7 @@ void launch_ccl(const Sub *d_subs, int nsub, int max_w, int max_h, int max_d, in
     const int64_t want = std::min((int64_t)ceil_div(max_fg, 256 * kFlatFgPerThread),
                                   (int64_t)(8 * num_sms / (nsub > 0 ? nsub : 1) + 1));
     KLAUNCH("k_ccl_flatten", s, (k_ccl_flatten_fg<<<dim3((unsigned)std::max<int64_t>(want, 1), nsub), 256, 0, s>>>(
-                                    d_subs, fg, fg_count, labels, root_bits, blk_counts, d_status)));
+                                    d_subs, fg, fg_count, labels, root_bits, blk_counts, fg_root, d_status)));
   } else {
     KLAUNCH("k_ccl_flatten", s, (k_ccl_flatten<false><<<dim3(ceil_div(max_n, kScanBlock), nsub), 256, 0, s>>>(
                                     d_subs, const_cast<uint8_t *>(mask), labels, root_bits, blk_counts, d_status)));

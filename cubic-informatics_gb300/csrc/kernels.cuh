@@ -117,7 +117,8 @@ void launch_scan(const ScanSeg &sg, int nsub, const uint32_t *in, uint32_t *out,
 void launch_ccl(const Sub *d_subs, int nsub, int max_w, int max_h, int max_d, int64_t max_n, const uint8_t *mask,
                 int32_t *labels, int2 *edges, unsigned long long *edge_count, uint32_t *root_bits,
                 uint32_t *blk_counts, int *d_status, int num_sms, cudaStream_t s, const FgEntry *fg = nullptr,
-                const unsigned long long *fg_count = nullptr, int64_t max_fg = 0, int64_t nblk = 0);
+                const unsigned long long *fg_count = nullptr, int64_t max_fg = 0, int64_t nblk = 0,
+                int32_t *fg_root = nullptr);
 // Foreground mask (label != 0), root bitmap and per-block root counts from labels alone.
 void launch_roots_from_labels(const Sub *d_subs, int nsub, int64_t max_n, const int32_t *labels, uint8_t *mask,
                               uint32_t *root_bits, uint32_t *blk_counts, cudaStream_t s);
@@ -127,7 +128,7 @@ void launch_regions(const Sub *d_subs, int nsub, int64_t max_n, const ScanSeg &v
                     int64_t *d_num_regions, RegionAcc acc, int64_t slots, int *d_status, cudaStream_t s);
 // Accumulation from the fused sweep's foreground list instead of the mask and DoG.
 void launch_regions_fg(const Sub *d_subs, int nsub, int64_t max_n, int64_t max_fg, const ScanSeg &vseg,
-                       const int32_t *labels, const uint32_t *root_bits, const FgEntry *fg,
+                       const int32_t *fg_root, const uint32_t *root_bits, const FgEntry *fg,
                        const unsigned long long *fg_count, int32_t *rank, uint32_t *blk_counts,
                        uint32_t *blk_offsets, uint32_t *chunk, int64_t *d_num_regions, RegionAcc acc, int64_t slots,
                        int *d_status, int num_sms, cudaStream_t s);

@@ -219,7 +219,7 @@ __global__ void __launch_bounds__(256) k_accumulate(const Sub *subs, const uint8
 constexpr int kFgChunk = 8;
 
 __global__ void __launch_bounds__(256, 2) k_accumulate_fg(const Sub *subs, const FgEntry *fg,
-                                                       const unsigned long long *fg_count, const int32_t *labels,
+                                                       const unsigned long long *fg_count, const int32_t *fg_root,
                                                        const int32_t *rank, RegionAcc acc, int64_t slots) {
   const Sub S = subs[blockIdx.y];
   const int64_t cnt = (int64_t)fg_count[blockIdx.y];
@@ -238,7 +238,7 @@ __global__ void __launch_bounds__(256, 2) k_accumulate_fg(const Sub *subs, const
     for (int k = 0; k < kFgChunk; k++)
       if (k < ne) q0[k] = __ldg(src + 2 * k);
 #pragma unroll
-    for (int k = 0; k < kFgChunk; k++) lab[k] = k < ne ? labels[S.vox + __float_as_int(q0[k].x)] : 0;
+    for (int k = 0; k < kFgChunk; k++) lab[k] = k < ne ? __ldg(fg_root + S.fg + e0 + k) : 0;
 #pragma unroll
     for (int k = 0; k < kFgChunk; k++) rk[k] = k < ne ? rank[S.vox + lab[k]] : -1;
     RunAcc a;
@@ -435,7 +435,7 @@ void launch_regions(const Sub *d_subs, int nsub, int64_t max_n, const ScanSeg &v
 }
 
 void launch_regions_fg(const Sub *d_subs, int nsub, int64_t max_n, int64_t max_fg, const ScanSeg &vseg,
-                       const int32_t *labels, const uint32_t *root_bits, const FgEntry *fg,
+                       const int32_t *fg_root, const uint32_t *root_bits, const FgEntry *fg,
                        const unsigned long long *fg_count, int32_t *rank, uint32_t *blk_counts,
                        uint32_t *blk_offsets, uint32_t *chunk, int64_t *d_num_regions, RegionAcc acc, int64_t slots,
                        int *d_status, int num_sms, cudaStream_t s) {
@@ -447,7 +447,7 @@ void launch_regions_fg(const Sub *d_subs, int nsub, int64_t max_n, int64_t max_f
   if (want > cap) want = cap;
   if (want < 1) want = 1;
   const unsigned blocks = (unsigned)want;
-  KLAUNCH("k_accumulate_fg", s, (k_accumulate_fg<<<dim3(blocks, nsub), 256, 0, s>>>(d_subs, fg, fg_count, labels,
+  KLAUNCH("k_accumulate_fg", s, (k_accumulate_fg<<<dim3(blocks, nsub), 256, 0, s>>>(d_subs, fg, fg_count, fg_root,
                                                                                     rank, acc, slots)));
 }
 
