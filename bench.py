@@ -518,7 +518,8 @@ def main():
     # ---- roofline of the dominant kernel (live CUDA-event times from the timed region)
     peak, peak_kind = peaks()
     launches = sum(c for c, _ in ktimes.values())
-    top = max(ktimes.items(), key=lambda kv: kv[1][1])
+    dense = {k: v for k, v in ktimes.items() if k in KERNEL_BYTES_PER_VOXEL} or ktimes
+    top = max(dense.items(), key=lambda kv: kv[1][1])
     kname, (kcount, ktotal) = top
     per_launch_voxels = processed      # one launch covers every substack of the step
     alg = KERNEL_BYTES_PER_VOXEL.get(kname, 0) * per_launch_voxels
