@@ -312,7 +312,7 @@ __global__ void __launch_bounds__(kSweepThreads, 1)
 //
 // The split costs one write and one read of the DoG volume but frees the Hessian stage
 // from the z shift register's registers, so several Hessian blocks share an SM.
-constexpr int kDTX = 64, kDTY = 16;     // DoG tile
+constexpr int kDTX = 32, kDTY = 16;     // DoG tile (two blocks per SM)
 constexpr int kHTX = 64, kHTY = 16;     // Hessian tile
 constexpr int kHPX = kHTX + 8;          // Hessian ring row: columns x0-4 .. x0+67 (16-byte aligned start)
 constexpr int kHPY = kHTY + 4;
@@ -333,7 +333,7 @@ struct DogT {
   static constexpr int XITEMS = BH * XQ;
   static constexpr int OFF = HX - RXY;                        // item q reads from column 4q + OFF
   static constexpr int NV = (OFF + 2 * RXY + 4 + 3) / 4 * 4;  // inputs staged per item
-  static constexpr int NT = kDTX * kDTY / 2;                  // 512: two z columns per thread
+  static constexpr int NT = kDTX * kDTY / 2;                  // 256: two z columns per thread
   static constexpr size_t SMEM = (size_t)2 * IN_FLOATS * 4 + (size_t)2 * BH * kDTX * 8 + 64;
 };
 
@@ -449,7 +449,7 @@ __device__ __forceinline__ void unroll_steps(F &f, int base, int limit) {
 }
 
 template <int RA, int RB, int ZA, int ZB>
-__global__ void __launch_bounds__(DogT<RA, RB, ZA, ZB>::NT, 1)
+__global__ void __launch_bounds__(DogT<RA, RB, ZA, ZB>::NT, 2)
     k_dog_sweep(const __grid_constant__ CUtensorMap map, const __grid_constant__ DogTaps T, const Sub *subs,
                 float *dog, int *status) {
   using C = DogT<RA, RB, ZA, ZB>;
