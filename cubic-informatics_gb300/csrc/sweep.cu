@@ -313,8 +313,8 @@ __global__ void __launch_bounds__(kSweepThreads, 1)
 // The split costs one write and one read of the DoG volume but frees the Hessian stage
 // from the z shift register's registers, so several Hessian blocks share an SM.
 constexpr int kDTX = 32, kDTY = 16;     // DoG tile (two blocks per SM)
-constexpr int kHTX = 64, kHTY = 16;     // Hessian tile
-constexpr int kHPX = kHTX + 8;          // Hessian ring row: columns x0-4 .. x0+67 (16-byte aligned start)
+constexpr int kHTX = 32, kHTY = 16;     // Hessian tile (six blocks per SM)
+constexpr int kHPX = kHTX + 8;          // Hessian ring row: columns x0-4 .. x0+kHTX+3 (16-byte aligned start)
 constexpr int kHPY = kHTY + 4;
 constexpr int kHRing = 8;              // ring slots; a slot is 72 x 20 floats = 45 x 128 bytes
 constexpr int kHThreads = kHTX / 4 * kHTY;   // one x quad per thread
@@ -548,7 +548,7 @@ __global__ void __launch_bounds__(DogT<RA, RB, ZA, ZB>::NT, 2)
 // or a fixed-point sum, so the mask and every record stay identical without it.
 __device__ __forceinline__ float hdiff(float plus, float minus) { return __fmul_rn(__fsub_rn(plus, minus), 0.5f); }
 
-__global__ void __launch_bounds__(kHThreads, 3)
+__global__ void __launch_bounds__(kHThreads, 6)
     k_hess_sweep(const __grid_constant__ CUtensorMap map, const __grid_constant__ CUtensorMap nmap, const Sub *subs,
                  uint8_t *mask, FgEntry *fg, unsigned long long *fg_count, int *status) {
   extern __shared__ __align__(128) unsigned char smem[];
