@@ -668,8 +668,14 @@ extern "C" int hdog_dog(hdog_ctx *c, const float *d_norm, float *d_dog, void *st
   if (!d_norm || !d_dog) return fail(HDOG_ERR_ARG, "hdog_dog: null buffer");
   cudaStream_t st = (cudaStream_t)stream;
   TRY(single_sub(c, nullptr, st));
+  zero_async(c->status, sizeof(int), st);
   enqueue_dog(c, 1, d_norm, d_dog, st);
   HDOG_CUDA_TRY(cudaGetLastError());
+  // the sweep's bounded TMA waits report through the status word
+  int status = 0;
+  HDOG_CUDA_TRY(cudaMemcpyAsync(&status, c->status, sizeof(int), cudaMemcpyDeviceToHost, st));
+  HDOG_CUDA_TRY(cudaStreamSynchronize(st));
+  if (status) return fail(status, "hdog_dog: a bounded device wait hit its limit");
   return HDOG_OK;
 }
 

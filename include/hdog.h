@@ -124,6 +124,8 @@ int hdog_normalize(hdog_ctx *ctx, const uint16_t *d_img, float *d_norm, void *st
    normalization radius of 0 (the copy path, which computes no box means) both are zero. */
 int hdog_normalize_parts(hdog_ctx *ctx, const uint16_t *d_img, float *d_norm, float *d_ero_l, float *d_dil_l,
                          void *stream);
+/* Synchronizes `stream`: the radius-specialised sweep's bounded waits report a timeout
+   (HDOG_ERR_TIMEOUT) through the call's return value. */
 int hdog_dog(hdog_ctx *ctx, const float *d_norm, float *d_dog, void *stream);
 /* d_hessian may be NULL; when given it receives the six planes xx,xy,xz,yy,yz,zz (pitch N). */
 int hdog_hessian_pd(hdog_ctx *ctx, const float *d_dog, uint8_t *d_mask, float *d_hessian,
