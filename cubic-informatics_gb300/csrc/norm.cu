@@ -472,7 +472,7 @@ __device__ __forceinline__ void box_chain(int L, LoadF load, float2 (&acc)[K]) {
   }
 }
 
-constexpr int kBoxYK = 16;   // y outputs per thread
+constexpr int kBoxYK = 12;   // y outputs per thread
 
 __global__ void __launch_bounds__(128) k_box_y(const Sub *subs, int r, const float2 *in, float2 *out) {
   const Sub S = subs[blockIdx.y];
