@@ -7,7 +7,8 @@
 // six Hessian planes in memory; this kernel reads the normalized volume once and writes
 // the uint8 mask plus a compact list of the foreground voxels' Hessian elements.
 //
-// A block owns a 64 x 16 output tile and sweeps z over the whole substack:
+// The generic kernel (k_dog_hess, any tap radii) gives a block a 64 x 16 output tile and
+// sweeps z over the whole substack:
 //   * each normalized slice (tile + halo, zero outside the volume) arrives by TMA
 //     (cp.async.bulk.tensor, mbarrier-completed, double buffered) while the previous one
 //     is filtered;
@@ -297,16 +298,17 @@ __global__ void __launch_bounds__(kSweepThreads, 1)
 // For common sigma pairs the chain runs as two z-sweeps with the four tap radii as
 // template parameters (RA/RB: xy radius of the small/large scale, ZA/ZB: z radius):
 //
-//   k_dog_sweep   normalized -> DoG volume.  A block owns a 64 x 16 tile and sweeps z;
-//                 stage A filters slice it along x (TMA-loaded, double-buffered), stage B
-//                 filters slice it-1 along y and feeds the z shift register, which emits
+//   k_dog_sweep   normalized -> DoG volume.  A block owns a kDTX x kDTY tile and sweeps
+//                 z; stage A filters slice it along x (TMA-loaded, double-buffered), stage
+//                 B filters slice it-1 along y and feeds the z shift register, which emits
 //                 DoG slice it-1-RZ straight to global memory.  One barrier per slice.
-//                 Taps are compile-time offsets into the constant bank.  The z shift
+//                 Tap pairs shared by both scales sit in per-thread registers, the taps of
+//                 the wider scale alone are constant-bank operands.  The z shift
 //                 register never moves: output zo lives in slot zo mod (2RZ+1), and a
 //                 switch on the step's phase picks the compile-time slot of every tap.
 //                 Every output is the reference's FMA chain, zero taps at the borders
 //                 included, so the volume equals the separate passes bit for bit.
-//   k_hess_sweep  DoG -> mask + foreground list.  A block owns a 64 x 16 tile; DoG slices
+//   k_hess_sweep  DoG -> mask + foreground list.  A block owns a kHTX x kHTY tile; DoG slices
 //                 (tile + 2-voxel halo, zero outside the volume) arrive by TMA into an
 //                 8-slot ring, up to five slices ahead; each thread tests one x quad.
 //
@@ -618,94 +620,102 @@ __global__ void __launch_bounds__(kHThreads, 6)
     // every in-plane gradient position of the quad inside the volume: the plain stencil
     // (only the z neighbours can fall outside, handled by zup / zdn)
     if (X0 >= 1 && X0 + 3 <= W - 2 && Y >= 1 && Y <= H - 2) {
-      // Voxels o = 2p, 2p+1 of the quad go as one pair through f32x2 subtract and multiply
-      // (each lane rounds as the scalar operation does): every stencil operand that sits
-      // at the same offset from both voxels comes from one 8-byte-aligned pair of a
-      // 128-bit ring load.  The x gradients of the xy and xz elements are taken at odd
-      // offsets, so they stay scalar and only their outer difference is paired.
-      auto ld12 = [&](const float *src, float2 *dst) {   // columns X0-4 .. X0+7 as 6 pairs
+      // ZI: both z neighbours inside the volume (every slice but the first and the last),
+      // compiled without the per-slice selects of the zero-halo rule
+      auto fast = [&](auto zin) {
+        constexpr bool ZI = decltype(zin)::value;
+        const bool zu = ZI || zup, zd = ZI || zdn;
+        // Voxels o = 2p, 2p+1 of the quad go as one pair through f32x2 subtract and multiply
+        // (each lane rounds as the scalar operation does): every stencil operand that sits
+        // at the same offset from both voxels comes from one 8-byte-aligned pair of a
+        // 128-bit ring load.  The x gradients of the xy and xz elements are taken at odd
+        // offsets, so they stay scalar and only their outer difference is paired.
+        auto ld12 = [&](const float *src, float2 *dst) {   // columns X0-4 .. X0+7 as 6 pairs
 #pragma unroll
-        for (int i = 0; i < 3; i++) {
-          const float4 f = *reinterpret_cast<const float4 *>(src + 4 * i);
-          dst[2 * i] = make_float2(f.x, f.y);
-          dst[2 * i + 1] = make_float2(f.z, f.w);
-        }
-      };
-      auto ld4 = [&](const float *src, float2 *dst) {    // columns X0 .. X0+3 as 2 pairs
-        const float4 f = *reinterpret_cast<const float4 *>(src + 4);
-        dst[0] = make_float2(f.x, f.y);
-        dst[1] = make_float2(f.z, f.w);
-      };
-      const float2 half = make_float2(0.5f, 0.5f), zero2 = make_float2(0.0f, 0.0f);
-      auto hd2 = [&](float2 plus, float2 minus) { return mul2(sub2(plus, minus), half); };
-      float2 h2[2][6];   // [pair][element]
-      {
-        float2 a[6], v[2], w[2], p2[2], m2[2];
-        ld12(P0 + b, a);
-        ld4(P0 + b - 2 * kHPX, v);
-        ld4(P0 + b + 2 * kHPX, w);
-        ld4(P2 + b, p2);
-        ld4(M2 + b, m2);
+          for (int i = 0; i < 3; i++) {
+            const float4 f = *reinterpret_cast<const float4 *>(src + 4 * i);
+            dst[2 * i] = make_float2(f.x, f.y);
+            dst[2 * i + 1] = make_float2(f.z, f.w);
+          }
+        };
+        auto ld4 = [&](const float *src, float2 *dst) {    // columns X0 .. X0+3 as 2 pairs
+          const float4 f = *reinterpret_cast<const float4 *>(src + 4);
+          dst[0] = make_float2(f.x, f.y);
+          dst[1] = make_float2(f.z, f.w);
+        };
+        const float2 half = make_float2(0.5f, 0.5f), zero2 = make_float2(0.0f, 0.0f);
+        auto hd2 = [&](float2 plus, float2 minus) { return mul2(sub2(plus, minus), half); };
+        float2 h2[2][6];   // [pair][element]
+        {
+          float2 a[6], v[2], w[2], p2[2], m2[2];
+          ld12(P0 + b, a);
+          ld4(P0 + b - 2 * kHPX, v);
+          ld4(P0 + b + 2 * kHPX, w);
+          ld4(P2 + b, p2);
+          ld4(M2 + b, m2);
 #pragma unroll
-        for (int p = 0; p < 2; p++) {
-          const float2 c = a[2 + p];   // voxels 2p, 2p+1 at row index 4 + 2p
-          h2[p][0] = hd2(hd2(a[3 + p], c), hd2(c, a[1 + p]));
-          h2[p][3] = hd2(hd2(w[p], c), hd2(c, v[p]));
-          h2[p][5] = hd2(zup ? hd2(p2[p], c) : zero2, zdn ? hd2(c, m2[p]) : zero2);
+          for (int p = 0; p < 2; p++) {
+            const float2 c = a[2 + p];   // voxels 2p, 2p+1 at row index 4 + 2p
+            h2[p][0] = hd2(hd2(a[3 + p], c), hd2(c, a[1 + p]));
+            h2[p][3] = hd2(hd2(w[p], c), hd2(c, v[p]));
+            h2[p][5] = hd2(zu ? hd2(p2[p], c) : zero2, zd ? hd2(c, m2[p]) : zero2);
+          }
         }
-      }
-      {
-        float2 u[6], dn[6];
-        ld12(P0 + b - kHPX, u);
-        ld12(P0 + b + kHPX, dn);
-        const float *uf = reinterpret_cast<const float *>(u), *df = reinterpret_cast<const float *>(dn);
+        {
+          float2 u[6], dn[6];
+          ld12(P0 + b - kHPX, u);
+          ld12(P0 + b + kHPX, dn);
+          const float *uf = reinterpret_cast<const float *>(u), *df = reinterpret_cast<const float *>(dn);
 #pragma unroll
-        for (int p = 0; p < 2; p++) {
-          const int o = 2 * p;
-          const float2 gd = make_float2(hdiff(df[o + 5], df[o + 3]), hdiff(df[o + 6], df[o + 4]));
-          const float2 gu = make_float2(hdiff(uf[o + 5], uf[o + 3]), hdiff(uf[o + 6], uf[o + 4]));
-          h2[p][1] = hd2(gd, gu);
+          for (int p = 0; p < 2; p++) {
+            const int o = 2 * p;
+            const float2 gd = make_float2(hdiff(df[o + 5], df[o + 3]), hdiff(df[o + 6], df[o + 4]));
+            const float2 gu = make_float2(hdiff(uf[o + 5], uf[o + 3]), hdiff(uf[o + 6], uf[o + 4]));
+            h2[p][1] = hd2(gd, gu);
+          }
         }
-      }
-      {
-        float2 pp[6], mm[6];
-        ld12(P1 + b, pp);
-        ld12(M1 + b, mm);
-        const float *pf = reinterpret_cast<const float *>(pp), *mf = reinterpret_cast<const float *>(mm);
+        {
+          float2 pp[6], mm[6];
+          ld12(P1 + b, pp);
+          ld12(M1 + b, mm);
+          const float *pf = reinterpret_cast<const float *>(pp), *mf = reinterpret_cast<const float *>(mm);
 #pragma unroll
-        for (int p = 0; p < 2; p++) {
-          const int o = 2 * p;
-          const float2 gp = zup ? make_float2(hdiff(pf[o + 5], pf[o + 3]), hdiff(pf[o + 6], pf[o + 4])) : zero2;
-          const float2 gm = zdn ? make_float2(hdiff(mf[o + 5], mf[o + 3]), hdiff(mf[o + 6], mf[o + 4])) : zero2;
-          h2[p][2] = hd2(gp, gm);
+          for (int p = 0; p < 2; p++) {
+            const int o = 2 * p;
+            const float2 gp = zu ? make_float2(hdiff(pf[o + 5], pf[o + 3]), hdiff(pf[o + 6], pf[o + 4])) : zero2;
+            const float2 gm = zd ? make_float2(hdiff(mf[o + 5], mf[o + 3]), hdiff(mf[o + 6], mf[o + 4])) : zero2;
+            h2[p][2] = hd2(gp, gm);
+          }
         }
-      }
-      {
-        float2 pu[2], pd[2], mu[2], md[2];
-        ld4(P1 + b - kHPX, pu);
-        ld4(P1 + b + kHPX, pd);
-        ld4(M1 + b - kHPX, mu);
-        ld4(M1 + b + kHPX, md);
+        {
+          float2 pu[2], pd[2], mu[2], md[2];
+          ld4(P1 + b - kHPX, pu);
+          ld4(P1 + b + kHPX, pd);
+          ld4(M1 + b - kHPX, mu);
+          ld4(M1 + b + kHPX, md);
+#pragma unroll
+          for (int p = 0; p < 2; p++)
+            h2[p][4] = hd2(zu ? hd2(pd[p], pu[p]) : zero2, zd ? hd2(md[p], mu[p]) : zero2);
+        }
 #pragma unroll
         for (int p = 0; p < 2; p++)
-          h2[p][4] = hd2(zup ? hd2(pd[p], pu[p]) : zero2, zdn ? hd2(md[p], mu[p]) : zero2);
-      }
 #pragma unroll
-      for (int p = 0; p < 2; p++)
+          for (int k = 0; k < 6; k++) {
+            hv[2 * p][k] = h2[p][k].x;
+            hv[2 * p + 1][k] = h2[p][k].y;
+          }
+        uint32_t mword = 0;
 #pragma unroll
-        for (int k = 0; k < 6; k++) {
-          hv[2 * p][k] = h2[p][k].x;
-          hv[2 * p + 1][k] = h2[p][k].y;
+        for (int o = 0; o < 4; o++) {
+          const bool pdv = pd_test(hv[o][0], hv[o][1], hv[o][2], hv[o][3], hv[o][4], hv[o][5]);
+          mword |= (pdv ? 1u : 0u) << (8 * o);
+          fgv[o] = pdv;
+          nfg += pdv;
         }
-      uint32_t mword = 0;
-#pragma unroll
-      for (int o = 0; o < 4; o++) {
-        const bool pdv = pd_test(hv[o][0], hv[o][1], hv[o][2], hv[o][3], hv[o][4], hv[o][5]);
-        mword |= (pdv ? 1u : 0u) << (8 * o);
-        fgv[o] = pdv;
-        nfg += pdv;
-      }
-      *reinterpret_cast<uint32_t *>(mask + S.vox + i0) = mword;
+        *reinterpret_cast<uint32_t *>(mask + S.vox + i0) = mword;
+      };
+      if (zup && zdn) fast(std::true_type{});
+      else fast(std::false_type{});
     } else {
 #pragma unroll
       for (int o = 0; o < 4; o++) {
