@@ -165,6 +165,15 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
   return done != 0;
 }
 
+// One arrival on bar (release: the caller's shared-memory reads before it are ordered
+// before whatever a waiter does after the phase completes).
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+  asm volatile(
+      "{\n\t.reg .b64 st;\n\t"
+      "mbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(smem_u32(bar))
+      : "memory");
+}
+
 // One box of a 4-D tensor map (x, y, z, substack) into shared memory, completing on bar.
 __device__ __forceinline__ void tma_load_4d(const void *map, void *dst, uint64_t *bar, int x, int y, int z, int s,
                                             uint32_t bytes) {

@@ -566,12 +566,16 @@ __global__ void __launch_bounds__(kHThreads, 6)
   float *nring = reinterpret_cast<float *>(smem + (size_t)kHRing * PL * 4);
   uint64_t *bar = reinterpret_cast<uint64_t *>(smem + (size_t)kHRing * PL * 4 + (size_t)kNRing * kHTX * kHTY * 4);
   uint64_t *nbar = bar + kHRing;
+  // done[zh % kHRing] completes when every warp has finished iteration zh: its last reads
+  // of DoG slice zh-2 and of normalized slice zh
+  uint64_t *done = nbar + kNRing;
   const int t = threadIdx.x;
   const int D = S.D, W = S.W, H = S.H;
   const int32_t WH = W * H;
   if (t == 0) {
     for (int i = 0; i < kHRing; i++) mbar_init(&bar[i], 1);
     for (int i = 0; i < kNRing; i++) mbar_init(&nbar[i], 1);
+    for (int i = 0; i < kHRing; i++) mbar_init(&done[i], kHThreads / 32);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
@@ -600,11 +604,20 @@ __global__ void __launch_bounds__(kHThreads, 6)
   const int X0 = x0 + 4 * q, Y = y0 + ly;
   const int b = (ly + 2) * kHPX + 4 * q;   // ring index of column X0 - 4 on row Y
   for (int zh = 0; zh < D; zh++) {
-    if (t == 0 && ok && zh + 5 <= D + 1)
-      tma_slice(&map, ring + slot(zh + 5) * PL, &bar[slot(zh + 5)], tx, ty, zh + 5, blockIdx.y, tma_bytes);
-    if (t == 0 && ok && zh + 3 < D)
-      tma_slice(&nmap, nring + ((zh + 3) % kNRing) * kHTX * kHTY, &nbar[(zh + 3) % kNRing], x0, y0, zh + 3, blockIdx.y,
-                ntma_bytes);
+    // DoG slice zh+5 reuses the slot of slice zh-3 and normalized slice zh+3 the slot of
+    // slice zh-1, both read for the last time in iteration zh-1: the producer waits until
+    // every warp is past it (warps otherwise run up to the ring's depth apart)
+    if (t == 0 && ok && (zh + 5 <= D + 1 || zh + 3 < D)) {
+      if (zh >= 1 && !mbar_wait(&done[(zh - 1) % kHRing], ((zh - 1) / kHRing) & 1)) {
+        ok = false;
+        atomicExch(status, HDOG_ERR_TIMEOUT);
+      }
+      if (ok && zh + 5 <= D + 1)
+        tma_slice(&map, ring + slot(zh + 5) * PL, &bar[slot(zh + 5)], tx, ty, zh + 5, blockIdx.y, tma_bytes);
+      if (ok && zh + 3 < D)
+        tma_slice(&nmap, nring + ((zh + 3) % kNRing) * kHTX * kHTY, &nbar[(zh + 3) % kNRing], x0, y0, zh + 3,
+                  blockIdx.y, ntma_bytes);
+    }
     // slices zh-2 .. zh+1 were waited for already; zh+2 is new
     if (ok && !mbar_wait(&bar[slot(zh + 2)], use(zh + 2) & 1)) {
       ok = false;
@@ -776,7 +789,8 @@ __global__ void __launch_bounds__(kHThreads, 6)
       }
       base++;
     }
-    __syncthreads();   // slot of zh-2 is reloaded in the next iteration
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&done[zh % kHRing]);
   }
 }
 
@@ -820,7 +834,7 @@ static const SweepInst *find_inst(const DogTaps &T) {
 }
 
 static constexpr size_t kHessSmem =
-    (size_t)kHRing * kHPX * kHPY * 4 + (size_t)kNRing * kHTX * kHTY * 4 + (kHRing + kNRing) * 8;
+    (size_t)kHRing * kHPX * kHPY * 4 + (size_t)kNRing * kHTX * kHTY * 4 + (2 * kHRing + kNRing) * 8;
 static_assert((kHPX * kHPY * 4) % 128 == 0, "TMA ring slots must start on 128-byte boundaries");
 
 // Whether the fused sweep handles these parameters (else the separate passes run).
