@@ -304,7 +304,7 @@ static void plan(const hdog_params *p, int max_sub, int64_t &nvox, int64_t &reg_
   L.add(S * edge_capacity(nvox) * sizeof(int2));          // 28 cross-tile edges
   L.add(S * sizeof(unsigned long long));     // 29 edge counts
   L.add(S * fg_capacity(nvox) * sizeof(FgEntry));         // 30 foreground list
-  L.add(S * sizeof(unsigned long long));     // 31 foreground counts
+  L.add(S * kFgCountStride * sizeof(unsigned long long));   // 31 foreground counts (strided)
 }
 
 extern "C" int hdog_ctx_bytes(const hdog_params *p, int max_substacks, size_t *bytes) {
@@ -564,7 +564,8 @@ static int readback(hdog_ctx *c, int nsub, cudaStream_t st) {
   HDOG_CUDA_TRY(cudaGetLastError());
   HDOG_CUDA_TRY(cudaMemcpyAsync(c->h_counts, c->num_records, nsub * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
   HDOG_CUDA_TRY(cudaMemcpyAsync(c->h_counts + ms, c->num_regions, nsub * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
-  HDOG_CUDA_TRY(cudaMemcpyAsync(c->h_counts + 2 * ms, c->fg_count, nsub * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  HDOG_CUDA_TRY(cudaMemcpy2DAsync(c->h_counts + 2 * ms, sizeof(int64_t), c->fg_count, kFgCountStride * sizeof(int64_t),
+                                  sizeof(int64_t), nsub, cudaMemcpyDeviceToHost, st));
   HDOG_CUDA_TRY(cudaMemcpyAsync(c->h_counts + 3 * ms, c->status, sizeof(int), cudaMemcpyDeviceToHost, st));
   HDOG_CUDA_TRY(cudaStreamSynchronize(st));
   const int status = *(int *)(c->h_counts + 3 * ms);
@@ -591,7 +592,7 @@ static int run_batch(hdog_ctx *c, int nsub, cudaStream_t st) {
   }
   enqueue_normalize(c, nsub, c->norm, st);
   const bool fused = fused_ok(c);
-  if (fused) zero_async(c->fg_count, nsub * sizeof(unsigned long long), st);
+  if (fused) zero_async(c->fg_count, (size_t)nsub * kFgCountStride * sizeof(unsigned long long), st);
   enqueue_after_norm(c, nsub, fused, st);
   TRY(readback(c, nsub, st));
   if (fused) {

@@ -282,7 +282,7 @@ __device__ __forceinline__ uint32_t prune_links(uint32_t todo, const uint32_t (&
   return todo;
 }
 
-__global__ void __launch_bounds__(kCclThreads) k_ccl_local(const Sub *subs, const uint8_t *mask, int32_t *labels,
+__global__ void __launch_bounds__(kCclThreads, 4) k_ccl_local(const Sub *subs, const uint8_t *mask, int32_t *labels,
                                                           int2 *edges, unsigned long long *edge_count) {
   __shared__ uint32_t par[kCells];
   __shared__ uint8_t occ[kHalo];
@@ -358,10 +358,13 @@ __global__ void __launch_bounds__(kCclThreads) k_ccl_local(const Sub *subs, cons
   }
   __syncthreads();
   // 2. unions between neighbouring cells of the tile.  The unrolled neighbour tests only
-  //    collect a 13-bit list; the unions then run in warp-wide rounds, one per lane and
-  //    round, re-converged after each, so lanes whose finds and retries differ in length
-  //    do not split the warp for the rest of the pass.
+  //    collect a 13-bit list per cell, parked in minv (unused until step 3); the unions then
+  //    run in warp-wide rounds over the lane's whole cell column, one link per lane and
+  //    round, re-converged after each, so lanes whose finds and retries differ in length do
+  //    not split the warp, and a lane with many links in one layer does not hold the
+  //    others idle for that layer alone.  Union order does not change the components.
   const int cx = t % kCX, cy = t / kCX;
+  uint32_t layers = 0;   // bit cz: the cell of layer cz has links
   for (int cz = 0; cz < ncz; cz++) {
     const int c = (cz * kCY + cy) * kCX + cx;
     const uint32_t oc = occ[halo_of(cx, cy, cz)];
@@ -377,7 +380,19 @@ __global__ void __launch_bounds__(kCclThreads) k_ccl_local(const Sub *subs, cons
       }
       todo = prune_links(todo, on);
     }
-    while (__any_sync(0xFFFFFFFFu, todo != 0)) {
+    minv[c] = todo;
+    layers |= (todo ? 1u : 0u) << cz;
+  }
+  {
+    uint32_t todo = 0;
+    int c = 0;
+    while (__any_sync(0xFFFFFFFFu, todo != 0 || layers != 0)) {
+      if (!todo && layers) {
+        const int cz = __ffs(layers) - 1;
+        layers &= layers - 1;
+        c = (cz * kCY + cy) * kCX + cx;
+        todo = minv[c];
+      }
       if (todo) {
         const int k = __ffs(todo) - 1;
         todo &= todo - 1;
@@ -391,6 +406,7 @@ __global__ void __launch_bounds__(kCclThreads) k_ccl_local(const Sub *subs, cons
       __syncwarp();
     }
   }
+  for (int cz = 0; cz < ncz; cz++) minv[(cz * kCY + cy) * kCX + cx] = 0xFFFFFFFFu;
   __syncthreads();
   // 3. roots in place, then each component's minimum voxel (tile order = volume order)
   for (int cz = 0; cz < ncz; cz++) {
@@ -646,7 +662,7 @@ __global__ void __launch_bounds__(256) k_ccl_flatten_fg(const Sub *subs, const F
                                                        uint32_t *root_bits, uint32_t *blk_counts, int32_t *fg_root,
                                                        int *status) {
   const Sub S = subs[blockIdx.y];
-  const int64_t cnt = (int64_t)fg_count[blockIdx.y];
+  const int64_t cnt = (int64_t)fg_count[blockIdx.y * kFgCountStride];
   if (cnt > S.fg_cap) return;
   const int64_t n = (int64_t)S.W * S.H * S.D;
   int32_t *L = labels + S.vox;

@@ -24,6 +24,11 @@ struct Sub {
   const uint16_t *src;    // slice 0 of the raw input (device); slices are W*H apart
 };
 
+// Foreground-list counters of the substacks of a batch sit kFgCountStride 64-bit slots
+// apart: every warp of the Hessian sweep takes its list slots with an atomic on its
+// substack's counter, and counters on separate 4 KB lines spread those atomics over L2.
+constexpr int kFgCountStride = 512;
+
 // A foreground voxel and its six Hessian elements, written by the fused sweep.
 struct FgEntry {
   int32_t idx;            // linear voxel index inside the substack

@@ -222,7 +222,7 @@ __global__ void __launch_bounds__(256, 2) k_accumulate_fg(const Sub *subs, const
                                                        const unsigned long long *fg_count, const int32_t *fg_root,
                                                        const int32_t *rank, RegionAcc acc, int64_t slots) {
   const Sub S = subs[blockIdx.y];
-  const int64_t cnt = (int64_t)fg_count[blockIdx.y];
+  const int64_t cnt = (int64_t)fg_count[blockIdx.y * kFgCountStride];
   if (cnt > S.fg_cap) return;   // overflowed: the batch is redone without the fused sweep
   const int W = S.W, H = S.H;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x * kFgChunk;

@@ -273,7 +273,7 @@ __global__ void __launch_bounds__(kSweepThreads, 1)
       }
       const int tot = __shfl_sync(0xFFFFFFFFu, incl, 31);
       unsigned long long base = 0;
-      if (lane == 31 && tot) base = atomicAdd(&fg_count[blockIdx.y], (unsigned long long)tot);
+      if (lane == 31 && tot) base = atomicAdd(&fg_count[blockIdx.y * kFgCountStride], (unsigned long long)tot);
       base = __shfl_sync(0xFFFFFFFFu, base, 31) + (unsigned long long)(incl - nfg);
       for (int u = 0; u < 2; u++) {
         if (!fgv[u]) continue;
@@ -777,7 +777,7 @@ __global__ void __launch_bounds__(kHThreads, 6)
     }
     const int tot = __shfl_sync(0xFFFFFFFFu, incl, 31);
     unsigned long long base = 0;
-    if (lane == 31 && tot) base = atomicAdd(&fg_count[blockIdx.y], (unsigned long long)tot);
+    if (lane == 31 && tot) base = atomicAdd(&fg_count[blockIdx.y * kFgCountStride], (unsigned long long)tot);
     base = __shfl_sync(0xFFFFFFFFu, base, 31) + (unsigned long long)(incl - nfg);
 #pragma unroll
     for (int o = 0; o < 4; o++) {
@@ -875,7 +875,7 @@ int launch_dog_hess(const Sub *d_subs, int nsub, int W, int H, int D, const DogT
                     float *dog, uint8_t *mask, FgEntry *fg, unsigned long long *fg_count, int *d_status,
                     cudaStream_t s) {
   const int rxy = max(T.r[0], T.r[2]), rz = max(T.r[1], T.r[3]);
-  zero_async(fg_count, nsub * sizeof(unsigned long long), s);
+  zero_async(fg_count, (size_t)nsub * kFgCountStride * sizeof(unsigned long long), s);
   const SweepInst *si = find_inst(T);
   if (si) {
     CUtensorMap map_n, map_d, map_t;
