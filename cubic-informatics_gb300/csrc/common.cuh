@@ -86,15 +86,16 @@ __device__ __forceinline__ float cdiff(float plus, float minus) {
 //   xx*yy > xy*xy              (`a - b > 0` folded to `a > b`, both products rounded)
 //   t = fma(xx*yy, zz, (2xy*yz)*xz); t = fma(-(xx*yz), yz, t); t = fma(-(yy*xz), xz, t)
 //   t < (zz*xy)*xy             (the last subtraction of the determinant folded into `< 0`)
+// All three conditions are evaluated and combined without short-circuit: the products
+// have no side effects, so the result is the same, and the tile kernels test four voxels
+// per thread without a divergent branch per voxel.
 __device__ __forceinline__ bool pd_test(float xx, float xy, float xz, float yy, float yz, float zz) {
-  if (!(xx < 0.0f)) return false;
   const float p = __fmul_rn(xx, yy);
-  if (!(p > __fmul_rn(xy, xy))) return false;
   const float q = __fmul_rn(__fmul_rn(2.0f, xy), yz);
   float t = __fmaf_rn(p, zz, __fmul_rn(q, xz));
   t = __fmaf_rn(-__fmul_rn(xx, yz), yz, t);
   t = __fmaf_rn(-__fmul_rn(yy, xz), xz, t);
-  return t < __fmul_rn(__fmul_rn(zz, xy), xy);
+  return (xx < 0.0f) & (p > __fmul_rn(xy, xy)) & (t < __fmul_rn(__fmul_rn(zz, xy), xy));
 }
 
 // The six Hessian elements at voxel (x, y, z) straight from global memory, with the
