@@ -556,7 +556,13 @@ static void enqueue_after_norm(hdog_ctx *c, int nsub, bool fused, cudaStream_t s
                   c->blk_counts, c->blk_offsets, c->chunk, c->num_records, c->records, c->nblk, st);
 }
 
-static bool fused_ok(hdog_ctx *c) { return c->use_sweep && sweep_supported(c->taps, c->W, c->max_smem); }
+// The fused sweep and the list-based region sums; the latter add coordinates in 32 bits
+// inside a warp (at most 512 entries of coordinates below 2^16), so larger frames take
+// the separate passes.
+static bool fused_ok(hdog_ctx *c) {
+  return c->use_sweep && c->W <= 65535 && c->H <= 65535 && c->D <= 65535 &&
+         sweep_supported(c->taps, c->W, c->max_smem);
+}
 
 // Reads record / region / foreground counts and the status word back (one sync).
 static int readback(hdog_ctx *c, int nsub, cudaStream_t st) {

@@ -213,60 +213,129 @@ __global__ void __launch_bounds__(256) k_accumulate(const Sub *subs, const uint8
   run_flush(a, S, acc, slots);
 }
 
-// The same accumulation from the foreground list of the fused sweep: each thread takes
-// kFgChunk consecutive entries (neighbouring voxels of one tile row pair, so mostly one
-// region) and flushes a run whenever the region changes.
-constexpr int kFgChunk = 8;
+// The same accumulation from the foreground list of the fused sweep, a warp at a time:
+// lane l takes entry e0 + 32 j + l (coalesced), consecutive entries of one region (the
+// sweep appends the foreground of a 32 x 4 patch at a time, so runs are long) are summed
+// across the warp by a segmented shuffle scan, and only the last lane of each run issues
+// the atomics.  A run that reaches lane 31 carries into lane 0 of the next 32 entries, so
+// a region's sums leave the warp once per kAccSpan-entry task at most.  All sums are
+// integers (fixed point for the float ones), so the grouping does not change them.
+constexpr int kAccSpan = 512;   // entries per warp task
+static_assert((long long)kAccSpan * 65535 < (1ll << 32), "32-bit coordinate sums of a warp task");
 
-__global__ void __launch_bounds__(256, 2) k_accumulate_fg(const Sub *subs, const FgEntry *fg,
+// Sums of one run inside a warp task: the coordinate sums of at most kAccSpan entries fit
+// 32 bits because the list path runs only for frames below 2^16 voxels on every axis
+// (they widen to 64 bits in the atomics).
+struct RunSums {
+  uint32_t count, max_ord, x, y, z;
+  unsigned long long norm, h[6];
+};
+
+__device__ __forceinline__ void sums_add(RunSums &a, const RunSums &b) {
+  a.count += b.count;
+  a.max_ord = max(a.max_ord, b.max_ord);
+  a.norm += b.norm;
+  a.x += b.x;
+  a.y += b.y;
+  a.z += b.z;
+#pragma unroll
+  for (int k = 0; k < 6; k++) a.h[k] += b.h[k];
+}
+
+__device__ __forceinline__ RunSums sums_shfl_up(const RunSums &a, int d) {
+  RunSums b;
+  b.count = __shfl_up_sync(0xFFFFFFFFu, a.count, d);
+  b.max_ord = __shfl_up_sync(0xFFFFFFFFu, a.max_ord, d);
+  b.norm = __shfl_up_sync(0xFFFFFFFFu, a.norm, d);
+  b.x = __shfl_up_sync(0xFFFFFFFFu, a.x, d);
+  b.y = __shfl_up_sync(0xFFFFFFFFu, a.y, d);
+  b.z = __shfl_up_sync(0xFFFFFFFFu, a.z, d);
+#pragma unroll
+  for (int k = 0; k < 6; k++) b.h[k] = __shfl_up_sync(0xFFFFFFFFu, a.h[k], d);
+  return b;
+}
+
+__device__ __forceinline__ RunSums sums_shfl(const RunSums &a, int src) {
+  RunSums b;
+  b.count = __shfl_sync(0xFFFFFFFFu, a.count, src);
+  b.max_ord = __shfl_sync(0xFFFFFFFFu, a.max_ord, src);
+  b.norm = __shfl_sync(0xFFFFFFFFu, a.norm, src);
+  b.x = __shfl_sync(0xFFFFFFFFu, a.x, src);
+  b.y = __shfl_sync(0xFFFFFFFFu, a.y, src);
+  b.z = __shfl_sync(0xFFFFFFFFu, a.z, src);
+#pragma unroll
+  for (int k = 0; k < 6; k++) b.h[k] = __shfl_sync(0xFFFFFFFFu, a.h[k], src);
+  return b;
+}
+
+__device__ __forceinline__ void sums_flush(const RunSums &a, int64_t r, const Sub &S, RegionAcc acc, int64_t slots) {
+  if (r <= 0 || r >= S.reg_cap || a.count == 0) return;
+  const int64_t g = S.reg + r;
+  atomicAdd(&acc.count[g], a.count);
+  atomicMax(&acc.max_ord[g], a.max_ord);
+  atomicAdd(&acc.sum_norm[g], a.norm);
+  atomicAdd(&acc.sum_xyz[g], (unsigned long long)a.x);
+  atomicAdd(&acc.sum_xyz[slots + g], (unsigned long long)a.y);
+  atomicAdd(&acc.sum_xyz[2 * slots + g], (unsigned long long)a.z);
+#pragma unroll
+  for (int k = 0; k < 6; k++) atomicAdd(&acc.hess[k * slots + g], a.h[k]);
+}
+
+__global__ void __launch_bounds__(256) k_accumulate_fg(const Sub *subs, const FgEntry *fg,
                                                        const unsigned long long *fg_count, const int32_t *fg_root,
                                                        const int32_t *rank, RegionAcc acc, int64_t slots) {
   const Sub S = subs[blockIdx.y];
   const int64_t cnt = (int64_t)fg_count[blockIdx.y * kFgCountStride];
   if (cnt > S.fg_cap) return;   // overflowed: the batch is redone without the fused sweep
   const int W = S.W, H = S.H;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x * kFgChunk;
-  for (int64_t e0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * kFgChunk; e0 < cnt; e0 += stride) {
-    // the chunk's gathers level by level (entries, then labels, then ranks), so a thread
-    // has all loads of a level in flight at once instead of one dependent chain per entry
-    const int ne = (int)min((int64_t)kFgChunk, cnt - e0);
-    float4 q0[kFgChunk];
-    int32_t lab[kFgChunk];
-    int32_t rk[kFgChunk];
-    const float4 *src = reinterpret_cast<const float4 *>(fg + S.fg + e0);
-#pragma unroll
-    for (int k = 0; k < kFgChunk; k++)
-      if (k < ne) q0[k] = __ldg(src + 2 * k);
-#pragma unroll
-    for (int k = 0; k < kFgChunk; k++) lab[k] = k < ne ? __ldg(fg_root + S.fg + e0 + k) : 0;
-#pragma unroll
-    for (int k = 0; k < kFgChunk; k++) rk[k] = k < ne ? rank[S.vox + lab[k]] : -1;
-    RunAcc a;
-    run_reset(a, -1);
-#pragma unroll
-    for (int k = 0; k < kFgChunk; k++) {
-      if (k >= ne) break;
-      const int32_t i = __float_as_int(q0[k].x);
-      const float4 q1 = __ldg(src + 2 * k + 1);
-      if (rk[k] != a.r) {
-        run_flush(a, S, acc, slots);
-        run_reset(a, rk[k]);
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const float4 *ent = reinterpret_cast<const float4 *>(fg + S.fg);
+  for (int64_t e0 = warp * kAccSpan; e0 < cnt; e0 += nwarps * kAccSpan) {
+    const int64_t e1 = min(e0 + kAccSpan, cnt);
+    RunSums carry = {};   // the run that reached lane 31 of the previous 32 entries (same in every lane)
+    int32_t ck = -1;      // its region
+    for (int64_t b = e0; b < e1; b += 32) {
+      const int64_t e = b + lane;
+      RunSums v = {};
+      int32_t key = -1;
+      if (e < e1) {
+        const float4 q0 = __ldg(ent + 2 * e), q1 = __ldg(ent + 2 * e + 1);
+        key = rank[S.vox + __ldg(fg_root + S.fg + e)];
+        const int32_t i = __float_as_int(q0.x);
+        v.count = 1;
+        v.max_ord = f2ord(q0.y);
+        v.norm = to_fix(q0.y);
+        v.x = (uint32_t)(i % W);
+        v.y = (uint32_t)((i / W) % H);
+        v.z = (uint32_t)(i / (W * H));
+        v.h[0] = to_fix(q0.z);
+        v.h[1] = to_fix(q0.w);
+        v.h[2] = to_fix(q1.x);
+        v.h[3] = to_fix(q1.y);
+        v.h[4] = to_fix(q1.z);
+        v.h[5] = to_fix(q1.w);
       }
-      const int x = i % W, y = (i / W) % H, z = i / (W * H);
-      a.count++;
-      a.max_ord = max(a.max_ord, f2ord(q0[k].y));
-      a.norm += to_fix(q0[k].y);
-      a.x += (unsigned long long)x;
-      a.y += (unsigned long long)y;
-      a.z += (unsigned long long)z;
-      a.h[0] += to_fix(q0[k].z);
-      a.h[1] += to_fix(q0[k].w);
-      a.h[2] += to_fix(q1.x);
-      a.h[3] += to_fix(q1.y);
-      a.h[4] += to_fix(q1.z);
-      a.h[5] += to_fix(q1.w);
+      // the carried run joins lane 0's run, or leaves the warp
+      if (lane == 0) {
+        if (key == ck) sums_add(v, carry);
+        else sums_flush(carry, ck, S, acc, slots);
+      }
+      const int32_t prev = __shfl_up_sync(0xFFFFFFFFu, key, 1);
+      const uint32_t heads = __ballot_sync(0xFFFFFFFFu, lane == 0 || key != prev);
+      const int start = 31 - __clz(heads & (0xFFFFFFFFu >> (31 - lane)));   // first lane of this run
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const RunSums u = sums_shfl_up(v, d);
+        if (lane - d >= start) sums_add(v, u);
+      }
+      // last lane of a run that ends inside these 32 entries: flush; lane 31 carries
+      if (lane != 31 && ((heads >> (lane + 1)) & 1u)) sums_flush(v, key, S, acc, slots);
+      carry = sums_shfl(v, 31);
+      ck = __shfl_sync(0xFFFFFFFFu, key, 31);
     }
-    run_flush(a, S, acc, slots);
+    if (lane == 0) sums_flush(carry, ck, S, acc, slots);
   }
 }
 
@@ -442,7 +511,7 @@ void launch_regions_fg(const Sub *d_subs, int nsub, int64_t max_n, int64_t max_f
   launch_scan(vseg, nsub, blk_counts, blk_offsets, chunk, d_num_regions, 1, s);
   KLAUNCH("k_rank", s, (k_rank<<<dim3(ceil_div(max_n, kScanBlock), nsub), kRankThreads, 0, s>>>(d_subs, root_bits, blk_offsets,
                                                                                       rank, acc, slots, d_status)));
-  int64_t want = (int64_t)ceil_div(max_fg, 256 * kFgChunk);
+  int64_t want = (int64_t)ceil_div(max_fg, 8 * kAccSpan);   // eight warps of 256-thread blocks
   const int64_t cap = (int64_t)8 * num_sms / (nsub > 0 ? nsub : 1) + 1;
   if (want > cap) want = cap;
   if (want < 1) want = 1;
