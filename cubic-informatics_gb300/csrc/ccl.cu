@@ -515,26 +515,30 @@ __global__ void __launch_bounds__(kCclThreads, 4) k_ccl_local(const Sub *subs, c
       if ((int64_t)j < S.edge_cap) edges[S.edge + j] = ebuf[i];
     }
   }
-  // 6. labels: the component's minimum voxel as a global index, background -> 0 (whole
-  //    rows, vector stores)
+  // 6. labels: the component's minimum voxel as a global index, background -> 0.  First
+  //    every occupied cell's label, once per cell, into par (whose roots are no longer
+  //    needed), then whole rows of voxels from their cells' labels (vector stores).
+  for (int cz = 0; cz < ncz; cz++) {
+    const int c = (cz * kCY + cy) * kCX + cx;
+    if (!occ[halo_of(cx, cy, cz)]) continue;
+    const uint32_t r = minv[par[c]];
+    par[c] = (uint32_t)((T.z0 + (int)(r / (kTX * kTY))) * WH + (int64_t)(T.y0 + (int)((r / kTX) % kTY)) * S.W +
+                        T.x0 + (int)(r % kTX));
+  }
+  __syncthreads();
   const int lx0 = (t % (kTX / 4)) * 4, ly = t / (kTX / 4);
   const int x = T.x0 + lx0, y = T.y0 + ly;
   if (y >= S.H) return;
   const bool vec = x + 3 < S.W && (S.W % 4 == 0);
   int32_t *L = labels + S.vox;
+  const int c0x = lx0 >> 1;   // the quad's voxels lie in cells c0x (first two) and c0x + 1
   for (int lz = 0; lz < T.tz; lz++) {
     const int64_t g = (T.z0 + lz) * WH + (int64_t)y * S.W + x;
-    int32_t out[4];
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-      const int lx = lx0 + k;
-      out[k] = 0;
-      if ((occ[halo_of(lx >> 1, ly >> 1, lz >> 1)] >> cell_bit(lx, ly, lz)) & 1u) {
-        const uint32_t r = minv[par[((lz >> 1) * kCY + (ly >> 1)) * kCX + (lx >> 1)]];
-        out[k] = (int32_t)((T.z0 + (int)(r / (kTX * kTY))) * WH + (int64_t)(T.y0 + (int)((r / kTX) % kTY)) * S.W +
-                           T.x0 + (int)(r % kTX));
-      }
-    }
+    const int b = ((lz & 1) << 2) | ((ly & 1) << 1);   // bit of the even-x voxel in its cell
+    const uint32_t o0 = occ[halo_of(c0x, ly >> 1, lz >> 1)] >> b, o1 = occ[halo_of(c0x + 1, ly >> 1, lz >> 1)] >> b;
+    const int cb = ((lz >> 1) * kCY + (ly >> 1)) * kCX + c0x;
+    const int32_t l0 = (o0 & 3u) ? (int32_t)par[cb] : 0, l1 = (o1 & 3u) ? (int32_t)par[cb + 1] : 0;
+    int32_t out[4] = {(o0 & 1u) ? l0 : 0, (o0 & 2u) ? l0 : 0, (o1 & 1u) ? l1 : 0, (o1 & 2u) ? l1 : 0};
     if (vec) {
       *reinterpret_cast<int4 *>(L + g) = make_int4(out[0], out[1], out[2], out[3]);
     } else {
