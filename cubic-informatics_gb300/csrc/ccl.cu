@@ -672,12 +672,17 @@ __global__ void __launch_bounds__(256) k_ccl_flatten_fg(const Sub *subs, const F
   int32_t *L = labels + S.vox;
   const int32_t *ent = reinterpret_cast<const int32_t *>(fg + S.fg);   // idx is each entry's first word
   constexpr int kWords = (int)(sizeof(FgEntry) / sizeof(int32_t));
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x * kFlatFgPerThread;
-  for (int64_t e0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * kFlatFgPerThread; e0 < cnt; e0 += stride) {
+  // a warp takes 32 * kFlatFgPerThread consecutive entries, lane l every 32nd from l, so each
+  // load and store of the warp covers 32 consecutive entries
+  const int lane = threadIdx.x & 31;
+  const int64_t span = 32 * kFlatFgPerThread;
+  const int64_t stride = ((int64_t)gridDim.x * blockDim.x >> 5) * span;
+  for (int64_t w0 = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * span; w0 < cnt; w0 += stride) {
+    const int64_t e0 = w0 + lane;   // entries e0 + 32 k
     // level by level: the entries' voxels, their labels, the labels' parents
     int32_t idx[kFlatFgPerThread], l[kFlatFgPerThread], p[kFlatFgPerThread];
 #pragma unroll
-    for (int k = 0; k < kFlatFgPerThread; k++) idx[k] = e0 + k < cnt ? __ldg(ent + (e0 + k) * kWords) : -1;
+    for (int k = 0; k < kFlatFgPerThread; k++) idx[k] = e0 + 32 * k < cnt ? __ldg(ent + (e0 + 32 * k) * kWords) : -1;
 #pragma unroll
     for (int k = 0; k < kFlatFgPerThread; k++) l[k] = idx[k] >= 0 ? __ldcg(L + idx[k]) : -1;
 #pragma unroll
@@ -687,7 +692,7 @@ __global__ void __launch_bounds__(256) k_ccl_flatten_fg(const Sub *subs, const F
       if (l[k] < 0) continue;
       const int32_t r = p[k] == l[k] ? l[k] : uf_root(L, p[k], n, status);
       if (r != l[k]) L[idx[k]] = r;
-      fg_root[S.fg + e0 + k] = r;   // the entry's root, read by the region accumulation
+      fg_root[S.fg + e0 + 32 * k] = r;   // the entry's root, read by the region accumulation
       if (r == idx[k]) {
         const int64_t b = idx[k] / kScanBlock;
         const int o = (int)(idx[k] % kScanBlock);
