@@ -84,6 +84,48 @@ __global__ void __launch_bounds__(256) k_mm_z(const Sub *subs, int rz, uint32_t 
   }
 }
 
+// The same z pass with nearest borders and a compile-time radius, streaming van Herk /
+// Gil-Werman in registers: a thread owns two neighbouring columns and runs down z, every
+// input slice loaded once (the windowed loop above reads each one 2R+1 times).  Both
+// voxels are packed as (v, 65535 - v), so one __vminu2 carries the min and the max.
+template <int R>
+__global__ void __launch_bounds__(128) k_mm_z_stream(const Sub *subs, uint32_t *mm) {
+  constexpr int L = 2 * R + 1;
+  const Sub S = subs[blockIdx.y];
+  const int64_t plane = (int64_t)S.W * S.H;
+  const int64_t p = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * 2;
+  if (p >= plane) return;
+  const int D = S.D, dv = S.depth_valid;
+  const uint16_t *col = S.src + p;
+  uint32_t *oc = mm + S.vox + p;
+  auto ld = [&](int z) -> uint2 {
+    z = clampi(z, 0, D - 1);
+    if (z >= dv) return make_uint2(kZeroPacked, kZeroPacked);
+    const uint32_t v = __ldg(reinterpret_cast<const uint32_t *>(col + (int64_t)z * plane));
+    return make_uint2(__byte_perm(v, ~v, 0x5410), __byte_perm(v, ~v, 0x7632));
+  };
+  auto vmin = [](uint2 a, uint2 b) { return make_uint2(__vminu2(a.x, b.x), __vminu2(a.y, b.y)); };
+  uint2 suf[L], cur[L];
+#pragma unroll
+  for (int j = 0; j < L; j++) suf[j] = ld(j - R);
+#pragma unroll
+  for (int j = L - 2; j >= 0; j--) suf[j] = vmin(suf[j], suf[j + 1]);
+  for (int t0 = 0; t0 < D; t0 += L) {
+#pragma unroll
+    for (int j = 0; j < L; j++) cur[j] = ld(t0 - R + L + j);
+    uint2 pre = make_uint2(0xFFFFFFFFu, 0xFFFFFFFFu);
+#pragma unroll
+    for (int i = 0; i < L; i++) {
+      const uint2 m = i == 0 ? suf[0] : vmin(suf[i], pre);
+      if (t0 + i < D) *reinterpret_cast<uint2 *>(oc + (int64_t)(t0 + i) * plane) = m;
+      pre = vmin(pre, cur[i]);
+    }
+    suf[L - 1] = cur[L - 1];
+#pragma unroll
+    for (int j = L - 2; j >= 0; j--) suf[j] = vmin(cur[j], suf[j + 1]);
+  }
+}
+
 // Van Herk / Gil-Werman over blocks of L entries of a smem line: g = running min from
 // each block's start (written to G), h = running min to each block's end (written over
 // A).  The window [t, t + L - 1] is then min(h[t], g[t + L - 1]).
@@ -604,7 +646,10 @@ static void allow_smem(F *fn, size_t bytes) {
 
 template <int BORDER>
 static void mm_z(const Sub *d_subs, int nsub, int plane, int rz, bool vec4, uint32_t *mm, cudaStream_t s) {
-  if (vec4) {
+  if (BORDER == 0 && vec4 && rz == 5) {
+    dim3 grid(ceil_div(plane / 2, 128), nsub);
+    KLAUNCH("k_mm_z", s, (k_mm_z_stream<5><<<grid, 128, 0, s>>>(d_subs, mm)));
+  } else if (vec4) {
     dim3 grid(ceil_div(plane / 4, 256), nsub);
     KLAUNCH("k_mm_z", s, (k_mm_z<BORDER, 4><<<grid, 256, 0, s>>>(d_subs, rz, mm)));
   } else {
