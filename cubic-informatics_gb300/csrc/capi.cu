@@ -531,16 +531,16 @@ static void enqueue_dog(hdog_ctx *c, int nsub, const float *norm, float *dog, cu
 // The chain after normalization: DoG + Hessian (fused sweep or separate passes), CCL,
 // region numbering and accumulation, features and record compaction.
 static void enqueue_after_norm(hdog_ctx *c, int nsub, bool fused, cudaStream_t st) {
+  // each foreground entry's voxel index, then its root (written by the CCL flatten), per
+  // entry beside the list (fb is free after the normalization)
+  int32_t *fg_root = reinterpret_cast<int32_t *>(c->fb);
   if (fused) {
-    launch_dog_hess(c->d_subs, nsub, c->W, c->H, c->D, c->taps, c->norm, c->dog, c->mask, c->fg, c->fg_count,
-                    c->status, st);
+    launch_dog_hess(c->d_subs, nsub, c->W, c->H, c->D, c->taps, c->norm, c->dog, c->mask, c->fg, fg_root,
+                    c->fg_count, c->status, st);
   } else {
     enqueue_dog(c, nsub, c->norm, c->dog, st);
     launch_hessian_pd(c->d_subs, nsub, c->W, c->H, c->D, c->dog, c->mask, nullptr, st);
   }
-  // each foreground entry's root, per entry beside the list (fb is free after the
-  // normalization)
-  int32_t *fg_root = reinterpret_cast<int32_t *>(c->fb);
   launch_ccl(c->d_subs, nsub, c->W, c->H, c->D, c->nvox, c->mask, c->labels, c->edges, c->edge_count, c->root_bits,
              c->blk_counts, c->status, c->num_sms, st, fused ? c->fg : nullptr, fused ? c->fg_count : nullptr,
              c->fg_cap, c->nblk, fg_root);

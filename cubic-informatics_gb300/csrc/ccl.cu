@@ -657,12 +657,14 @@ __global__ void __launch_bounds__(256) k_ccl_flatten(const Sub *subs, uint8_t *m
 
 // The same pass over the fused sweep's foreground list instead of the whole volume (the list
 // holds every foreground voxel but voxel 0): root bits and block counts start at zero and
-// each root sets its own bit and counts itself.  A substack whose list overflowed is
+// each root sets its own bit and counts itself.  fg_root holds each entry's voxel index
+// (written by the sweep beside the 32-byte entry, so that this pass reads 4 bytes per
+// entry) and is overwritten with the entry's root.  A substack whose list overflowed is
 // skipped; its batch is redone with the separate passes.
 constexpr int kFlatFgPerThread = 8;
 
-__global__ void __launch_bounds__(256) k_ccl_flatten_fg(const Sub *subs, const FgEntry *fg,
-                                                       const unsigned long long *fg_count, int32_t *labels,
+__global__ void __launch_bounds__(256) k_ccl_flatten_fg(const Sub *subs, const unsigned long long *fg_count,
+                                                       int32_t *labels,
                                                        uint32_t *root_bits, uint32_t *blk_counts, int32_t *fg_root,
                                                        int *status) {
   const Sub S = subs[blockIdx.y];
@@ -670,8 +672,6 @@ __global__ void __launch_bounds__(256) k_ccl_flatten_fg(const Sub *subs, const F
   if (cnt > S.fg_cap) return;
   const int64_t n = (int64_t)S.W * S.H * S.D;
   int32_t *L = labels + S.vox;
-  const int32_t *ent = reinterpret_cast<const int32_t *>(fg + S.fg);   // idx is each entry's first word
-  constexpr int kWords = (int)(sizeof(FgEntry) / sizeof(int32_t));
   // a warp takes 32 * kFlatFgPerThread consecutive entries, lane l every 32nd from l, so each
   // load and store of the warp covers 32 consecutive entries
   const int lane = threadIdx.x & 31;
@@ -682,7 +682,7 @@ __global__ void __launch_bounds__(256) k_ccl_flatten_fg(const Sub *subs, const F
     // level by level: the entries' voxels, their labels, the labels' parents
     int32_t idx[kFlatFgPerThread], l[kFlatFgPerThread], p[kFlatFgPerThread];
 #pragma unroll
-    for (int k = 0; k < kFlatFgPerThread; k++) idx[k] = e0 + 32 * k < cnt ? __ldg(ent + (e0 + 32 * k) * kWords) : -1;
+    for (int k = 0; k < kFlatFgPerThread; k++) idx[k] = e0 + 32 * k < cnt ? fg_root[S.fg + e0 + 32 * k] : -1;
 #pragma unroll
     for (int k = 0; k < kFlatFgPerThread; k++) l[k] = idx[k] >= 0 ? __ldcg(L + idx[k]) : -1;
 #pragma unroll
@@ -723,7 +723,7 @@ void launch_ccl(const Sub *d_subs, int nsub, int max_w, int max_h, int max_d, in
     const int64_t want = std::min((int64_t)ceil_div(max_fg, 256 * kFlatFgPerThread),
                                   (int64_t)(8 * num_sms / (nsub > 0 ? nsub : 1) + 1));
     KLAUNCH("k_ccl_flatten", s, (k_ccl_flatten_fg<<<dim3((unsigned)std::max<int64_t>(want, 1), nsub), 256, 0, s>>>(
-                                    d_subs, fg, fg_count, labels, root_bits, blk_counts, fg_root, d_status)));
+                                    d_subs, fg_count, labels, root_bits, blk_counts, fg_root, d_status)));
   } else {
     KLAUNCH("k_ccl_flatten", s, (k_ccl_flatten<false><<<dim3(ceil_div(max_n, kScanBlock), nsub), 256, 0, s>>>(
                                     d_subs, const_cast<uint8_t *>(mask), labels, root_bits, blk_counts, d_status)));

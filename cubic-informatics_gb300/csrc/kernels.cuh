@@ -108,8 +108,8 @@ bool launch_dog_sweep(const Sub *d_subs, int nsub, int W, int H, int D, const Do
 // DoG + Hessian + PD: the radius-specialised pair (norm -> dog -> mask + list) when the tap
 // radii have an instantiation, else the generic fused sweep (dog untouched).
 int launch_dog_hess(const Sub *d_subs, int nsub, int W, int H, int D, const DogTaps &T, const float *norm,
-                    float *dog, uint8_t *mask, FgEntry *fg, unsigned long long *fg_count, int *d_status,
-                    cudaStream_t s);
+                    float *dog, uint8_t *mask, FgEntry *fg, int32_t *fg_idx, unsigned long long *fg_count,
+                    int *d_status, cudaStream_t s);
 // ---- ccl.cu ----
 // Segments of a per-substack scan: substack s scans len[s] counts starting at off[s];
 // chk[s] is its offset in the chunk-sum scratch (one slot per 1024 counts).

@@ -54,7 +54,8 @@ __device__ __forceinline__ void tma_slice(const CUtensorMap *map, float *dst, ui
 template <int RZ>
 __global__ void __launch_bounds__(kSweepThreads, 1)
     k_dog_hess(const __grid_constant__ CUtensorMap map, const __grid_constant__ DogTaps T, const Sub *subs,
-               const float *norm, uint8_t *mask, FgEntry *fg, unsigned long long *fg_count, int *status) {
+               const float *norm, uint8_t *mask, FgEntry *fg, int32_t *fg_idx, unsigned long long *fg_count,
+               int *status) {
   constexpr int WIN = 2 * RZ + 1;
   extern __shared__ __align__(128) unsigned char smem[];
   const Sub S = subs[blockIdx.y];
@@ -287,6 +288,7 @@ __global__ void __launch_bounds__(kSweepThreads, 1)
           const float4 *src = reinterpret_cast<const float4 *>(&e);
           dst[0] = src[0];
           dst[1] = src[1];
+          fg_idx[S.fg + base] = (int32_t)idx[u];
         }
         base++;
       }
@@ -552,7 +554,7 @@ __device__ __forceinline__ float hdiff(float plus, float minus) { return __fmul_
 
 __global__ void __launch_bounds__(kHThreads, 6)
     k_hess_sweep(const __grid_constant__ CUtensorMap map, const __grid_constant__ CUtensorMap nmap, const Sub *subs,
-                 uint8_t *mask, FgEntry *fg, unsigned long long *fg_count, int *status) {
+                 uint8_t *mask, FgEntry *fg, int32_t *fg_idx, unsigned long long *fg_count, int *status) {
   extern __shared__ __align__(128) unsigned char smem[];
   constexpr int PL = kHPX * kHPY;
   constexpr uint32_t tma_bytes = (uint32_t)(PL * 4);
@@ -786,6 +788,7 @@ __global__ void __launch_bounds__(kHThreads, 6)
         float4 *dst = reinterpret_cast<float4 *>(fg + S.fg + base);
         dst[0] = make_float4(__int_as_float(i0 + o), nslice[ly * kHTX + 4 * q + o], hv[o][0], hv[o][1]);
         dst[1] = make_float4(hv[o][2], hv[o][3], hv[o][4], hv[o][5]);
+        fg_idx[S.fg + base] = i0 + o;
       }
       base++;
     }
@@ -872,8 +875,8 @@ bool launch_dog_sweep(const Sub *d_subs, int nsub, int W, int H, int D, const Do
 }
 
 int launch_dog_hess(const Sub *d_subs, int nsub, int W, int H, int D, const DogTaps &T, const float *norm,
-                    float *dog, uint8_t *mask, FgEntry *fg, unsigned long long *fg_count, int *d_status,
-                    cudaStream_t s) {
+                    float *dog, uint8_t *mask, FgEntry *fg, int32_t *fg_idx, unsigned long long *fg_count,
+                    int *d_status, cudaStream_t s) {
   const int rxy = max(T.r[0], T.r[2]), rz = max(T.r[1], T.r[3]);
   zero_async(fg_count, (size_t)nsub * kFgCountStride * sizeof(unsigned long long), s);
   const SweepInst *si = find_inst(T);
@@ -889,7 +892,7 @@ int launch_dog_hess(const Sub *d_subs, int nsub, int W, int H, int D, const DogT
     const unsigned tiles_h = ceil_div(W, kHTX) * ceil_div(H, kHTY);
     cudaFuncSetAttribute(k_hess_sweep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kHessSmem);
     KLAUNCH("k_hess_sweep", s, (k_hess_sweep<<<dim3(tiles_h, nsub), kHThreads, kHessSmem, s>>>(
-                                   map_d, map_t, d_subs, mask, fg, fg_count, d_status)));
+                                   map_d, map_t, d_subs, mask, fg, fg_idx, fg_count, d_status)));
     return 0;
   }
   CUtensorMap map;
@@ -899,11 +902,11 @@ int launch_dog_hess(const Sub *d_subs, int nsub, int W, int H, int D, const DogT
   if (rz <= 5) {
     cudaFuncSetAttribute(k_dog_hess<5>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     KLAUNCH("k_dog_hess", s, (k_dog_hess<5><<<dim3(tiles, nsub), kSweepThreads, smem, s>>>(
-                                 map, T, d_subs, norm, mask, fg, fg_count, d_status)));
+                                 map, T, d_subs, norm, mask, fg, fg_idx, fg_count, d_status)));
   } else {
     cudaFuncSetAttribute(k_dog_hess<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     KLAUNCH("k_dog_hess", s, (k_dog_hess<8><<<dim3(tiles, nsub), kSweepThreads, smem, s>>>(
-                                 map, T, d_subs, norm, mask, fg, fg_count, d_status)));
+                                 map, T, d_subs, norm, mask, fg, fg_idx, fg_count, d_status)));
   }
   return 0;
 }
