@@ -322,7 +322,6 @@ constexpr int kHPX = kHTX + 8;          // Hessian ring row: columns x0-4 .. x0+
 constexpr int kHPY = kHTY + 4;
 constexpr int kHRing = 8;              // ring slots; a slot is 72 x 20 floats = 45 x 128 bytes
 constexpr int kHThreads = kHTX / 4 * kHTY;   // one x quad per thread
-constexpr int kNRing = 4;                     // normalized-slice slots of the Hessian sweep
 
 template <int RA, int RB, int ZA, int ZB>
 struct DogT {
@@ -553,39 +552,29 @@ __global__ void __launch_bounds__(DogT<RA, RB, ZA, ZB>::NT, 2)
 __device__ __forceinline__ float hdiff(float plus, float minus) { return __fmul_rn(__fsub_rn(plus, minus), 0.5f); }
 
 __global__ void __launch_bounds__(kHThreads, 6)
-    k_hess_sweep(const __grid_constant__ CUtensorMap map, const __grid_constant__ CUtensorMap nmap, const Sub *subs,
-                 uint8_t *mask, FgEntry *fg, int32_t *fg_idx, unsigned long long *fg_count, int *status) {
+    k_hess_sweep(const __grid_constant__ CUtensorMap map, const Sub *subs, const float *norm, uint8_t *mask,
+                 FgEntry *fg, int32_t *fg_idx, unsigned long long *fg_count, int *status) {
   extern __shared__ __align__(128) unsigned char smem[];
   constexpr int PL = kHPX * kHPY;
   constexpr uint32_t tma_bytes = (uint32_t)(PL * 4);
-  constexpr uint32_t ntma_bytes = (uint32_t)(kHTX * kHTY * 4);
   const Sub S = subs[blockIdx.y];
   const int ntx = (S.W + kHTX - 1) / kHTX, nty = (S.H + kHTY - 1) / kHTY;
   if ((int64_t)blockIdx.x >= (int64_t)ntx * nty) return;
   const int x0 = (int)(blockIdx.x % ntx) * kHTX, y0 = (int)(blockIdx.x / ntx) * kHTY;
   float *ring = reinterpret_cast<float *>(smem);
-  // normalized values of the tile's slice zh (the foreground list carries them), kNRing slots
-  float *nring = reinterpret_cast<float *>(smem + (size_t)kHRing * PL * 4);
-  uint64_t *bar = reinterpret_cast<uint64_t *>(smem + (size_t)kHRing * PL * 4 + (size_t)kNRing * kHTX * kHTY * 4);
-  uint64_t *nbar = bar + kHRing;
-  // done[zh % kHRing] completes when every warp has finished iteration zh: its last reads
-  // of DoG slice zh-2 and of normalized slice zh
-  uint64_t *done = nbar + kNRing;
+  uint64_t *bar = reinterpret_cast<uint64_t *>(smem + (size_t)kHRing * PL * 4);
+  // done[zh % kHRing] completes when every warp has finished iteration zh, with its last
+  // reads of DoG slice zh-2
+  uint64_t *done = bar + kHRing;
   const int t = threadIdx.x;
   const int D = S.D, W = S.W, H = S.H;
   const int32_t WH = W * H;
   if (t == 0) {
     for (int i = 0; i < kHRing; i++) mbar_init(&bar[i], 1);
-    for (int i = 0; i < kNRing; i++) mbar_init(&nbar[i], 1);
     for (int i = 0; i < kHRing; i++) mbar_init(&done[i], kHThreads / 32);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
-  // normalized slice z -> slot z % kNRing, use z / kNRing; slices 0 .. 2 up front, then
-  // slice zh + 3 while slice zh is tested (its slot held slice zh - 1, read one barrier earlier)
-  if (t == 0)
-    for (int z = 0; z < 3 && z < D; z++)
-      tma_slice(&nmap, nring + (z % kNRing) * kHTX * kHTY, &nbar[z % kNRing], x0, y0, z, blockIdx.y, ntma_bytes);
   const int tx = x0 - 4, ty = y0 - 2;
   // ring slot of DoG slice z (z = -2 .. D+1; slices outside the volume arrive zero-filled)
   auto slot = [](int z) { return (z + 2 * kHRing) % kHRing; };
@@ -606,19 +595,15 @@ __global__ void __launch_bounds__(kHThreads, 6)
   const int X0 = x0 + 4 * q, Y = y0 + ly;
   const int b = (ly + 2) * kHPX + 4 * q;   // ring index of column X0 - 4 on row Y
   for (int zh = 0; zh < D; zh++) {
-    // DoG slice zh+5 reuses the slot of slice zh-3 and normalized slice zh+3 the slot of
-    // slice zh-1, both read for the last time in iteration zh-1: the producer waits until
-    // every warp is past it (warps otherwise run up to the ring's depth apart)
-    if (t == 0 && ok && (zh + 5 <= D + 1 || zh + 3 < D)) {
+    // DoG slice zh+5 reuses the slot of slice zh-3, read for the last time in iteration
+    // zh-1: the producer waits until every warp is past it (warps otherwise run up to the
+    // ring's depth apart)
+    if (t == 0 && ok && zh + 5 <= D + 1) {
       if (zh >= 1 && !mbar_wait(&done[(zh - 1) % kHRing], ((zh - 1) / kHRing) & 1)) {
         ok = false;
         atomicExch(status, HDOG_ERR_TIMEOUT);
       }
-      if (ok && zh + 5 <= D + 1)
-        tma_slice(&map, ring + slot(zh + 5) * PL, &bar[slot(zh + 5)], tx, ty, zh + 5, blockIdx.y, tma_bytes);
-      if (ok && zh + 3 < D)
-        tma_slice(&nmap, nring + ((zh + 3) % kNRing) * kHTX * kHTY, &nbar[(zh + 3) % kNRing], x0, y0, zh + 3,
-                  blockIdx.y, ntma_bytes);
+      if (ok) tma_slice(&map, ring + slot(zh + 5) * PL, &bar[slot(zh + 5)], tx, ty, zh + 5, blockIdx.y, tma_bytes);
     }
     // slices zh-2 .. zh+1 were waited for already; zh+2 is new
     if (ok && !mbar_wait(&bar[slot(zh + 2)], use(zh + 2) & 1)) {
@@ -765,12 +750,12 @@ __global__ void __launch_bounds__(kHThreads, 6)
         nfg += fgv[o];
       }
     }
-    // warp-aggregated append to the foreground list (every lane of the block takes part)
-    if (ok && !mbar_wait(&nbar[zh % kNRing], (zh / kNRing) & 1)) {
-      ok = false;
-      atomicExch(status, HDOG_ERR_TIMEOUT);
-    }
-    const float *nslice = nring + (zh % kNRing) * kHTX * kHTY;
+    // warp-aggregated append to the foreground list (every lane of the block takes part).
+    // The normalized values of the quad (one 16-byte load, W % 4 == 0) are read only by
+    // threads with foreground, before the slot reservation so that the two latencies
+    // overlap.
+    const float4 nq = nfg ? __ldg(reinterpret_cast<const float4 *>(norm + S.vox + i0)) : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float nv[4] = {nq.x, nq.y, nq.z, nq.w};
     const int lane = t & 31;
     int incl = nfg;
     for (int dd = 1; dd < 32; dd <<= 1) {
@@ -786,7 +771,7 @@ __global__ void __launch_bounds__(kHThreads, 6)
       if (!fgv[o]) continue;
       if ((int64_t)base < S.fg_cap) {
         float4 *dst = reinterpret_cast<float4 *>(fg + S.fg + base);
-        dst[0] = make_float4(__int_as_float(i0 + o), nslice[ly * kHTX + 4 * q + o], hv[o][0], hv[o][1]);
+        dst[0] = make_float4(__int_as_float(i0 + o), nv[o], hv[o][0], hv[o][1]);
         dst[1] = make_float4(hv[o][2], hv[o][3], hv[o][4], hv[o][5]);
         fg_idx[S.fg + base] = i0 + o;
       }
@@ -837,7 +822,7 @@ static const SweepInst *find_inst(const DogTaps &T) {
 }
 
 static constexpr size_t kHessSmem =
-    (size_t)kHRing * kHPX * kHPY * 4 + (size_t)kNRing * kHTX * kHTY * 4 + (2 * kHRing + kNRing) * 8;
+    (size_t)kHRing * kHPX * kHPY * 4 + (2 * kHRing) * 8;
 static_assert((kHPX * kHPY * 4) % 128 == 0, "TMA ring slots must start on 128-byte boundaries");
 
 // Whether the fused sweep handles these parameters (else the separate passes run).
@@ -881,10 +866,9 @@ int launch_dog_hess(const Sub *d_subs, int nsub, int W, int H, int D, const DogT
   zero_async(fg_count, (size_t)nsub * kFgCountStride * sizeof(unsigned long long), s);
   const SweepInst *si = find_inst(T);
   if (si) {
-    CUtensorMap map_n, map_d, map_t;
+    CUtensorMap map_n, map_d;
     if (encode_map(&map_n, norm, W, H, D, nsub, si->bw, si->bh) != CUDA_SUCCESS) return -1;
     if (encode_map(&map_d, dog, W, H, D, nsub, kHPX, kHPY) != CUDA_SUCCESS) return -1;
-    if (encode_map(&map_t, norm, W, H, D, nsub, kHTX, kHTY) != CUDA_SUCCESS) return -1;
     const unsigned tiles_d = ceil_div(W, kDTX) * ceil_div(H, kDTY);
     cudaFuncSetAttribute(si->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)si->smem);
     KLAUNCH("k_dog_sweep", s, (si->fn<<<dim3(tiles_d, nsub), si->threads, si->smem, s>>>(map_n, T, d_subs, dog,
@@ -892,7 +876,7 @@ int launch_dog_hess(const Sub *d_subs, int nsub, int W, int H, int D, const DogT
     const unsigned tiles_h = ceil_div(W, kHTX) * ceil_div(H, kHTY);
     cudaFuncSetAttribute(k_hess_sweep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kHessSmem);
     KLAUNCH("k_hess_sweep", s, (k_hess_sweep<<<dim3(tiles_h, nsub), kHThreads, kHessSmem, s>>>(
-                                   map_d, map_t, d_subs, mask, fg, fg_idx, fg_count, d_status)));
+                                   map_d, d_subs, norm, mask, fg, fg_idx, fg_count, d_status)));
     return 0;
   }
   CUtensorMap map;
