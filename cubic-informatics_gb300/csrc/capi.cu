@@ -218,6 +218,7 @@ struct hdog_ctx {
   unsigned long long *edge_count = nullptr;
   FgEntry *fg = nullptr;
   unsigned long long *fg_count = nullptr;
+  unsigned long long *fg_count_packed = nullptr;
   RegionAcc acc{};
   RegionOut out{};
   hdog_record *records = nullptr;
@@ -305,6 +306,7 @@ static void plan(const hdog_params *p, int max_sub, int64_t &nvox, int64_t &reg_
   L.add(S * sizeof(unsigned long long));     // 29 edge counts
   L.add(S * fg_capacity(nvox) * sizeof(FgEntry));         // 30 foreground list
   L.add(S * kFgCountStride * sizeof(unsigned long long));   // 31 foreground counts (strided)
+  L.add(S * sizeof(unsigned long long));     // 32 foreground counts, packed for the read-back
 }
 
 extern "C" int hdog_ctx_bytes(const hdog_params *p, int max_substacks, size_t *bytes) {
@@ -398,6 +400,7 @@ extern "C" int hdog_ctx_create(const hdog_params *p, int max_substacks, hdog_ctx
   c->edge_cap = edge_capacity(c->nvox);
   c->fg = (FgEntry *)at(30);
   c->fg_count = (unsigned long long *)at(31);
+  c->fg_count_packed = (unsigned long long *)at(32);
   c->fg_cap = fg_capacity(c->nvox);
   cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->dev);
   cudaDeviceGetAttribute(&c->max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->dev);
@@ -570,8 +573,11 @@ static int readback(hdog_ctx *c, int nsub, cudaStream_t st) {
   HDOG_CUDA_TRY(cudaGetLastError());
   HDOG_CUDA_TRY(cudaMemcpyAsync(c->h_counts, c->num_records, nsub * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
   HDOG_CUDA_TRY(cudaMemcpyAsync(c->h_counts + ms, c->num_regions, nsub * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
-  HDOG_CUDA_TRY(cudaMemcpy2DAsync(c->h_counts + 2 * ms, sizeof(int64_t), c->fg_count, kFgCountStride * sizeof(int64_t),
-                                  sizeof(int64_t), nsub, cudaMemcpyDeviceToHost, st));
+  // a strided (2D) copy could wait on the copy engine behind a host stack's chunks, so the
+  // counters are packed on the device first
+  pack_fg_counts_async(c->fg_count, nsub, c->fg_count_packed, st);
+  HDOG_CUDA_TRY(cudaMemcpyAsync(c->h_counts + 2 * ms, c->fg_count_packed, nsub * sizeof(int64_t), cudaMemcpyDeviceToHost,
+                                st));
   HDOG_CUDA_TRY(cudaMemcpyAsync(c->h_counts + 3 * ms, c->status, sizeof(int), cudaMemcpyDeviceToHost, st));
   HDOG_CUDA_TRY(cudaStreamSynchronize(st));
   const int status = *(int *)(c->h_counts + 3 * ms);

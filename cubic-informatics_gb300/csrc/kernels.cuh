@@ -102,6 +102,7 @@ int soft_backward(const hdog_soft_params *p, const float *vol, const int32_t *po
 
 // Zero `bytes` (a multiple of 4) of device memory on stream s with a kernel.
 void zero_async(void *p, size_t bytes, cudaStream_t s);
+void pack_fg_counts_async(const unsigned long long *fg_count, int nsub, unsigned long long *packed, cudaStream_t s);
 
 bool launch_dog_sweep(const Sub *d_subs, int nsub, int W, int H, int D, const DogTaps &T, const float *norm,
                       float *dog, int *d_status, int max_smem, cudaStream_t s);

@@ -483,6 +483,19 @@ void zero_async(void *p, size_t bytes, cudaStream_t s) {
                                static_cast<uint32_t *>(p), n)));
 }
 
+// The substacks' list counters (kFgCountStride apart) into consecutive slots, for one
+// plain device-to-host copy.
+__global__ void k_pack_fg_counts(const unsigned long long *fg_count, int nsub, unsigned long long *packed) {
+  for (int i = (int)(blockIdx.x * blockDim.x + threadIdx.x); i < nsub; i += (int)(gridDim.x * blockDim.x))
+    packed[i] = fg_count[(int64_t)i * kFgCountStride];
+}
+
+void pack_fg_counts_async(const unsigned long long *fg_count, int nsub, unsigned long long *packed, cudaStream_t s) {
+  if (nsub > 0)
+    KLAUNCH("k_pack_fg_counts", s, (k_pack_fg_counts<<<std::min<unsigned>(ceil_div(nsub, 256), 64u), 256, 0, s>>>(
+                                       fg_count, nsub, packed)));
+}
+
 // ------------------------------------------------------------------ launchers
 void launch_scan(const ScanSeg &sg, int nsub, const uint32_t *in, uint32_t *out, uint32_t *chunk,
                  int64_t *totals, int64_t add, cudaStream_t s) {
