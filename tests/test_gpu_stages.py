@@ -27,6 +27,9 @@ CASES = {
     # substack shallower than the z window
     "ragged_r20_203x150x19": (203, 150, 19, {}),
     "shallow_r20_64x40x6": (64, 40, 6, {}),
+    # the streaming z min/max (r_z 5, W*H a multiple of 4) on 3 and 7 slices
+    "shallow_r20_48x32x3": (48, 32, 3, {}),
+    "odd_depth_r20_96x24x7": (96, 24, 7, {}),
 }
 
 
