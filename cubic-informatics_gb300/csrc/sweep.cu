@@ -312,7 +312,10 @@ __global__ void __launch_bounds__(kSweepThreads, 1)
 //                 included, so the volume equals the separate passes bit for bit.
 //   k_hess_sweep  DoG -> mask + foreground list.  A block owns a kHTX x kHTY tile; DoG slices
 //                 (tile + 2-voxel halo, zero outside the volume) arrive by TMA into an
-//                 8-slot ring, up to five slices ahead; each thread tests one x quad.
+//                 8-slot ring, up to five slices ahead; each thread tests one x quad.  No
+//                 block barrier per slice: warps release ring slots through mbarriers.
+//                 The normalized values the list carries are read from global memory by
+//                 the threads whose quad has foreground.
 //
 // The split costs one write and one read of the DoG volume but frees the Hessian stage
 // from the z shift register's registers, so several Hessian blocks share an SM.
@@ -320,7 +323,7 @@ constexpr int kDTX = 32, kDTY = 16;     // DoG tile (two blocks per SM)
 constexpr int kHTX = 32, kHTY = 16;     // Hessian tile (six blocks per SM)
 constexpr int kHPX = kHTX + 8;          // Hessian ring row: columns x0-4 .. x0+kHTX+3 (16-byte aligned start)
 constexpr int kHPY = kHTY + 4;
-constexpr int kHRing = 8;              // ring slots; a slot is 72 x 20 floats = 45 x 128 bytes
+constexpr int kHRing = 8;              // ring slots; a slot is 40 x 20 floats = 25 x 128 bytes
 constexpr int kHThreads = kHTX / 4 * kHTY;   // one x quad per thread
 
 template <int RA, int RB, int ZA, int ZB>
