@@ -89,7 +89,8 @@ def test_gpu_forward_and_adjoint_match_reference(reference):
     loss = hdog.soft.soft_loss(v, s, torch.tensor(pos, device="cuda"), torch.tensor(neg, device="cuda"),
                                radius_norm_xy=RXY, radius_norm_z=RZ, min_intensity=MIN_INT, tau=tau)
     loss.backward()
-    assert abs(float(loss) - L) <= 1e-5 * abs(L), (float(loss), L)
+    lv = float(loss.detach())
+    assert abs(lv - L) <= 1e-5 * abs(L), (lv, L)
     g_s = s.grad.numpy().astype(np.float64)
     assert np.all(np.abs(g_s - gs) <= 1e-4 * np.abs(gs) + 1e-9), (g_s, gs)
     g_v = v.grad.cpu().numpy().astype(np.float64)
