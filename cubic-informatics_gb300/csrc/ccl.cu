@@ -661,7 +661,7 @@ __global__ void __launch_bounds__(256) k_ccl_flatten(const Sub *subs, uint8_t *m
 // (written by the sweep beside the 32-byte entry, so that this pass reads 4 bytes per
 // entry) and is overwritten with the entry's root.  A substack whose list overflowed is
 // skipped; its batch is redone with the separate passes.
-constexpr int kFlatFgPerThread = 8;
+constexpr int kFlatFgPerThread = 16;
 
 __global__ void __launch_bounds__(256) k_ccl_flatten_fg(const Sub *subs, const unsigned long long *fg_count,
                                                        int32_t *labels,
