@@ -84,5 +84,5 @@ def fit_sigmas(vol, pos, neg, sigma0, steps=20, lr=0.05, **kw):
         opt.step()
         with torch.no_grad():
             sigma.clamp_(min=0.3)
-        history.append(float(loss))
+        history.append(float(loss.detach()))
     return sigma.detach(), history
