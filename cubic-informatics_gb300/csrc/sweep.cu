@@ -319,7 +319,7 @@ __global__ void __launch_bounds__(kSweepThreads, 1)
 //
 // The split costs one write and one read of the DoG volume but frees the Hessian stage
 // from the z shift register's registers, so several Hessian blocks share an SM.
-constexpr int kDTX = 32, kDTY = 16;     // DoG tile (two blocks per SM)
+constexpr int kDTX = 32, kDTY = 16;     // DoG tile (three 256-thread blocks per SM, 80 registers)
 constexpr int kHTX = 32, kHTY = 16;     // Hessian tile (six blocks per SM)
 constexpr int kHPX = kHTX + 8;          // Hessian ring row: columns x0-4 .. x0+kHTX+3 (16-byte aligned start)
 constexpr int kHPY = kHTY + 4;
@@ -455,7 +455,7 @@ __device__ __forceinline__ void unroll_steps(F &f, int base, int limit) {
 }
 
 template <int RA, int RB, int ZA, int ZB>
-__global__ void __launch_bounds__(DogT<RA, RB, ZA, ZB>::NT, 2)
+__global__ void __launch_bounds__(DogT<RA, RB, ZA, ZB>::NT, 3)
     k_dog_sweep(const __grid_constant__ CUtensorMap map, const __grid_constant__ DogTaps T, const Sub *subs,
                 float *dog, int *status) {
   using C = DogT<RA, RB, ZA, ZB>;
