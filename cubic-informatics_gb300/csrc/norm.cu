@@ -294,7 +294,7 @@ __global__ void __launch_bounds__(256) k_mm_x(const Sub *subs, int r, int ry, in
 // y pass: one thread per (column, segment of rows) of a slice; a warp reads 32
 // consecutive columns of a row per load.
 template <int R, int BORDER>
-__global__ void __launch_bounds__(128) k_mm_y_stream(const Sub *subs, int seg, const uint32_t *in, uint32_t *out) {
+__global__ void __launch_bounds__(128, 8) k_mm_y_stream(const Sub *subs, int seg, const uint32_t *in, uint32_t *out) {
   constexpr int L = 2 * R + 1;
   const Sub S = subs[blockIdx.z];
   const int W = S.W, H = S.H;
