@@ -20,6 +20,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -66,11 +67,10 @@ class ClockSampler:
     def __init__(self, index):
         self.index = index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", "clocks_rank%d.csv" % index)
+        self.path = os.path.join(tempfile.gettempdir(), "hdog_bench_clocks_%d_rank%d.csv" % (os.getpid(), index))
 
     def __enter__(self):
         try:
-            os.makedirs(os.path.dirname(self.path), exist_ok=True)
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
                                           "--format=csv,noheader,nounits", "-lms", "200"],
@@ -162,49 +162,87 @@ def max_over_ranks(x, dist):
     return float(t.item())
 
 
+def _oracle_params():
+    """The workload's parameters as the oracle's struct (no call into libhdog)."""
+    from types import SimpleNamespace
+    from oracle import oracle as orc
+    return orc.params_from(SimpleNamespace(**PARAMS))
+
+
+def _cpu_sample(vol, nsample):
+    """The first `nsample` substacks of the stack's schedule, zero tail applied, and the
+    unique input voxels they stand for (stack voxels x nsample / all substacks)."""
+    from oracle import oracle as orc
+    op = _oracle_params()
+    z0s = orc.schedule(L, DEPTH, orc.depth_margin(op))
+    subs = []
+    for z0 in z0s[:nsample]:
+        sub = np.zeros((DEPTH, H, W), np.uint16)
+        dv = min(DEPTH, L - z0)
+        sub[:dv] = vol[z0:z0 + dv]
+        subs.append((z0, dv, sub))
+    return op, subs, W * H * L * len(subs) / len(z0s), len(z0s)
+
+
+def _run_cpu_sample(op, subs):
+    from oracle import oracle as orc
+    for z0, dv, sub in subs:
+        orc.substack(op, sub, dv, z0)
+
+
 def cpu_baseline(vol, steps=1, nsample=4):
     """The CPU oracle on the first `nsample` substacks of the stack's schedule: a bounded
     sample of the same workload (about 10-15 s), on every host core its OpenMP parts use."""
-    import hdog
-    from oracle import oracle as orc
-    p = hdog.make_params(**PARAMS)
-    op = orc.params_from(p)
-    z0s = hdog.substack_schedule(L, DEPTH, hdog.depth_margin(p))[:nsample]
-    subs = [np.ascontiguousarray(vol[z0:z0 + DEPTH]) for z0 in z0s]
+    op, subs, unique, nall = _cpu_sample(vol, nsample)
     t = time.time()
     for _ in range(steps):
-        for z0, sub in zip(z0s, subs):
-            orc.substack(op, sub, sub.shape[0], z0)
+        _run_cpu_sample(op, subs)
     dt = (time.time() - t) / steps
-    nall = len(hdog.substack_schedule(L, DEPTH, hdog.depth_margin(p)))
-    unique = W * H * L * len(z0s) / nall
     return {"value": unique / dt / 1e9, "unit": "Gvox/s", "cores": os.cpu_count(), "kind": "port",
             "sample": "the first %d of the stack's %d 2560x2160x32 substacks, %.1f s; value over the unique input "
                       "voxels they stand for (stack voxels x %d/%d); OpenMP filter passes, single-thread CCL and "
-                      "region pass" % (len(z0s), nall, dt, len(z0s), nall)}
+                      "region pass" % (len(subs), nall, dt, len(subs), nall)}
 
 
 def run_reference(args):
+    """The reference's CPU implementation of the path (the oracle port of src/3D, built
+    from its C restatement; the reference's own executable needs a CUDA GPU and its host
+    part cannot be built for this Arm host) on the same workload.  A step is a bounded
+    sample of the stack: its first two substacks, through every stage and the records."""
     ws, rank, local = dist_env()
     if rank != 0:
         return 0
     vol, _ = make_stack()
+    op, subs, unique, nall = _cpu_sample(vol, 2)
     for _ in range(args.warmup):
-        pass   # the CPU port has no warm-up state; warm-up steps are not repeated work
+        _run_cpu_sample(op, subs)
     t = time.time()
-    base = None
     for _ in range(args.steps):
-        base = cpu_baseline(vol, steps=1)
-    total = time.time() - t
-    line = {"metric": METRIC, "impl": "reference", "value": base["value"], "unit": "Gvox/s",
+        _run_cpu_sample(op, subs)
+    step_s = (time.time() - t) / args.steps
+    value = unique / step_s / 1e9
+    sample = ("each step: the first %d of the stack's %d 2560x2160x32 substacks (%.1f s); value over the unique "
+              "input voxels they stand for (stack voxels x %d/%d); OpenMP filter passes, single-thread CCL and "
+              "region pass" % (len(subs), nall, step_s, len(subs), nall))
+    base = {"value": value, "unit": "Gvox/s", "cores": os.cpu_count(), "kind": "port", "sample": sample}
+    line = {"metric": METRIC, "impl": "reference", "value": value, "unit": "Gvox/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": total / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+            "ms_per_step": step_s * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "sample": base["sample"]},
+            "config": camera_config(args.gpus), "sample": sample,
             "cpu_baseline": base,
-            "e2e": {"value": base["value"], "unit": "Gvox/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "e2e": {"value": value, "unit": "Gvox/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
+
+
+def camera_config(n_gpus):
+    """The workload's description, the same for both arms."""
+    nsub = 8
+    return {"workload": WORKLOAD, "unique_voxels_per_step": W * H * L,
+            "processed_voxels_per_step": W * H * DEPTH * nsub,
+            "parallelism": "replicas" if n_gpus > 1 else "single GPU",
+            "l2": "inputs larger than L2 (%.2f GB uint16 stack per step, L2 129 MB)" % (W * H * L * 2 / 1e9)}
 
 
 def profile_case():
@@ -472,6 +510,7 @@ def main():
     nsub = len(hdog.substack_schedule(L, DEPTH, margin))
     unique = W * H * L
     processed = W * H * DEPTH * nsub
+    assert processed == camera_config(ws)["processed_voxels_per_step"]
 
     stack_dev = torch.from_numpy(vol).to(dev)
     host = torch.from_numpy(vol).pin_memory()
@@ -537,11 +576,9 @@ def main():
         "metric": METRIC, "value": value, "unit": "Gvox/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "mode": "batched: %d substacks per launch" % nsub,
-                   "unique_voxels_per_step": unique, "processed_voxels_per_step": processed,
-                   "records_per_step": n_records, "parallelism": "replicas" if ws > 1 else "single GPU",
-                   "l2": "inputs larger than L2 (%.2f GB uint16 stack per step, L2 129 MB)" % (unique * 2 / 1e9),
-                   "generator_s": round(gen_s, 1)},
+        "config": camera_config(ws),
+        "mode": "batched: %d substacks per launch" % nsub, "records_per_step": n_records,
+        "generator_s": round(gen_s, 1),
         "plain": {"value": plain_value, "ms_per_step": pms, "mode": "one substack per launch sequence"},
         "batched_over_plain": value / plain_value,
         "e2e": {"value": unique * ws / (e2e_ms * 1e-3) / 1e9, "unit": "Gvox/s",

@@ -846,6 +846,15 @@ static int run_stack_locked(hdog_ctx *c, const uint16_t *stack, int on_device, i
     starts.push_back(z0s.size());
   }
   const size_t nbatch = starts.size() - 1;
+  // on an early error return the chunk copies may still be reading the caller's host
+  // stack: wait for them, so the caller can free or reuse it once the call returns
+  struct CopyWait {
+    cudaStream_t st = nullptr;
+    bool armed = false;
+    ~CopyWait() {
+      if (armed) cudaStreamSynchronize(st);
+    }
+  } copy_wait;
   if (!on_device) {
     const size_t bytes = (size_t)length * plane * sizeof(uint16_t);
     if (bytes > c->stack_bytes) {
@@ -868,6 +877,8 @@ static int run_stack_locked(hdog_ctx *c, const uint16_t *stack, int on_device, i
     // the copies start after the work already queued on st (which may still read stack_buf)
     HDOG_CUDA_TRY(cudaEventRecord(c->start_ev, st));
     HDOG_CUDA_TRY(cudaStreamWaitEvent(c->copy_st, c->start_ev, 0));
+    copy_wait.st = c->copy_st;
+    copy_wait.armed = true;
     size_t z_done = 0;
     for (size_t b = 0; b < nbatch; b++) {
       const size_t last = starts[b + 1] - 1;
@@ -893,6 +904,7 @@ static int run_stack_locked(hdog_ctx *c, const uint16_t *stack, int on_device, i
     TRY(run_batch(c, nsub, st));
     TRY(collect_records(c, nsub, out, st));
   }
+  copy_wait.armed = false;   // every batch waited for its chunk, so the copies are done
   return HDOG_OK;
 }
 
@@ -1200,6 +1212,18 @@ extern "C" int hdog_ctx_set_option(hdog_ctx *c, int option, int value) {
       return HDOG_OK;
     default: return fail(HDOG_ERR_ARG, "unknown option");
   }
+}
+
+// ------------------------------------------------------------------ diagnostics
+extern "C" int hdog_ccl_edge_count(hdog_ctx *c, int64_t *edges, int64_t *capacity) {
+  if (!c || !edges || !capacity) return fail(HDOG_ERR_ARG, "hdog_ccl_edge_count: bad argument");
+  std::lock_guard<std::mutex> lock(c->mu);
+  HDOG_CUDA_TRY(cudaSetDevice(c->dev));
+  unsigned long long n = 0;
+  HDOG_CUDA_TRY(cudaMemcpy(&n, c->edge_count, sizeof(n), cudaMemcpyDeviceToHost));
+  *edges = (int64_t)n;
+  *capacity = c->edge_cap;
+  return HDOG_OK;
 }
 
 // ------------------------------------------------------------------ timing

@@ -35,23 +35,57 @@ static_assert(sizeof(Sub) <= kNaStatus, "descriptor slot too small");
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
-// Device address of g_noalloc_scratch, looked up once per device with that device
-// current (in host code the array's name is only a host-side stand-in).
+// Device address of g_noalloc_scratch (in host code the array's name is only a host-side
+// stand-in).  It is looked up with the device current, once per device context: the cache
+// keeps the context's id (cuCtxGetId, unique for the life of the process), so after a
+// cudaDeviceReset, which destroys the primary context and with it the module, the next
+// call looks the address up again in the new context.
+typedef int (*CtxGetCurrentFn)(void **);
+typedef int (*CtxGetIdFn)(void *, unsigned long long *);
 constexpr int kMaxDevices = 64;
-static void *g_scratch_addr[kMaxDevices];
+struct ScratchAddr {
+  unsigned long long ctx_id = 0;
+  void *addr = nullptr;
+};
+static ScratchAddr g_scratch_addr[kMaxDevices];
 static std::mutex g_scratch_mu;
+
+template <class F>
+static F driver_fn(const char *name) {
+  void *p = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  if (cudaGetDriverEntryPointByVersion(name, &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+      q != cudaDriverEntryPointSuccess)
+    return nullptr;
+  return reinterpret_cast<F>(p);
+}
+
+// Id of the calling thread's current context, 0 when it cannot be read.
+static unsigned long long current_ctx_id() {
+  static CtxGetCurrentFn get_current = driver_fn<CtxGetCurrentFn>("cuCtxGetCurrent");
+  static CtxGetIdFn get_id = driver_fn<CtxGetIdFn>("cuCtxGetId");
+  void *ctx = nullptr;
+  unsigned long long id = 0;
+  if (!get_current || !get_id || get_current(&ctx) != 0 || !ctx || get_id(ctx, &id) != 0) return 0;
+  return id;
+}
 
 static int scratch_for_current_device(unsigned char **out) {
   int dev = 0;
   HDOG_CUDA_TRY(cudaGetDevice(&dev));
   if (dev < 0 || dev >= kMaxDevices) return hdog_set_cuda_error(cudaErrorInvalidDevice, "hdog_ccl_noalloc: device id");
+  // makes the device's primary context current (created if need be), so its id can be read
+  HDOG_CUDA_TRY(cudaSetDevice(dev));
+  const unsigned long long id = current_ctx_id();
   std::lock_guard<std::mutex> lock(g_scratch_mu);
-  if (!g_scratch_addr[dev]) {
+  ScratchAddr &c = g_scratch_addr[dev];
+  if (id == 0 || c.ctx_id != id || !c.addr) {
     void *p = nullptr;
     HDOG_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_scratch));
-    g_scratch_addr[dev] = p;
+    c.addr = p;
+    c.ctx_id = id;   // 0: the id was unreadable, so the next call looks the address up again
   }
-  *out = static_cast<unsigned char *>(g_scratch_addr[dev]);
+  *out = static_cast<unsigned char *>(c.addr);
   return HDOG_OK;
 }
 

@@ -134,6 +134,7 @@ _SIGNATURES = {
     "hdog_run_param_file": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int]),
     "hdog_ctx_set_option": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int]),
     "hdog_ccl_noalloc": (ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P]),
+    "hdog_ccl_edge_count": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]),
     "hdog_timing_enable": (ctypes.c_int, [_P, ctypes.c_int]),
     "hdog_timing_read": (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_size_t]),
     "hdog_records_to_global": (ctypes.c_int, [_P, ctypes.c_int64, ctypes.POINTER(hdog_global_params), _P, _P]),
@@ -312,6 +313,13 @@ class Context:
         """Substacks in the first batch of run_stack with a host-memory stack (0: the
         context's max_substacks); the copy of the later slices overlaps that batch."""
         check(lib().hdog_ctx_set_option(self._h, HDOG_OPT_HOST_BATCH, int(n)))
+
+    def ccl_edge_count(self):
+        """(edges, capacity) of the last labelling's first substack: cross-tile edges found
+        and the edge list's size (more edges than that are merged from the mask)."""
+        e, c = ctypes.c_int64(), ctypes.c_int64()
+        check(lib().hdog_ccl_edge_count(self._h, ctypes.byref(e), ctypes.byref(c)))
+        return e.value, c.value
 
     def timing(self, on=True):
         """Per-kernel CUDA-event timing of this context's launches."""

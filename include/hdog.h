@@ -181,8 +181,10 @@ int hdog_run_param_file(const char *param_path, int verbose);
    in one fixed 4.7 MB device array inside the library (per device, for the life of the
    process).  Larger volumes return HDOG_ERR_SHAPE.  Calls share that array: calls that
    overlap on the GPU (other streams or host threads) race; calls in sequence on one
-   stream do not.  The first call on a device looks up the array's device address with
-   that device current.  Synchronizes `stream` before returning. */
+   stream do not.  The first call on a device (and the first after a cudaDeviceReset,
+   which gives the device a new context) looks up the array's device address with that
+   device current; make that first call before any stream capture.  Synchronizes `stream`
+   before returning. */
 int hdog_ccl_noalloc(const uint8_t *d_mask, int32_t *d_labels, int width, int height, int depth,
                      void *stream);
 
@@ -295,6 +297,12 @@ enum {
                                 batch.  Records are the same for every value. */
 };
 int hdog_ctx_set_option(hdog_ctx *ctx, int option, int value);
+
+/* ---- diagnostics ----
+   Cross-tile edges the last labelling of the context's first substack produced, and the
+   edge list's capacity; above it the labelling merged those edges from the mask instead.
+   No counterpart in the reference (its CCL has no edge list).  Synchronizes the device. */
+int hdog_ccl_edge_count(hdog_ctx *ctx, int64_t *edges, int64_t *capacity);
 
 /* ---- per-kernel timing (CUDA events on the launching stream) ---- */
 /* When on, every kernel launch of the context's calls is bracketed by two events. */

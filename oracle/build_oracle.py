@@ -17,7 +17,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 REF_OUT = os.path.join(HERE, "_ref")
 LIB = os.path.join(BUILD, "liboracle.so")
-REFERENCE = "/root/reference"
+# the reference checkout: HDOG_REFERENCE, else its location in the build container
+REFERENCE = os.environ.get("HDOG_REFERENCE", "/root/reference")
 REF_KERNEL_FILES = ["NormalizeFilter", "DoG3DFilter", "Hessian3DFilter_element", "CCL3D", "Eigenvalues",
                     "Erosion3DFilter"]
 

@@ -171,4 +171,6 @@ def ref_pd_only(planes):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else os.path.join(ROOT, "gpurun_out", "golden"))
+    if len(sys.argv) != 2:
+        sys.exit("usage: python oracle/ref_golden.py OUT_DIR")
+    main(sys.argv[1])

@@ -23,7 +23,7 @@ import types
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("HDOG_REFERENCE", "/root/reference")
 SCRIPT = os.path.join(REF, "script")
 
 DT_LOCAL = np.dtype([("local_x", "f4"), ("local_y", "f4"), ("local_z", "f4"), ("structureness", "f4"),

@@ -61,5 +61,8 @@ def test_ccl_edge_list_overflow_merges_from_the_mask(kind):
         mask = (np.random.default_rng(5).random((D, H, W)) < 0.5).astype(np.uint8)
     with hdog.Context(params(W, H, D)) as ctx:
         labels = ctx.ccl(torch.from_numpy(mask).cuda()).cpu().numpy()
+        edges, cap = ctx.ccl_edge_count()
+    # the premise: the edge list overflowed, so the merges came from the mask
+    assert edges > cap, (edges, cap)
     ref, _ = orc.ccl(mask)
     assert np.array_equal(labels, ref), kind
