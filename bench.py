@@ -543,6 +543,16 @@ def main():
     e2e_ms = (time.perf_counter() - t0) * 1e3
     e2e_ms = max_over_ranks(e2e_ms, dist) / args.steps
     assert recs_e2e.tobytes() == recs.tobytes(), "host-input run differs from device-input run"
+    # the pinned host -> device copy rate of this machine, for reading the end-to-end figure
+    h2d_ms = []
+    for _ in range(3):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        stack_dev.copy_(host, non_blocking=True)
+        b.record(stream)
+        torch.cuda.synchronize()
+        h2d_ms.append(a.elapsed_time(b))
+    h2d_gbs = unique * 2 / (min(h2d_ms) * 1e-3) / 1e9
 
     # ---- plain: one substack per launch sequence (the reference's processing order)
     plain = hdog.Context(p, max_substacks=1)
@@ -582,7 +592,8 @@ def main():
         "plain": {"value": plain_value, "ms_per_step": pms, "mode": "one substack per launch sequence"},
         "batched_over_plain": value / plain_value,
         "e2e": {"value": unique * ws / (e2e_ms * 1e-3) / 1e9, "unit": "Gvox/s",
-                "h2d_bytes_per_step": unique * 2, "d2h_bytes_per_step": n_records * 28},
+                "h2d_bytes_per_step": unique * 2, "d2h_bytes_per_step": n_records * 28,
+                "ms_per_step": e2e_ms, "pinned_h2d_gbs": round(h2d_gbs, 1)},
         "gpu_launches": int(launches),
         "kernel_ms_per_step": {k: round(v[1] / args.steps, 4) for k, v in sorted(ktimes.items(), key=lambda kv: -kv[1][1])},
         # algorithmic GB/s of each dense kernel (its per-voxel bytes over its event time)

@@ -834,16 +834,26 @@ static int run_stack_locked(hdog_ctx *c, const uint16_t *stack, int on_device, i
   if (z0s.empty()) return HDOG_OK;
   const size_t plane = (size_t)c->W * c->H;
   const uint16_t *dev = stack;
-  // batches of as many substacks as the context holds; with host input the first batch
-  // holds host_batch substacks, so that only its slices are copied before work starts and
-  // the copy of the rest overlaps it
+  // batches of as many substacks as the context holds.  With host input the first batch
+  // holds host_batch substacks, so that only its slices are copied before work starts, and
+  // each later batch at most twice the one before: its slices are copied while the one
+  // before runs, and a batch's compute takes several times longer than the copy of twice
+  // its new slices (a 32-slice substack adds 16 new slices), so no batch waits for its chunk.
   std::vector<size_t> starts;   // first substack of each batch, then the end
   {
-    const size_t full = (size_t)c->max_sub;
-    size_t first = full;
-    if (!on_device && c->host_batch > 0) first = std::min(full, (size_t)c->host_batch);
-    for (size_t b0 = 0; b0 < z0s.size(); b0 += (b0 == 0 ? first : full)) starts.push_back(b0);
-    starts.push_back(z0s.size());
+    const size_t full = (size_t)c->max_sub, n = z0s.size();
+    size_t size = full;
+    if (!on_device && c->host_batch > 0) size = std::min(full, (size_t)c->host_batch);
+    for (size_t b0 = 0; b0 < n;) {
+      starts.push_back(b0);
+      size_t take = std::min(size, n - b0);
+      const size_t next = std::min(full, 2 * size);
+      // a remainder smaller than half the next batch joins this one when the context holds it
+      if (!on_device && n - b0 - take > 0 && n - b0 - take < (next + 1) / 2 && n - b0 <= full) take = n - b0;
+      b0 += take;
+      size = on_device ? full : next;
+    }
+    starts.push_back(n);
   }
   const size_t nbatch = starts.size() - 1;
   // on an early error return the chunk copies may still be reading the caller's host

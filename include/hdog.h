@@ -290,11 +290,12 @@ enum {
   HDOG_OPT_FUSED_SWEEP = 1,  /* 1 (default): DoG, Hessian and the PD test in one z-sweep kernel
                                 when the radii allow; 0: separate passes (same results) */
   HDOG_OPT_HOST_BATCH = 2    /* substacks in the first batch when hdog_run_stack gets its stack
-                                in host memory (default 1; 0: as many as the context holds;
-                                later batches hold as many as the context holds): the stack is
-                                copied in chunks on a second stream and each batch waits only
-                                for its own slices, so the copy of the rest overlaps the first
-                                batch.  Records are the same for every value. */
+                                in host memory (default 1; 0: as many as the context holds);
+                                each later batch holds at most twice as many as the one before
+                                (and at most what the context holds): the stack is copied in
+                                chunks on a second stream and each batch waits only for its own
+                                slices, so the copy of each chunk overlaps the batch before it.
+                                Records are the same for every value. */
 };
 int hdog_ctx_set_option(hdog_ctx *ctx, int option, int value);
 
