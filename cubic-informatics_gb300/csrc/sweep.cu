@@ -553,8 +553,58 @@ __global__ void __launch_bounds__(DogT<RA, RB, ZA, ZB>::NT, 3)
 // `0 +` only turns -0 into +0, and a zero's sign never changes a magnitude, a comparison
 // or a fixed-point sum, so the mask and every record stay identical without it.
 __device__ __forceinline__ float hdiff(float plus, float minus) { return __fmul_rn(__fsub_rn(plus, minus), 0.5f); }
+// The same on two voxels at once (each lane rounds as the scalar operations do).
+__device__ __forceinline__ float2 hd2(float2 plus, float2 minus) {
+  return mul2(sub2(plus, minus), make_float2(0.5f, 0.5f));
+}
 
-__global__ void __launch_bounds__(kHThreads, 6)
+// The pinned Sylvester test (common.cuh pd_test) on two voxels: every product and FMA is
+// the scalar one lane by lane; fma(-(a*b), c, t) is written fma(a*b, c * -1, t), the same
+// exact product with the sign moved.  Returns the two results in bits 0 and 8.
+__device__ __forceinline__ uint32_t pd_test2(float2 xx, float2 xy, float2 xz, float2 yy, float2 yz, float2 zz) {
+  const float2 m1 = make_float2(-1.0f, -1.0f);
+  const float2 p = mul2(xx, yy);
+  const float2 q = mul2(mul2(make_float2(2.0f, 2.0f), xy), yz);
+  float2 t = fma2(p, zz, mul2(q, xz));
+  t = fma2(mul2(xx, yz), mul2(yz, m1), t);
+  t = fma2(mul2(yy, xz), mul2(xz, m1), t);
+  const float2 xy2 = mul2(xy, xy);
+  const float2 rhs = mul2(mul2(zz, xy), xy);
+  const uint32_t a = (xx.x < 0.0f) & (p.x > xy2.x) & (t.x < rhs.x);
+  const uint32_t b = (xx.y < 0.0f) & (p.y > xy2.y) & (t.y < rhs.y);
+  return a | (b << 8);
+}
+
+// Gradient pairs of one ring row.  Voxel pairs come in two frames: the C frame
+// (X0, X0+1), (X0+2, X0+3) -- the thread's own quad -- and the G frame (X0-1, X0),
+// (X0+1, X0+2), (X0+3, X0+4), in which x differences of pairs loaded on 8-byte
+// boundaries land without repacking.  gx in the G frame from the row's columns
+// X0-2 .. X0+5 (l = X0-2, X0-1; c = the quad; r = X0+4, X0+5).
+__device__ __forceinline__ void gx_g(float2 l, float2 c0, float2 c1, float2 r, float2 (&g)[3]) {
+  g[0] = hd2(c0, l);
+  g[1] = hd2(c1, c0);
+  g[2] = hd2(r, c1);
+}
+
+__device__ __forceinline__ void ld_row(const float *p, float2 &l, float2 &c0, float2 &c1, float2 &r) {
+  l = *reinterpret_cast<const float2 *>(p - 2);
+  const float4 c = *reinterpret_cast<const float4 *>(p);
+  c0 = make_float2(c.x, c.y);
+  c1 = make_float2(c.z, c.w);
+  r = *reinterpret_cast<const float2 *>(p + 4);
+}
+__device__ __forceinline__ void ld_quad(const float *p, float2 &c0, float2 &c1) {
+  const float4 c = *reinterpret_cast<const float4 *>(p);
+  c0 = make_float2(c.x, c.y);
+  c1 = make_float2(c.z, c.w);
+}
+
+// Blocks per SM the Hessian sweep is compiled for: five fit its z pipeline in 96
+// registers without spilling.
+#ifndef HDOG_HESS_BLOCKS
+#define HDOG_HESS_BLOCKS 5
+#endif
+__global__ void __launch_bounds__(kHThreads, HDOG_HESS_BLOCKS)
     k_hess_sweep(const __grid_constant__ CUtensorMap map, const Sub *subs, const float *norm, uint8_t *mask,
                  FgEntry *fg, int32_t *fg_idx, unsigned long long *fg_count, int *status) {
   extern __shared__ __align__(128) unsigned char smem[];
@@ -596,7 +646,34 @@ __global__ void __launch_bounds__(kHThreads, 6)
     }
   const int q = t % (kHTX / 4), ly = t / (kHTX / 4);
   const int X0 = x0 + 4 * q, Y = y0 + ly;
-  const int b = (ly + 2) * kHPX + 4 * q;   // ring index of column X0 - 4 on row Y
+  const int b = (ly + 2) * kHPX + 4 * q + 4;   // ring index of column X0 on row Y
+  // every in-plane gradient position of the quad inside the volume: the z-pipelined
+  // stencil below (only the z neighbours can fall outside); the frame's edges take the
+  // literal zero-halo path voxel by voxel.  Fixed per thread for the whole sweep.
+  const bool interior = X0 >= 1 && X0 + 3 <= W - 2 && Y >= 1 && Y <= H - 2;
+  // z pipeline of the interior path: first derivatives of slices zh-1 and zh on row Y
+  // (gx in the G frame, gy and gz in the C frame) and DoG of slices zh and zh+1 on row Y
+  const float2 zero2 = make_float2(0.0f, 0.0f);
+  float2 gxm[3] = {zero2, zero2, zero2}, gx0[3];
+  float2 gym[2] = {zero2, zero2}, gy0[2], gzm[2] = {zero2, zero2}, gz0[2];
+  float2 fm[2] = {zero2, zero2}, f0[2];
+  if (interior) {
+    // slice 0: gx, gy on row Y; gz from slices 1 and -1 (zero)
+    const float *P0 = ring + slot(0) * PL + b, *P1 = ring + slot(1) * PL + b;
+    float2 l, r, u0, u1, d0, d1;
+    ld_row(P0, l, f0[0], f0[1], r);
+    gx_g(l, f0[0], f0[1], r, gx0);
+    ld_quad(P0 - kHPX, u0, u1);
+    ld_quad(P0 + kHPX, d0, d1);
+    gy0[0] = hd2(d0, u0);
+    gy0[1] = hd2(d1, u1);
+    float2 p0, p1;
+    ld_quad(P1, p0, p1);
+    gz0[0] = hd2(p0, zero2);
+    gz0[1] = hd2(p1, zero2);
+    fm[0] = f0[0]; fm[1] = f0[1];
+    f0[0] = p0; f0[1] = p1;
+  }
   for (int zh = 0; zh < D; zh++) {
     // DoG slice zh+5 reuses the slot of slice zh-3, read for the last time in iteration
     // zh-1: the producer waits until every warp is past it (warps otherwise run up to the
@@ -613,112 +690,78 @@ __global__ void __launch_bounds__(kHThreads, 6)
       ok = false;
       atomicExch(status, HDOG_ERR_TIMEOUT);
     }
-    const float *P0 = ring + slot(zh) * PL, *P1 = ring + slot(zh + 1) * PL, *P2 = ring + slot(zh + 2) * PL;
-    const float *M1 = ring + slot(zh - 1) * PL, *M2 = ring + slot(zh - 2) * PL;
-    const bool zup = zh + 1 < D, zdn = zh >= 1;
-    float hv[4][6];
-    bool fgv[4] = {false, false, false, false};
-    int nfg = 0;
+    uint32_t mword = 0;
     const int32_t i0 = zh * WH + Y * W + X0;
-    // every in-plane gradient position of the quad inside the volume: the plain stencil
-    // (only the z neighbours can fall outside, handled by zup / zdn)
-    if (X0 >= 1 && X0 + 3 <= W - 2 && Y >= 1 && Y <= H - 2) {
-      // ZI: both z neighbours inside the volume (every slice but the first and the last),
-      // compiled without the per-slice selects of the zero-halo rule
-      auto fast = [&](auto zin) {
-        constexpr bool ZI = decltype(zin)::value;
-        const bool zu = ZI || zup, zd = ZI || zdn;
-        // Voxels o = 2p, 2p+1 of the quad go as one pair through f32x2 subtract and multiply
-        // (each lane rounds as the scalar operation does): every stencil operand that sits
-        // at the same offset from both voxels comes from one 8-byte-aligned pair of a
-        // 128-bit ring load.  The x gradients of the xy and xz elements are taken at odd
-        // offsets, so they stay scalar and only their outer difference is paired.
-        auto ld12 = [&](const float *src, float2 *dst) {   // columns X0-4 .. X0+7 as 6 pairs
+    float hv[4][6];
+    if (interior) {
+      const float *P0 = ring + slot(zh) * PL + b, *P1 = ring + slot(zh + 1) * PL + b;
+      const float *P2 = ring + slot(zh + 2) * PL + b;
+      // ---- in-plane second derivatives of slice zh
+      float2 hxx[2], hxy[3], hyy[2];
+      hxx[0] = hd2(gx0[1], gx0[0]);
+      hxx[1] = hd2(gx0[2], gx0[1]);
+      {
+        float2 l, c0, c1, r, gu[3], gd[3];
+        ld_row(P0 - kHPX, l, c0, c1, r);
+        gx_g(l, c0, c1, r, gu);
+        float2 e0, e1;
+        ld_quad(P0 - 2 * kHPX, e0, e1);
+        const float2 gyu0 = hd2(fm[0], e0), gyu1 = hd2(fm[1], e1);   // gy on row Y-1
+        ld_row(P0 + kHPX, l, c0, c1, r);
+        gx_g(l, c0, c1, r, gd);
+        ld_quad(P0 + 2 * kHPX, e0, e1);
+        const float2 gyd0 = hd2(e0, fm[0]), gyd1 = hd2(e1, fm[1]);                      // gy on row Y+1
 #pragma unroll
-          for (int i = 0; i < 3; i++) {
-            const float4 f = *reinterpret_cast<const float4 *>(src + 4 * i);
-            dst[2 * i] = make_float2(f.x, f.y);
-            dst[2 * i + 1] = make_float2(f.z, f.w);
-          }
-        };
-        auto ld4 = [&](const float *src, float2 *dst) {    // columns X0 .. X0+3 as 2 pairs
-          const float4 f = *reinterpret_cast<const float4 *>(src + 4);
-          dst[0] = make_float2(f.x, f.y);
-          dst[1] = make_float2(f.z, f.w);
-        };
-        const float2 half = make_float2(0.5f, 0.5f), zero2 = make_float2(0.0f, 0.0f);
-        auto hd2 = [&](float2 plus, float2 minus) { return mul2(sub2(plus, minus), half); };
-        float2 h2[2][6];   // [pair][element]
-        {
-          float2 a[6], v[2], w[2], p2[2], m2[2];
-          ld12(P0 + b, a);
-          ld4(P0 + b - 2 * kHPX, v);
-          ld4(P0 + b + 2 * kHPX, w);
-          ld4(P2 + b, p2);
-          ld4(M2 + b, m2);
+        for (int i = 0; i < 3; i++) hxy[i] = hd2(gd[i], gu[i]);
+        hyy[0] = hd2(gyd0, gyu0);
+        hyy[1] = hd2(gyd1, gyu1);
+      }
+      // ---- first derivatives of slice zh+1 on row Y, then the z second derivatives
+      float2 gxp[3], gyp[2], gzp[2], fp[2];
+      {
+        float2 l, r, u0, u1, d0, d1;
+        l = *reinterpret_cast<const float2 *>(P1 - 2);
+        r = *reinterpret_cast<const float2 *>(P1 + 4);
+        gx_g(l, f0[0], f0[1], r, gxp);
+        ld_quad(P1 - kHPX, u0, u1);
+        ld_quad(P1 + kHPX, d0, d1);
+        gyp[0] = hd2(d0, u0);
+        gyp[1] = hd2(d1, u1);
+        ld_quad(P2, fp[0], fp[1]);
+        const bool zin = zh + 1 < D;   // gz outside the volume is zero
+        gzp[0] = zin ? hd2(fp[0], fm[0]) : zero2;
+        gzp[1] = zin ? hd2(fp[1], fm[1]) : zero2;
+      }
+      float2 hxz[3], hyz[2], hzz[2];
 #pragma unroll
-          for (int p = 0; p < 2; p++) {
-            const float2 c = a[2 + p];   // voxels 2p, 2p+1 at row index 4 + 2p
-            h2[p][0] = hd2(hd2(a[3 + p], c), hd2(c, a[1 + p]));
-            h2[p][3] = hd2(hd2(w[p], c), hd2(c, v[p]));
-            h2[p][5] = hd2(zu ? hd2(p2[p], c) : zero2, zd ? hd2(c, m2[p]) : zero2);
-          }
-        }
-        {
-          float2 u[6], dn[6];
-          ld12(P0 + b - kHPX, u);
-          ld12(P0 + b + kHPX, dn);
-          const float *uf = reinterpret_cast<const float *>(u), *df = reinterpret_cast<const float *>(dn);
+      for (int i = 0; i < 3; i++) hxz[i] = hd2(gxp[i], gxm[i]);
+      hyz[0] = hd2(gyp[0], gym[0]);
+      hyz[1] = hd2(gyp[1], gym[1]);
+      hzz[0] = hd2(gzp[0], gzm[0]);
+      hzz[1] = hd2(gzp[1], gzm[1]);
+      // advance the pipeline
 #pragma unroll
-          for (int p = 0; p < 2; p++) {
-            const int o = 2 * p;
-            const float2 gd = make_float2(hdiff(df[o + 5], df[o + 3]), hdiff(df[o + 6], df[o + 4]));
-            const float2 gu = make_float2(hdiff(uf[o + 5], uf[o + 3]), hdiff(uf[o + 6], uf[o + 4]));
-            h2[p][1] = hd2(gd, gu);
-          }
-        }
-        {
-          float2 pp[6], mm[6];
-          ld12(P1 + b, pp);
-          ld12(M1 + b, mm);
-          const float *pf = reinterpret_cast<const float *>(pp), *mf = reinterpret_cast<const float *>(mm);
+      for (int i = 0; i < 3; i++) { gxm[i] = gx0[i]; gx0[i] = gxp[i]; }
 #pragma unroll
-          for (int p = 0; p < 2; p++) {
-            const int o = 2 * p;
-            const float2 gp = zu ? make_float2(hdiff(pf[o + 5], pf[o + 3]), hdiff(pf[o + 6], pf[o + 4])) : zero2;
-            const float2 gm = zd ? make_float2(hdiff(mf[o + 5], mf[o + 3]), hdiff(mf[o + 6], mf[o + 4])) : zero2;
-            h2[p][2] = hd2(gp, gm);
-          }
-        }
-        {
-          float2 pu[2], pd[2], mu[2], md[2];
-          ld4(P1 + b - kHPX, pu);
-          ld4(P1 + b + kHPX, pd);
-          ld4(M1 + b - kHPX, mu);
-          ld4(M1 + b + kHPX, md);
+      for (int j = 0; j < 2; j++) {
+        gym[j] = gy0[j]; gy0[j] = gyp[j];
+        gzm[j] = gz0[j]; gz0[j] = gzp[j];
+        fm[j] = f0[j]; f0[j] = fp[j];
+      }
+      // G frame -> C frame for the two elements that live there (voxel 2j+h)
+      const float2 cxy[2] = {make_float2(hxy[0].y, hxy[1].x), make_float2(hxy[1].y, hxy[2].x)};
+      const float2 cxz[2] = {make_float2(hxz[0].y, hxz[1].x), make_float2(hxz[1].y, hxz[2].x)};
 #pragma unroll
-          for (int p = 0; p < 2; p++)
-            h2[p][4] = hd2(zu ? hd2(pd[p], pu[p]) : zero2, zd ? hd2(md[p], mu[p]) : zero2);
-        }
-#pragma unroll
-        for (int p = 0; p < 2; p++)
-#pragma unroll
-          for (int k = 0; k < 6; k++) {
-            hv[2 * p][k] = h2[p][k].x;
-            hv[2 * p + 1][k] = h2[p][k].y;
-          }
-        uint32_t mword = 0;
-#pragma unroll
-        for (int o = 0; o < 4; o++) {
-          const bool pdv = pd_test(hv[o][0], hv[o][1], hv[o][2], hv[o][3], hv[o][4], hv[o][5]);
-          mword |= (pdv ? 1u : 0u) << (8 * o);
-          fgv[o] = pdv;
-          nfg += pdv;
-        }
-        *reinterpret_cast<uint32_t *>(mask + S.vox + i0) = mword;
-      };
-      if (zup && zdn) fast(std::true_type{});
-      else fast(std::false_type{});
+      for (int j = 0; j < 2; j++) {
+        mword |= pd_test2(hxx[j], cxy[j], cxz[j], hyy[j], hyz[j], hzz[j]) << (16 * j);
+        hv[2 * j][0] = hxx[j].x; hv[2 * j + 1][0] = hxx[j].y;
+        hv[2 * j][1] = cxy[j].x; hv[2 * j + 1][1] = cxy[j].y;
+        hv[2 * j][2] = cxz[j].x; hv[2 * j + 1][2] = cxz[j].y;
+        hv[2 * j][3] = hyy[j].x; hv[2 * j + 1][3] = hyy[j].y;
+        hv[2 * j][4] = hyz[j].x; hv[2 * j + 1][4] = hyz[j].y;
+        hv[2 * j][5] = hzz[j].x; hv[2 * j + 1][5] = hzz[j].y;
+      }
+      *reinterpret_cast<uint32_t *>(mask + S.vox + i0) = mword;
     } else {
 #pragma unroll
       for (int o = 0; o < 4; o++) {
@@ -749,39 +792,42 @@ __global__ void __launch_bounds__(kHThreads, 6)
         hv[o][5] = hdiff(GZ(1), GZ(-1));
         const bool pdv = pd_test(hv[o][0], hv[o][1], hv[o][2], hv[o][3], hv[o][4], hv[o][5]);
         mask[S.vox + i0 + o] = pdv ? 1 : 0;
-        fgv[o] = pdv && i0 + o != 0;
-        nfg += fgv[o];
+        // voxel 0 is background (its label is 0 in the reference's CCL)
+        mword |= (pdv && i0 + o != 0 ? 1u : 0u) << (8 * o);
       }
     }
-    // warp-aggregated append to the foreground list (every lane of the block takes part).
-    // The normalized values of the quad (one 16-byte load, W % 4 == 0) are read only by
-    // threads with foreground, before the slot reservation so that the two latencies
-    // overlap.
-    const float4 nq = nfg ? __ldg(reinterpret_cast<const float4 *>(norm + S.vox + i0)) : make_float4(0.f, 0.f, 0.f, 0.f);
-    const float nv[4] = {nq.x, nq.y, nq.z, nq.w};
-    const int lane = t & 31;
-    int incl = nfg;
-    for (int dd = 1; dd < 32; dd <<= 1) {
-      const int vv = __shfl_up_sync(0xFFFFFFFFu, incl, dd);
-      if (lane >= dd) incl += vv;
-    }
-    const int tot = __shfl_sync(0xFFFFFFFFu, incl, 31);
-    unsigned long long base = 0;
-    if (lane == 31 && tot) base = atomicAdd(&fg_count[blockIdx.y * kFgCountStride], (unsigned long long)tot);
-    base = __shfl_sync(0xFFFFFFFFu, base, 31) + (unsigned long long)(incl - nfg);
+    // warp-aggregated append of the foreground voxels to the list.  Warps without any
+    // skip it; otherwise each lane's slot offset comes from three bit-sliced ballots of its
+    // count.  The normalized values of the quad (one 16-byte load, W % 4 == 0) are read only
+    // by threads with foreground, before the slot reservation so the latencies overlap.
+    const int nfg = __popc(mword);
+    const unsigned any = __ballot_sync(0xFFFFFFFFu, nfg != 0);
+    if (any) {
+      const float4 nq = nfg ? __ldg(reinterpret_cast<const float4 *>(norm + S.vox + i0)) : make_float4(0.f, 0.f, 0.f, 0.f);
+      const int lane = t & 31;
+      const unsigned b0 = __ballot_sync(0xFFFFFFFFu, nfg & 1), b1 = __ballot_sync(0xFFFFFFFFu, nfg & 2),
+                     b2 = __ballot_sync(0xFFFFFFFFu, nfg & 4);
+      const unsigned lt = (1u << lane) - 1u;
+      const int excl = __popc(b0 & lt) + 2 * __popc(b1 & lt) + 4 * __popc(b2 & lt);
+      const int tot = __popc(b0) + 2 * __popc(b1) + 4 * __popc(b2);
+      unsigned long long base = 0;
+      if (lane == 0) base = atomicAdd(&fg_count[blockIdx.y * kFgCountStride], (unsigned long long)tot);
+      base = __shfl_sync(0xFFFFFFFFu, base, 0) + (unsigned long long)excl;
+      const float nv[4] = {nq.x, nq.y, nq.z, nq.w};
 #pragma unroll
-    for (int o = 0; o < 4; o++) {
-      if (!fgv[o]) continue;
-      if ((int64_t)base < S.fg_cap) {
-        float4 *dst = reinterpret_cast<float4 *>(fg + S.fg + base);
-        dst[0] = make_float4(__int_as_float(i0 + o), nv[o], hv[o][0], hv[o][1]);
-        dst[1] = make_float4(hv[o][2], hv[o][3], hv[o][4], hv[o][5]);
-        fg_idx[S.fg + base] = i0 + o;
+      for (int o = 0; o < 4; o++) {
+        if (!((mword >> (8 * o)) & 1u)) continue;
+        if ((int64_t)base < S.fg_cap) {
+          float4 *dst = reinterpret_cast<float4 *>(fg + S.fg + base);
+          dst[0] = make_float4(__int_as_float(i0 + o), nv[o], hv[o][0], hv[o][1]);
+          dst[1] = make_float4(hv[o][2], hv[o][3], hv[o][4], hv[o][5]);
+          fg_idx[S.fg + base] = i0 + o;
+        }
+        base++;
       }
-      base++;
     }
     __syncwarp();
-    if (lane == 0) mbar_arrive(&done[zh % kHRing]);
+    if ((t & 31) == 0) mbar_arrive(&done[zh % kHRing]);
   }
 }
 

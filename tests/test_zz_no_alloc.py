@@ -62,9 +62,8 @@ def test_noalloc_labels_equal_oracle_and_context_labels_on_consecutive_calls():
 @pytest.mark.gpu
 @pytest.mark.parametrize("kind", ["dense_random", "sparse_random"])
 def test_noalloc_at_its_voxel_limit(kind):
-    """Exactly 2^22 voxels (256 x 256 x 64: 16-byte rows, row and slice wrap-around edges).
-    The dense mask gives more cross-tile edges than the fixed edge list holds, so the
-    labelling merges them from the mask instead; the sparse one stays on the edge list."""
+    """Exactly 2^22 voxels (256 x 256 x 64: 16-byte rows, row and slice wrap-around edges),
+    a dense and a sparse random mask, two calls each."""
     import torch
     W, H, D = 256, 256, 64
     assert W * H * D == MAX_VOXELS
