@@ -599,6 +599,28 @@ __device__ __forceinline__ void ld_quad(const float *p, float2 &c0, float2 &c1) 
   c1 = make_float2(c.z, c.w);
 }
 
+// Staged list entries per warp: one iteration adds at most 128 (four voxels per lane).
+constexpr int kHStage = 128;
+
+// Moves a warp's `n` staged entries to the substack's list: one slot reservation, then
+// 16-byte stores over consecutive entries.  Entries past the list's capacity are dropped
+// but counted, so the host sees the overflow and redoes the batch.
+__device__ __forceinline__ void flush_stage(const FgEntry *stage, int n, const Sub &S, FgEntry *fg, int32_t *fg_idx,
+                                            unsigned long long *count) {
+  __syncwarp();
+  const int lane = threadIdx.x & 31;
+  unsigned long long base = 0;
+  if (lane == 0) base = atomicAdd(count, (unsigned long long)n);
+  base = __shfl_sync(0xFFFFFFFFu, base, 0);
+  const int64_t room = S.fg_cap - (int64_t)base;
+  const int keep = room <= 0 ? 0 : (room < n ? (int)room : n);
+  const float4 *src = reinterpret_cast<const float4 *>(stage);
+  float4 *dst = reinterpret_cast<float4 *>(fg + S.fg + base);
+  for (int i = lane; i < 2 * keep; i += 32) dst[i] = src[i];
+  for (int i = lane; i < keep; i += 32) fg_idx[S.fg + base + i] = stage[i].idx;
+  __syncwarp();
+}
+
 // Blocks per SM the Hessian sweep is compiled for: five fit its z pipeline in 96
 // registers without spilling.
 #ifndef HDOG_HESS_BLOCKS
@@ -620,6 +642,9 @@ __global__ void __launch_bounds__(kHThreads, HDOG_HESS_BLOCKS)
   // reads of DoG slice zh-2
   uint64_t *done = bar + kHRing;
   const int t = threadIdx.x;
+  // this warp's staging of list entries (flushed to the global list kHStage at a time at most)
+  FgEntry *stage = reinterpret_cast<FgEntry *>(smem + (size_t)kHRing * PL * 4 + 2 * kHRing * 8) + (t >> 5) * kHStage;
+  int staged = 0;   // entries in this warp's staging buffer (the same in every lane)
   const int D = S.D, W = S.W, H = S.H;
   const int32_t WH = W * H;
   if (t == 0) {
@@ -796,10 +821,11 @@ __global__ void __launch_bounds__(kHThreads, HDOG_HESS_BLOCKS)
         mword |= (pdv && i0 + o != 0 ? 1u : 0u) << (8 * o);
       }
     }
-    // warp-aggregated append of the foreground voxels to the list.  Warps without any
-    // skip it; otherwise each lane's slot offset comes from three bit-sliced ballots of its
-    // count.  The normalized values of the quad (one 16-byte load, W % 4 == 0) are read only
-    // by threads with foreground, before the slot reservation so the latencies overlap.
+    // the foreground voxels go to the warp's staging buffer in shared memory; a full buffer
+    // goes to the global list with one slot reservation and coalesced stores.  Warps
+    // without foreground skip all of it; each lane's place comes from three bit-sliced
+    // ballots of its count.  The normalized values of the quad (one 16-byte load, W % 4 ==
+    // 0) are read only by threads with foreground.
     const int nfg = __popc(mword);
     const unsigned any = __ballot_sync(0xFFFFFFFFu, nfg != 0);
     if (any) {
@@ -810,25 +836,26 @@ __global__ void __launch_bounds__(kHThreads, HDOG_HESS_BLOCKS)
       const unsigned lt = (1u << lane) - 1u;
       const int excl = __popc(b0 & lt) + 2 * __popc(b1 & lt) + 4 * __popc(b2 & lt);
       const int tot = __popc(b0) + 2 * __popc(b1) + 4 * __popc(b2);
-      unsigned long long base = 0;
-      if (lane == 0) base = atomicAdd(&fg_count[blockIdx.y * kFgCountStride], (unsigned long long)tot);
-      base = __shfl_sync(0xFFFFFFFFu, base, 0) + (unsigned long long)excl;
+      if (staged + tot > kHStage) {
+        flush_stage(stage, staged, S, fg, fg_idx, &fg_count[blockIdx.y * kFgCountStride]);
+        staged = 0;
+      }
       const float nv[4] = {nq.x, nq.y, nq.z, nq.w};
+      int k = staged + excl;
 #pragma unroll
       for (int o = 0; o < 4; o++) {
         if (!((mword >> (8 * o)) & 1u)) continue;
-        if ((int64_t)base < S.fg_cap) {
-          float4 *dst = reinterpret_cast<float4 *>(fg + S.fg + base);
-          dst[0] = make_float4(__int_as_float(i0 + o), nv[o], hv[o][0], hv[o][1]);
-          dst[1] = make_float4(hv[o][2], hv[o][3], hv[o][4], hv[o][5]);
-          fg_idx[S.fg + base] = i0 + o;
-        }
-        base++;
+        float4 *dst = reinterpret_cast<float4 *>(stage + k);
+        dst[0] = make_float4(__int_as_float(i0 + o), nv[o], hv[o][0], hv[o][1]);
+        dst[1] = make_float4(hv[o][2], hv[o][3], hv[o][4], hv[o][5]);
+        k++;
       }
+      staged += tot;
     }
     __syncwarp();
     if ((t & 31) == 0) mbar_arrive(&done[zh % kHRing]);
   }
+  if (staged) flush_stage(stage, staged, S, fg, fg_idx, &fg_count[blockIdx.y * kFgCountStride]);
 }
 
 // ------------------------------------------------------------------ host side
@@ -871,7 +898,7 @@ static const SweepInst *find_inst(const DogTaps &T) {
 }
 
 static constexpr size_t kHessSmem =
-    (size_t)kHRing * kHPX * kHPY * 4 + (2 * kHRing) * 8;
+    (size_t)kHRing * kHPX * kHPY * 4 + (2 * kHRing) * 8 + (size_t)(kHThreads / 32) * kHStage * sizeof(FgEntry);
 static_assert((kHPX * kHPY * 4) % 128 == 0, "TMA ring slots must start on 128-byte boundaries");
 
 // Whether the fused sweep handles these parameters (else the separate passes run).
