@@ -264,73 +264,112 @@ def profile_case():
 
 
 UNEVEN_SHAPES = [(2560, 2160), (1280, 2160), (2560, 1080)]
+UNEVEN_SUBSET = 6
+UNEVEN_SUB = ("the first 6 stacks of the 40-stack uneven mix (z ~ U{64..512}, xy 2560x2160 / 1280x2160 / 2560x1080 "
+              "with p = 1/3 each, nuclei at 2e-5 per voxel); HDoG depth 32, sigma_dog (2,1.5,3.2,2.4), "
+              "radius_norm (20,5)")
 UNEVEN = ("40 uneven stacks: z ~ U{64..512}, xy 2560x2160 / 1280x2160 / 2560x1080 with p = 1/3 each, "
           "nuclei at 2e-5 per voxel (the 256x256x64 case's shape and amplitude distributions); "
           "HDoG depth 32, sigma_dog (2,1.5,3.2,2.4), radius_norm (20,5)")
 
 
-def uneven_workload(args):
-    """The uneven-stack mix: each shape's stacks through one context with their substacks
-    packed into shared batches (hdog_run_stacks), against the plain loop (one substack per
-    launch sequence, stack after stack).  Stacks are generated one at a time and kept in
-    HBM (about 79 GB); a step is one pass over all of them."""
+def uneven_stacks(n, seed, dev):
+    """n seeded stacks of the uneven mix on the device: z ~ U{64..512}, a frame shape each
+    with p = 1/3, nuclei at 2e-5 per voxel.  -> (list of (shape, tensor), unique voxels, s)."""
     import torch
-    import hdog
     from hdog import synth
-    torch.cuda.set_device(0)
-    rng = np.random.default_rng(synth.SEED_BASE + 2)
-    groups = {}
-    unique = 0
+    rng = np.random.default_rng(seed)
+    stacks, unique = [], 0
     t0 = time.time()
-    for i in range(40):
+    for i in range(n):
         w, h = UNEVEN_SHAPES[int(rng.integers(3))]
         length = int(rng.integers(64, 513))
-        n = max(1, int(round(2e-5 * w * h * length)))
-        vol = synth.volume(synth.spec(w, h, length, n, synth.SEED_BASE + 1000 + i))
-        groups.setdefault((w, h), []).append(torch.from_numpy(vol).cuda())
+        nn = max(1, int(round(2e-5 * w * h * length)))
+        vol = synth.volume(synth.spec(w, h, length, nn, synth.SEED_BASE + 1000 + i))
+        stacks.append(((w, h), torch.from_numpy(vol).to(dev)))
         unique += w * h * length
         del vol
-    gen_s = time.time() - t0
-    # one context at a time (a batched context at 2560x2160 reserves about 80 GB)
-    def timed_group(key, tensors, max_sub, steps, warmup, packed):
-        ctx = hdog.Context(hdog.make_params(**dict(PARAMS, width=key[0], height=key[1])), max_substacks=max_sub)
-        run = (lambda: ctx.run_stacks(tensors)[0]) if packed else \
-            (lambda: np.concatenate([ctx.run_stack(t) for t in tensors]))
-        for _ in range(warmup):
-            run()
-        torch.cuda.synchronize()
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record()
-        for _ in range(steps):
-            out = run()
-        b.record()
-        torch.cuda.synchronize()
-        ctx.close()
-        return a.elapsed_time(b) / steps, out
+    return stacks, unique, time.time() - t0
 
-    bms, pms, brec, prec = 0.0, 0.0, {}, {}
-    for k, v in groups.items():
-        ms, brec[k] = timed_group(k, v, 8, args.steps, max(1, args.warmup), True)
-        bms += ms
-        ms, prec[k] = timed_group(k, v, 1, max(1, min(args.steps, 2)), 1, False)
-        pms += ms
-    for k in groups:
-        assert brec[k].tobytes() == prec[k].tobytes(), "batched and plain records differ for %dx%d" % k
-    nrec = sum(len(r) for r in brec.values())
-    line = {"metric": METRIC, "value": unique / (bms * 1e-3) / 1e9, "unit": "Gvox/s", "n_gpus": 1,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": bms, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": UNEVEN, "stacks_per_shape": {"%dx%d" % k: len(v) for k, v in groups.items()},
-                       "unique_voxels_per_step": unique, "records_per_step": nrec,
-                       "mode": "batched: substacks of a shape's stacks packed 8 per launch",
-                       "generator_s": round(gen_s, 1)},
+
+def run_uneven(stacks, unique, steps, warmup, max_sub, dev_id=0):
+    """The batched graph form (one captured CUDA graph over all stacks, one context per frame
+    shape, autotuned launch shapes) against the plain loop (one substack per launch sequence,
+    stack after stack, as the reference runs them); records compared byte for byte."""
+    import torch
+    import hdog
+    shapes = sorted({s for s, _ in stacks})
+    tensors = [t for _, t in stacks]
+    # plain: one context of one substack per frame shape
+    plain_ctx = {k: hdog.Context(hdog.make_params(dev_id=dev_id, **dict(PARAMS, width=k[0], height=k[1])), 1)
+                 for k in shapes}
+    run_plain = lambda: [plain_ctx[s].run_stack(t) for s, t in stacks]
+    for _ in range(1):
+        prec = run_plain()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    psteps = max(1, min(steps, 2))
+    a.record()
+    for _ in range(psteps):
+        prec = run_plain()
+    b.record()
+    torch.cuda.synchronize()
+    pms = a.elapsed_time(b) / psteps
+    for c in plain_ctx.values():
+        c.close()
+    prec = np.concatenate(prec)
+    # graph form
+    t0 = time.time()
+    ctxs = [hdog.Context(hdog.make_params(dev_id=dev_id, **dict(PARAMS, width=k[0], height=k[1])), max_sub)
+            for k in shapes]
+    graph = hdog.Graph(ctxs, tensors)
+    create_s = time.time() - t0
+    for _ in range(max(1, warmup)):
+        grec, counts = graph.run()
+    torch.cuda.synchronize()
+    a.record()
+    for _ in range(steps):
+        grec, counts = graph.run()
+    b.record()
+    torch.cuda.synchronize()
+    gms = a.elapsed_time(b) / steps
+    tuning = {"%dx%d" % k: c.tuning() for k, c in zip(shapes, ctxs)}
+    graph.close()
+    for c in ctxs:
+        c.close()
+    assert grec.tobytes() == prec.tobytes(), "graph and plain records differ on the uneven stacks"
+    return {"value": unique / (gms * 1e-3) / 1e9, "ms_per_step": gms,
             "plain": {"value": unique / (pms * 1e-3) / 1e9, "ms_per_step": pms,
                       "mode": "one substack per launch sequence, stack after stack"},
-            "batched_over_plain": pms / bms,
-            "timing": "each shape's stacks timed with CUDA events around its own context's calls; "
-                      "ms_per_step sums the shapes"}
+            "batched_over_plain": pms / gms, "records_per_step": int(len(grec)),
+            "mode": "one captured CUDA graph over every stack: %d substacks per context at most, persistent sweeps "
+                    "over a device work queue where the autotuner chose them" % max_sub,
+            "graph_create_s": round(create_s, 2), "tuning": tuning}
+
+
+def uneven_workload(args):
+    """The 40-stack uneven mix through the batched graph form against the plain loop.
+    Stacks are generated one at a time and kept in HBM (about 79 GB)."""
+    import torch
+    torch.cuda.set_device(0)
+    stacks, unique, gen_s = uneven_stacks(40, synth_seed(2), "cuda:0")
+    res = run_uneven(stacks, unique, args.steps, args.warmup, 4)
+    shapes = {}
+    for s, _ in stacks:
+        shapes["%dx%d" % s] = shapes.get("%dx%d" % s, 0) + 1
+    line = {"metric": METRIC, "value": res["value"], "unit": "Gvox/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": res["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": UNEVEN, "stacks_per_shape": shapes, "unique_voxels_per_step": unique},
+            "generator_s": round(gen_s, 1)}
+    line.update({k: v for k, v in res.items() if k not in ("value", "ms_per_step")})
     print(json.dumps(line), flush=True)
     return 0
+
+
+def synth_seed(k):
+    from hdog import synth
+    return synth.SEED_BASE + k
 
 
 STREAM = ("dense stack uint16 2560x2160x1536 (17 GB) in pinned host memory, 1.5M nuclei, 30% of them in "
@@ -475,6 +514,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-uneven", action="store_true", help="skip the uneven-stack subset of the default line")
     ap.add_argument("--workload", default="camera", choices=["camera", "uneven", "stream", "soft"],
                     help="camera: the 2560x2160x128 stack (default); uneven: the 40-stack mix; "
                          "stream: the 17 GB stack from host memory; soft: the differentiable chain")
@@ -605,6 +645,18 @@ def main():
                      "end_to_end_alg_gbs": e2e_alg_gbs, "end_to_end_frac": e2e_alg_gbs / peak},
         "clocks": clocks.summary(),
     }
+    if not args.no_uneven:
+        # the uneven-stack subset: the batched graph form against the plain loop
+        del stack_dev
+        torch.cuda.empty_cache()
+        ustacks, uunique, ugen = uneven_stacks(UNEVEN_SUBSET, synth_seed(2), dev)
+        u = run_uneven(ustacks, uunique, max(2, min(args.steps, 4)), 1, 8, local)
+        u["config"] = {"workload": UNEVEN_SUB, "unique_voxels_per_step": uunique,
+                       "frames": sorted({"%dx%d" % sh for sh, _ in ustacks}), "generator_s": round(ugen, 1)}
+        u["value"] = u["value"] * ws
+        u["plain"]["value"] = u["plain"]["value"] * ws
+        line["uneven"] = u
+        del ustacks
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(vol)
     if rank == 0:

@@ -11,7 +11,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
-CU_SOURCES = ["norm.cu", "dog.cu", "sweep.cu", "ccl.cu", "regions.cu", "records.cu", "soft.cu", "capi.cu", "noalloc.cu"]
+CU_SOURCES = ["norm.cu", "dog.cu", "sweep.cu", "ccl.cu", "regions.cu", "records.cu", "soft.cu", "capi.cu", "noalloc.cu", "graph.cu"]
 HEADERS = ["common.cuh", "kernels.cuh", "json_min.hpp", os.path.join(INCLUDE, "hdog.h")]
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -10,6 +10,7 @@
 #include <cstdio>
 #include <cstring>
 #include <fstream>
+#include <memory>
 #include <mutex>
 #include <sstream>
 #include <string>
@@ -219,6 +220,11 @@ struct hdog_ctx {
   FgEntry *fg = nullptr;
   unsigned long long *fg_count = nullptr;
   unsigned long long *fg_count_packed = nullptr;
+  unsigned *qctr = nullptr;      // work-queue counters of the persistent sweeps
+  LaunchShape shape;             // launch shape of the sweeps (autotuned per frame shape)
+  bool tuned = false;            // shape and graph_batch chosen by the autotuner
+  int graph_batch = 0;           // substacks per launch in the graph form (0: max_sub)
+  std::string tune_report;       // JSON of the autotuner's timings
   RegionAcc acc{};
   RegionOut out{};
   hdog_record *records = nullptr;
@@ -252,7 +258,7 @@ struct TimerScope {
 static size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 
 struct Layout {
-  size_t off[40];
+  size_t off[48];
   int n = 0;
   size_t total = 0;
   size_t add(size_t bytes) {
@@ -307,6 +313,7 @@ static void plan(const hdog_params *p, int max_sub, int64_t &nvox, int64_t &reg_
   L.add(S * fg_capacity(nvox) * sizeof(FgEntry));         // 30 foreground list
   L.add(S * kFgCountStride * sizeof(unsigned long long));   // 31 foreground counts (strided)
   L.add(S * sizeof(unsigned long long));     // 32 foreground counts, packed for the read-back
+  L.add(4 * sizeof(unsigned));               // 33 work-queue counters
 }
 
 extern "C" int hdog_ctx_bytes(const hdog_params *p, int max_substacks, size_t *bytes) {
@@ -402,7 +409,9 @@ extern "C" int hdog_ctx_create(const hdog_params *p, int max_substacks, hdog_ctx
   c->fg_count = (unsigned long long *)at(31);
   c->fg_count_packed = (unsigned long long *)at(32);
   c->fg_cap = fg_capacity(c->nvox);
+  c->qctr = (unsigned *)at(33);
   cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->dev);
+  c->shape.num_sms = c->num_sms;
   cudaDeviceGetAttribute(&c->max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->dev);
   const size_t hb = (size_t)max_substacks * sizeof(Sub) + 6 * (size_t)max_substacks * sizeof(int64_t) +
                     (3 * (size_t)max_substacks + 2) * sizeof(int64_t);
@@ -539,7 +548,7 @@ static void enqueue_after_norm(hdog_ctx *c, int nsub, bool fused, cudaStream_t s
   int32_t *fg_root = reinterpret_cast<int32_t *>(c->fb);
   if (fused) {
     launch_dog_hess(c->d_subs, nsub, c->W, c->H, c->D, c->taps, c->norm, c->dog, c->mask, c->fg, fg_root,
-                    c->fg_count, c->status, st);
+                    c->fg_count, c->status, c->shape, c->qctr, st);
   } else {
     enqueue_dog(c, nsub, c->norm, c->dog, st);
     launch_hessian_pd(c->d_subs, nsub, c->W, c->H, c->D, c->dog, c->mask, nullptr, st);
@@ -588,7 +597,9 @@ static int readback(hdog_ctx *c, int nsub, cudaStream_t st) {
 
 // Whole chain for nsub substacks whose descriptors are set (host side).  Leaves record
 // counts, region counts and the status word in c->h_counts after a stream sync.
-static int run_batch(hdog_ctx *c, int nsub, cudaStream_t st) {
+// Enqueues the whole chain for nsub substacks whose host descriptors are set, up to the
+// records in c->records (no host synchronization).
+static int enqueue_batch(hdog_ctx *c, int nsub, bool fused, cudaStream_t st) {
   TRY(upload_subs(c, nsub, st));
   zero_async(c->status, sizeof(int), st);
   if (c->p.erosion_radius_xy > 0 || c->p.erosion_radius_z > 0) {
@@ -603,9 +614,15 @@ static int run_batch(hdog_ctx *c, int nsub, cudaStream_t st) {
     TRY(upload_subs(c, nsub, st));
   }
   enqueue_normalize(c, nsub, c->norm, st);
-  const bool fused = fused_ok(c);
   if (fused) zero_async(c->fg_count, (size_t)nsub * kFgCountStride * sizeof(unsigned long long), st);
   enqueue_after_norm(c, nsub, fused, st);
+  HDOG_CUDA_TRY(cudaGetLastError());
+  return HDOG_OK;
+}
+
+static int run_batch(hdog_ctx *c, int nsub, cudaStream_t st) {
+  const bool fused = fused_ok(c);
+  TRY(enqueue_batch(c, nsub, fused, st));
   TRY(readback(c, nsub, st));
   if (fused) {
     bool over = false;
@@ -979,6 +996,388 @@ extern "C" int hdog_run_stacks(hdog_ctx *c, const hdog_stack_in *stacks, int n_s
     TRY(collect_records(c, nsub, c->last, st));
   }
   return copy_out(c->last, out, cap, n_records);
+}
+
+// ------------------------------------------------------------------ autotuner
+// Launch shapes of the two sweeps (one block per tile, or a persistent grid of a few
+// blocks per SM over the device work queue) and the substacks per launch of the graph
+// form, chosen by timing the caller's own first batch with CUDA events.  Results are cached
+// per device, frame shape, depth, tap radii, normalization radii and context size: every
+// candidate gives the same output, only the time differs.
+struct TuneResult {
+  LaunchShape shape;
+  int batch = 0;
+  std::string report;   // JSON of the timings behind the choice
+};
+static std::mutex g_tune_mu;
+static std::vector<std::pair<std::string, TuneResult>> g_tune_cache;
+
+static std::string tune_key(const hdog_ctx *c) {
+  char k[256];
+  snprintf(k, sizeof(k), "%d:%dx%dx%d:%d,%d,%d,%d:%d,%d:%d:%d", c->dev, c->W, c->H, c->D, c->taps.r[0], c->taps.r[1],
+           c->taps.r[2], c->taps.r[3], c->p.radius_norm_xy, c->p.radius_norm_z, c->max_sub,
+           (c->p.erosion_radius_xy || c->p.erosion_radius_z) ? 1 : 0);
+  return k;
+}
+
+static bool tune_lookup(hdog_ctx *c) {
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  const std::string k = tune_key(c);
+  for (auto &e : g_tune_cache)
+    if (e.first == k) {
+      c->shape = e.second.shape;
+      c->shape.num_sms = c->num_sms;
+      c->graph_batch = e.second.batch;
+      c->tune_report = e.second.report;
+      c->tuned = true;
+      return true;
+    }
+  return false;
+}
+
+// Milliseconds of each kernel name in the timer since the last collect.
+static double timer_ms(EventTimer &t, const char *name) {
+  for (auto &e : t.totals)
+    if (e.first == name) return e.second.ms;
+  return 0.0;
+}
+
+// Tunes the context on the batch of nsub substacks whose host descriptors are set (their
+// inputs in device memory).  Leaves the context's scratch with one of the runs' results.
+static int tune_batch(hdog_ctx *c, int nsub, cudaStream_t st) {
+  if (c->tuned || tune_lookup(c)) return HDOG_OK;
+  KernelTimer *saved = g_timer;
+  EventTimer timer;
+  g_timer = &timer;
+  struct Restore {
+    KernelTimer *saved;
+    ~Restore() { g_timer = saved; }
+  } restore{saved};
+  const bool fused = fused_ok(c);
+  struct Cand {
+    int dog, hess;
+  };
+  // grid form, and persistent grids at and below the sweeps' occupancy (three DoG blocks,
+  // five Hessian blocks per SM)
+  const Cand cands[] = {{0, 0}, {3, 5}, {2, 4}};
+  double dog_ms[3] = {0, 0, 0}, hess_ms[3] = {0, 0, 0}, all_ms[3] = {0, 0, 0};
+  c->shape = LaunchShape{};
+  c->shape.num_sms = c->num_sms;
+  TRY(enqueue_batch(c, nsub, fused, st));   // warm-up
+  HDOG_CUDA_TRY(cudaStreamSynchronize(st));
+  timer.collect();
+  timer.totals.clear();
+  for (int i = 0; i < (fused ? 3 : 1); i++) {
+    c->shape.dog_per_sm = cands[i].dog;
+    c->shape.hess_per_sm = cands[i].hess;
+    TRY(enqueue_batch(c, nsub, fused, st));
+    HDOG_CUDA_TRY(cudaStreamSynchronize(st));
+    timer.collect();
+    dog_ms[i] = timer_ms(timer, "k_dog_sweep");
+    hess_ms[i] = timer_ms(timer, "k_hess_sweep");
+    for (auto &e : timer.totals) all_ms[i] += e.second.ms;
+    timer.totals.clear();
+  }
+  int bd = 0, bh = 0;
+  for (int i = 1; i < (fused ? 3 : 1); i++) {
+    if (dog_ms[i] < dog_ms[bd]) bd = i;
+    if (hess_ms[i] < hess_ms[bh]) bh = i;
+  }
+  c->shape.dog_per_sm = cands[bd].dog;
+  c->shape.hess_per_sm = cands[bh].hess;
+  // substacks per launch: the full batch against half of it, by time per substack of the chain
+  int batch = nsub;
+  double half_ms = 0.0, full_ms = 0.0;
+  {
+    TRY(enqueue_batch(c, nsub, fused, st));
+    HDOG_CUDA_TRY(cudaStreamSynchronize(st));
+    timer.collect();
+    for (auto &e : timer.totals) full_ms += e.second.ms;
+    timer.totals.clear();
+    if (nsub >= 2) {
+      const int h = nsub / 2;
+      TRY(enqueue_batch(c, h, fused, st));
+      HDOG_CUDA_TRY(cudaStreamSynchronize(st));
+      timer.collect();
+      for (auto &e : timer.totals) half_ms += e.second.ms;
+      timer.totals.clear();
+      if (half_ms / h < full_ms / nsub) batch = h;
+    }
+  }
+  c->graph_batch = batch;
+  char rep[768];
+  snprintf(rep, sizeof(rep),
+           "{\"frame\": [%d, %d, %d], \"tuned_on_substacks\": %d, \"candidates\": [[0, 0], [3, 5], [2, 4]], "
+           "\"k_dog_sweep_ms\": [%.4f, %.4f, %.4f], \"k_hess_sweep_ms\": [%.4f, %.4f, %.4f], "
+           "\"dog_per_sm\": %d, \"hess_per_sm\": %d, \"chain_ms_full_batch\": %.4f, \"chain_ms_half_batch\": %.4f, "
+           "\"batch\": %d}",
+           c->W, c->H, c->D, nsub, dog_ms[0], dog_ms[1], dog_ms[2], hess_ms[0], hess_ms[1], hess_ms[2],
+           c->shape.dog_per_sm, c->shape.hess_per_sm, full_ms, half_ms, batch);
+  c->tune_report = rep;
+  c->tuned = true;
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  g_tune_cache.emplace_back(tune_key(c), TuneResult{c->shape, batch, c->tune_report});
+  return HDOG_OK;
+}
+
+extern "C" int hdog_autotune(hdog_ctx *c, const uint16_t *d_stack, int length, void *stream) {
+  CTX_GUARD(c);
+  if (!d_stack || length < 1) return fail(HDOG_ERR_ARG, "hdog_autotune: bad argument");
+  std::vector<int> z0s;
+  TRY(schedule(length, c->D, c->margin, z0s));
+  if (z0s.empty()) return fail(HDOG_ERR_ARG, "hdog_autotune: the stack has no substack");
+  const int nsub = (int)std::min(z0s.size(), (size_t)c->max_sub);
+  const size_t plane = (size_t)c->W * c->H;
+  for (int s = 0; s < nsub; s++)
+    set_sub(c, s, d_stack + (size_t)z0s[s] * plane, std::min(c->D, length - z0s[s]), z0s[s]);
+  c->tuned = false;
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    const std::string k = tune_key(c);
+    for (size_t i = 0; i < g_tune_cache.size(); i++)
+      if (g_tune_cache[i].first == k) {
+        g_tune_cache.erase(g_tune_cache.begin() + i);
+        break;
+      }
+  }
+  return tune_batch(c, nsub, (cudaStream_t)stream);
+}
+
+extern "C" int hdog_ctx_tuning(hdog_ctx *c, char *buf, size_t cap) {
+  if (!c || !buf || cap == 0) return fail(HDOG_ERR_ARG, "hdog_ctx_tuning: bad argument");
+  std::lock_guard<std::mutex> lock(c->mu);
+  const std::string &r = c->tuned ? c->tune_report : std::string("{}");
+  if (r.size() + 1 > cap) return fail(HDOG_ERR_CAPACITY, "hdog_ctx_tuning: buffer too small");
+  memcpy(buf, r.c_str(), r.size() + 1);
+  return HDOG_OK;
+}
+
+// ------------------------------------------------------------------ the batched graph form
+struct hdog_graph {
+  int dev = 0;
+  std::vector<hdog_ctx *> ctxs;          // distinct contexts, in locking order
+  std::vector<hdog_graph_stack> stacks;
+  std::vector<hdog_ctx *> stack_ctx;     // the context of each stack
+  std::vector<int64_t> stack_first;      // run index of each stack's first substack
+  std::vector<int64_t> stack_nsub;
+  int64_t n_sub = 0;
+  int64_t out_cap = 0;
+  void *dmem = nullptr;                  // header (total, redo) | slot table | records
+  int64_t *d_total = nullptr;
+  int *d_redo = nullptr;
+  GraphSlot *d_table = nullptr;
+  hdog_record *d_out = nullptr;
+  int64_t *h_hdr = nullptr;              // pinned: total, redo, then the slot table
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  RecordBuf staged;                      // the run's records as placed on the device
+  RecordBuf last;                        // the last run's records in the caller's order
+  std::vector<int64_t> last_counts;
+  std::mutex mu;
+};
+
+// Locks the contexts of a graph in a fixed order for the duration of a call.
+struct CtxLocks {
+  std::vector<std::unique_lock<std::mutex>> held;
+  explicit CtxLocks(const std::vector<hdog_ctx *> &cs) {
+    for (hdog_ctx *c : cs) held.emplace_back(c->mu);
+  }
+};
+
+extern "C" int hdog_graph_destroy(hdog_graph *g) {
+  if (!g) return HDOG_OK;
+  cudaSetDevice(g->dev);
+  if (g->exec) cudaGraphExecDestroy(g->exec);
+  if (g->graph) cudaGraphDestroy(g->graph);
+  if (g->dmem) cudaFree(g->dmem);
+  if (g->h_hdr) cudaFreeHost(g->h_hdr);
+  g->staged.release();
+  g->last.release();
+  delete g;
+  return HDOG_OK;
+}
+
+extern "C" int hdog_graph_create(hdog_ctx *const *ctxs, int n_ctx, const hdog_graph_stack *stacks, int n_stacks,
+                                 void *stream, hdog_graph **out) {
+  if (!out) return fail(HDOG_ERR_ARG, "hdog_graph_create: null output pointer");
+  *out = nullptr;
+  if (!ctxs || n_ctx < 1 || n_stacks < 0 || (n_stacks > 0 && !stacks))
+    return fail(HDOG_ERR_ARG, "hdog_graph_create: bad argument");
+  cudaStream_t st = (cudaStream_t)stream;
+  std::unique_ptr<hdog_graph, int (*)(hdog_graph *)> g(new hdog_graph(), hdog_graph_destroy);
+  for (int i = 0; i < n_ctx; i++) {
+    if (!ctxs[i]) return fail(HDOG_ERR_ARG, "hdog_graph_create: null context");
+    if (ctxs[i]->dev != ctxs[0]->dev) return fail(HDOG_ERR_ARG, "hdog_graph_create: contexts on different devices");
+    if (ctxs[i]->max_sub > kGraphMaxBatch)
+      return fail(HDOG_ERR_ARG, "hdog_graph_create: contexts of at most 16 substacks");
+    for (int j = 0; j < i; j++)
+      if (ctxs[j] == ctxs[i] || (ctxs[j]->W == ctxs[i]->W && ctxs[j]->H == ctxs[i]->H))
+        return fail(HDOG_ERR_ARG, "hdog_graph_create: one context per frame shape");
+    g->ctxs.push_back(ctxs[i]);
+  }
+  std::sort(g->ctxs.begin(), g->ctxs.end());
+  g->dev = ctxs[0]->dev;
+  HDOG_CUDA_TRY(cudaSetDevice(g->dev));
+  CtxLocks locks(g->ctxs);
+  // every stack's substacks in the caller's order; each stack goes to the context of its frame
+  std::vector<std::vector<int>> z0_of(n_stacks);
+  int64_t processed = 0;
+  for (int i = 0; i < n_stacks; i++) {
+    const hdog_graph_stack &sp = stacks[i];
+    if (!sp.data || sp.length < 0) return fail(HDOG_ERR_ARG, "hdog_graph_create: bad stack");
+    hdog_ctx *c = nullptr;
+    for (hdog_ctx *x : g->ctxs)
+      if (x->W == sp.width && x->H == sp.height) c = x;
+    if (!c) return fail(HDOG_ERR_ARG, "hdog_graph_create: no context for a stack's frame shape");
+    TRY(schedule(sp.length, c->D, c->margin, z0_of[i]));
+    g->stacks.push_back(sp);
+    g->stack_ctx.push_back(c);
+    g->stack_first.push_back(g->n_sub);
+    g->stack_nsub.push_back((int64_t)z0_of[i].size());
+    g->n_sub += (int64_t)z0_of[i].size();
+    processed += (int64_t)z0_of[i].size() * c->nvox;
+  }
+  g->out_cap = std::max<int64_t>(65536, processed / 512);
+  const size_t table_bytes = align256((size_t)std::max<int64_t>(g->n_sub, 1) * sizeof(GraphSlot));
+  if (cudaMalloc(&g->dmem, 256 + table_bytes + (size_t)g->out_cap * sizeof(hdog_record)) != cudaSuccess)
+    return fail(HDOG_ERR_NOMEM, "hdog_graph_create: no device memory for the run's records");
+  g->d_total = (int64_t *)g->dmem;
+  g->d_redo = (int *)((char *)g->dmem + 8);
+  g->d_table = (GraphSlot *)((char *)g->dmem + 256);
+  g->d_out = (hdog_record *)((char *)g->dmem + 256 + table_bytes);
+  if (cudaMallocHost(&g->h_hdr, 16 + (size_t)std::max<int64_t>(g->n_sub, 1) * sizeof(GraphSlot)) != cudaSuccess)
+    return fail(HDOG_ERR_NOMEM, "hdog_graph_create: pinned host memory");
+  // per context: its substacks (stack by stack), the first batch tunes the launch shapes
+  struct Item {
+    int stack;
+    int z0;
+    int64_t id;
+  };
+  std::vector<std::vector<Item>> items(g->ctxs.size());
+  for (int i = 0; i < n_stacks; i++) {
+    const size_t k = std::find(g->ctxs.begin(), g->ctxs.end(), g->stack_ctx[i]) - g->ctxs.begin();
+    for (size_t j = 0; j < z0_of[i].size(); j++) items[k].push_back({i, z0_of[i][j], g->stack_first[i] + (int64_t)j});
+  }
+  auto set_item = [&](hdog_ctx *c, int s, const Item &it) {
+    const hdog_graph_stack &sp = g->stacks[it.stack];
+    set_sub(c, s, sp.data + (size_t)it.z0 * c->W * c->H, std::min(c->D, sp.length - it.z0), it.z0);
+  };
+  for (size_t k = 0; k < g->ctxs.size(); k++) {
+    hdog_ctx *c = g->ctxs[k];
+    if (items[k].empty()) continue;
+    const int nsub = (int)std::min(items[k].size(), (size_t)c->max_sub);
+    for (int s = 0; s < nsub; s++) set_item(c, s, items[k][s]);
+    TRY(tune_batch(c, nsub, st));
+  }
+  // capture every batch of every context, with the record placement after each, on a
+  // stream of its own (the caller's may be the legacy default stream, which cannot capture)
+  HDOG_CUDA_TRY(cudaStreamSynchronize(st));
+  struct CapStream {
+    cudaStream_t s = nullptr;
+    ~CapStream() {
+      if (s) cudaStreamDestroy(s);
+    }
+  } cap;
+  HDOG_CUDA_TRY(cudaStreamCreateWithFlags(&cap.s, cudaStreamNonBlocking));
+  st = cap.s;
+  KernelTimer *saved_timer = g_timer;
+  g_timer = nullptr;
+  HDOG_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  int rc = HDOG_OK;
+  zero_async(g->dmem, 256, st);
+  for (size_t k = 0; k < g->ctxs.size() && rc == HDOG_OK; k++) {
+    hdog_ctx *c = g->ctxs[k];
+    const bool fused = fused_ok(c);
+    const size_t per = (size_t)std::max(1, c->graph_batch > 0 ? c->graph_batch : c->max_sub);
+    for (size_t b = 0; b < items[k].size() && rc == HDOG_OK; b += per) {
+      const int nsub = (int)std::min(per, items[k].size() - b);
+      GraphIds ids{};
+      for (int s = 0; s < nsub; s++) {
+        set_item(c, s, items[k][b + s]);
+        ids.id[s] = (int)items[k][b + s].id;
+      }
+      rc = enqueue_batch(c, nsub, fused, st);
+      if (rc != HDOG_OK) break;
+      launch_graph_place(nsub, ids, c->num_records, c->fg_count, c->fg_cap, fused, c->status, g->d_total, g->d_table,
+                         g->d_redo, g->out_cap, st);
+      launch_graph_copy(nsub, ids, c->records, c->reg_cap, g->d_table, g->d_out, g->out_cap, st);
+    }
+  }
+  cudaGraph_t graph = nullptr;
+  const cudaError_t ec = cudaStreamEndCapture(st, &graph);
+  g_timer = saved_timer;
+  if (rc != HDOG_OK) {
+    if (graph) cudaGraphDestroy(graph);
+    return rc;
+  }
+  if (ec != cudaSuccess) return hdog_set_cuda_error(ec, "hdog_graph_create: stream capture");
+  g->graph = graph;
+  HDOG_CUDA_TRY(cudaGraphInstantiate(&g->exec, g->graph, 0));
+  *out = g.release();
+  return HDOG_OK;
+}
+
+extern "C" int hdog_graph_run(hdog_graph *g, hdog_record *out, int64_t cap, int64_t *n_records, int64_t *stack_counts,
+                              void *stream) {
+  if (!g || !n_records || (cap > 0 && !out)) return fail(HDOG_ERR_ARG, "hdog_graph_run: bad argument");
+  std::lock_guard<std::mutex> glock(g->mu);
+  HDOG_CUDA_TRY(cudaSetDevice(g->dev));
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t nst = g->stacks.size();
+  g->last.clear();
+  g->last_counts.assign(nst, 0);
+  bool redo = false;
+  {
+    CtxLocks locks(g->ctxs);
+    HDOG_CUDA_TRY(cudaGraphLaunch(g->exec, st));
+    HDOG_CUDA_TRY(cudaMemcpyAsync(g->h_hdr, g->dmem, 16, cudaMemcpyDeviceToHost, st));
+    if (g->n_sub > 0)
+      HDOG_CUDA_TRY(cudaMemcpyAsync(g->h_hdr + 2, g->d_table, (size_t)g->n_sub * sizeof(GraphSlot),
+                                    cudaMemcpyDeviceToHost, st));
+    HDOG_CUDA_TRY(cudaStreamSynchronize(st));
+    const int64_t total = g->h_hdr[0];
+    redo = (int)(g->h_hdr[1] & 0xFFFFFFFF) != 0 || total > g->out_cap;
+    if (!redo) {
+      if (!g->staged.reserve((size_t)total) || !g->last.reserve((size_t)total))
+        return fail(HDOG_ERR_NOMEM, "page-locked host buffer for the records failed");
+      if (total > 0)
+        HDOG_CUDA_TRY(cudaMemcpyAsync(g->staged.p, g->d_out, (size_t)total * sizeof(hdog_record), cudaMemcpyDeviceToHost,
+                                      st));
+      HDOG_CUDA_TRY(cudaStreamSynchronize(st));
+      g->staged.n = (size_t)total;
+      const GraphSlot *table = reinterpret_cast<const GraphSlot *>(g->h_hdr + 2);
+      size_t n = 0;
+      for (size_t i = 0; i < nst; i++)
+        for (int64_t j = 0; j < g->stack_nsub[i]; j++) {
+          const GraphSlot &sl = table[g->stack_first[i] + j];
+          if (sl.count > 0) memcpy(g->last.p + n, g->staged.p + sl.off, (size_t)sl.count * sizeof(hdog_record));
+          n += (size_t)sl.count;
+          g->last_counts[i] += sl.count;
+        }
+      g->last.n = n;
+    }
+  }
+  if (redo) {
+    // a batch needed the host's fallback (foreground list or region capacity, a bounded
+    // loop, or more records than the run's array holds): rerun stack by stack without the graph
+    g->last.clear();
+    for (size_t i = 0; i < nst; i++) {
+      hdog_ctx *c = g->stack_ctx[i];
+      std::lock_guard<std::mutex> lock(c->mu);
+      const size_t before = g->last.n;
+      TRY(run_stack_locked(c, g->stacks[i].data, 1, g->stacks[i].length, g->last, st));
+      g->last_counts[i] = (int64_t)(g->last.n - before);
+    }
+  }
+  if (stack_counts)
+    for (size_t i = 0; i < nst; i++) stack_counts[i] = g->last_counts[i];
+  return copy_out(g->last, out, cap, n_records);
+}
+
+extern "C" int hdog_graph_last_records(hdog_graph *g, hdog_record *out, int64_t cap, int64_t *n_records) {
+  if (!g || !n_records || (cap > 0 && !out)) return fail(HDOG_ERR_ARG, "hdog_graph_last_records: bad argument");
+  std::lock_guard<std::mutex> lock(g->mu);
+  return copy_out(g->last, out, cap, n_records);
 }
 
 // ------------------------------------------------------------------ differentiable chain

@@ -24,6 +24,23 @@ struct Sub {
   const uint16_t *src;    // slice 0 of the raw input (device); slices are W*H apart
 };
 
+// A device work queue of (substack, tile) items for a persistent launch: item i is tile
+// i % tiles of substack i / tiles; blocks take items with atomicAdd on *next (zeroed before
+// the launch) until it passes total.
+struct WorkQueue {
+  unsigned *next;
+  int total;
+  int tiles;
+};
+
+// Launch shape of the sweeps: blocks per SM of a persistent launch over the work queue, or
+// 0 for one block per tile and substack.  Chosen per frame shape by the autotuner.
+struct LaunchShape {
+  int dog_per_sm = 0;
+  int hess_per_sm = 0;
+  int num_sms = 152;
+};
+
 // Foreground-list counters of the substacks of a batch sit kFgCountStride 64-bit slots
 // apart: every warp of the Hessian sweep takes its list slots with an atomic on its
 // substack's counter, and counters on separate 4 KB lines spread those atomics over L2.
@@ -108,9 +125,10 @@ bool launch_dog_sweep(const Sub *d_subs, int nsub, int W, int H, int D, const Do
                       float *dog, int *d_status, int max_smem, cudaStream_t s);
 // DoG + Hessian + PD: the radius-specialised pair (norm -> dog -> mask + list) when the tap
 // radii have an instantiation, else the generic fused sweep (dog untouched).
+// ls / qctr (two device counters): the launch shape of the radius-specialised sweeps.
 int launch_dog_hess(const Sub *d_subs, int nsub, int W, int H, int D, const DogTaps &T, const float *norm,
                     float *dog, uint8_t *mask, FgEntry *fg, int32_t *fg_idx, unsigned long long *fg_count,
-                    int *d_status, cudaStream_t s);
+                    int *d_status, const LaunchShape &ls, unsigned *qctr, cudaStream_t s);
 // ---- ccl.cu ----
 // Segments of a per-substack scan: substack s scans len[s] counts starting at off[s];
 // chk[s] is its offset in the chunk-sum scratch (one slot per 1024 counts).
@@ -142,6 +160,20 @@ void launch_finalize(const Sub *d_subs, int nsub, int64_t max_reg_cap, const Sca
                      const int64_t *d_num_regions, RegionAcc acc, int64_t slots, RegionOut out,
                      FilterParams fp, uint32_t *blk_counts, uint32_t *blk_offsets, uint32_t *chunk,
                      int64_t *d_num_records, hdog_record *records, int64_t blk_stride, cudaStream_t s);
+
+// ---- graph.cu: record placement of the batched graph form ----
+constexpr int kGraphMaxBatch = 16;   // substacks per batch in the graph form
+struct GraphIds {
+  int id[kGraphMaxBatch];            // the run's index of each batch substack
+};
+struct GraphSlot {
+  long long off, count;              // a substack's records in the run's record array
+};
+void launch_graph_place(int nsub, const GraphIds &ids, const int64_t *num_records, const unsigned long long *fg_count,
+                        int64_t fg_cap, bool fused, const int *status, int64_t *total, GraphSlot *table, int *redo,
+                        int64_t out_cap, cudaStream_t s);
+void launch_graph_copy(int nsub, const GraphIds &ids, const hdog_record *records, int64_t reg_cap,
+                       const GraphSlot *table, hdog_record *out, int64_t out_cap, cudaStream_t s);
 
 constexpr int kMaxRadiusXY = 421;    // shared-memory bound of the min/max x and y passes
 constexpr int kScanBlock = 4096;     // voxels per block in the region scans (16 per thread)

@@ -23,6 +23,8 @@
 // kernel finishes without further waits.
 #include <cuda.h>
 
+#include <algorithm>
+
 #include <type_traits>
 
 #include "kernels.cuh"
@@ -454,22 +456,21 @@ __device__ __forceinline__ void unroll_steps(F &f, int base, int limit) {
   unroll_steps_from<0, N>(f, base, limit);
 }
 
-template <int RA, int RB, int ZA, int ZB>
+// PERSIST: a grid of a few blocks per SM takes (substack, tile) items from the device work
+// queue `q` until it is empty; otherwise one block per tile (blockIdx.x) and substack
+// (blockIdx.y).  Results are the same either way.
+template <int RA, int RB, int ZA, int ZB, bool PERSIST>
 __global__ void __launch_bounds__(DogT<RA, RB, ZA, ZB>::NT, 3)
     k_dog_sweep(const __grid_constant__ CUtensorMap map, const __grid_constant__ DogTaps T, const Sub *subs,
-                float *dog, int *status) {
+                float *dog, int *status, WorkQueue q) {
   using C = DogT<RA, RB, ZA, ZB>;
   extern __shared__ __align__(128) unsigned char smem[];
-  const Sub S = subs[blockIdx.y];
-  const int ntx = (S.W + kDTX - 1) / kDTX, nty = (S.H + kDTY - 1) / kDTY;
-  if ((int64_t)blockIdx.x >= (int64_t)ntx * nty) return;
-  const int x0 = (int)(blockIdx.x % ntx) * kDTX, y0 = (int)(blockIdx.x / ntx) * kDTY;
   float *inb = reinterpret_cast<float *>(smem);
   float2 *xb = reinterpret_cast<float2 *>(smem + (size_t)2 * C::IN_FLOATS * 4);
   uint64_t *bar = reinterpret_cast<uint64_t *>(smem + (size_t)2 * C::IN_FLOATS * 4 + (size_t)2 * C::BH * kDTX * 8);
   const int t = threadIdx.x;
-  const int D = S.D, W = S.W, H = S.H;
   __shared__ float2 tap_sh[TapPairs<RA, RB>::N + TapPairs<ZA, ZB>::N];
+  __shared__ int s_item;
   if (t == 0) {
     mbar_init(&bar[0], 1);
     mbar_init(&bar[1], 1);
@@ -477,11 +478,35 @@ __global__ void __launch_bounds__(DogT<RA, RB, ZA, ZB>::NT, 3)
     TapPairs<RA, RB>::stage(T, 0, 2, tap_sh);
     TapPairs<ZA, ZB>::stage(T, 1, 3, tap_sh + TapPairs<RA, RB>::N);
   }
-  __syncthreads();
+  bool ok = true;
+  // slices loaded by this block before the current tile: slice `it` of a tile is the block's
+  // (gbase + it)-th, which picks its input buffer and barrier phase
+  uint32_t gbase = 0;
+  for (;;) {
+  int sub, tile;
+  __syncthreads();   // the previous tile is done with both input buffers
+  if (PERSIST) {
+    if (t == 0) s_item = (int)atomicAdd(q.next, 1u);
+    __syncthreads();
+    const int item = s_item;
+    if (item >= q.total) break;
+    sub = item / q.tiles;
+    tile = item % q.tiles;
+  } else {
+    sub = blockIdx.y;
+    tile = blockIdx.x;
+  }
+  const Sub S = subs[sub];
+  const int ntx = (S.W + kDTX - 1) / kDTX, nty = (S.H + kDTY - 1) / kDTY;
+  if (tile >= ntx * nty) {
+    if (PERSIST) continue;
+    break;
+  }
+  const int x0 = (tile % ntx) * kDTX, y0 = (tile / ntx) * kDTY;
+  const int D = S.D, W = S.W, H = S.H;
   constexpr uint32_t tma_bytes = (uint32_t)(C::BW * C::BH * 4);
   const int tx = x0 - C::HX, ty = y0 - C::RXY;
-  if (t == 0 && D > 0) tma_slice(&map, inb, &bar[0], tx, ty, 0, blockIdx.y, tma_bytes);
-  bool ok = true;
+  if (t == 0 && ok && D > 0) tma_slice(&map, inb + (gbase & 1) * C::IN_FLOATS, &bar[gbase & 1], tx, ty, 0, sub, tma_bytes);
   // stage B ownership: columns (cx, cy) and (cx, cy + 1) of the tile
   const int cx = t % kDTX, cy = 2 * (t / kDTX);
   const int gx = x0 + cx, gy = y0 + cy;
@@ -501,8 +526,9 @@ __global__ void __launch_bounds__(DogT<RA, RB, ZA, ZB>::NT, 3)
   // is a fixed register (the loop below runs WIN steps per trip).
   auto step = [&](int it, auto PC) {
     constexpr int PH = (decltype(PC)::value + C::WIN - 1) % C::WIN;
+    const uint32_t gn = gbase + (uint32_t)it + 1u;   // the block's count of slice it + 1
     if (t == 0 && ok && it + 1 < D)
-      tma_slice(&map, inb + ((it + 1) & 1) * C::IN_FLOATS, &bar[(it + 1) & 1], tx, ty, it + 1, blockIdx.y, tma_bytes);
+      tma_slice(&map, inb + (gn & 1) * C::IN_FLOATS, &bar[gn & 1], tx, ty, it + 1, sub, tma_bytes);
     // ---- B: y pass of slice zy (zero past the volume: the border taps still multiply),
     // z shift register, DoG slice zy - RZ
     const int zy = it - 1;
@@ -521,11 +547,12 @@ __global__ void __launch_bounds__(DogT<RA, RB, ZA, ZB>::NT, 3)
     }
     // ---- A: x pass of slice it
     if (it < D) {
-      if (ok && !mbar_wait(&bar[it & 1], (it >> 1) & 1)) {
+      const uint32_t gi = gbase + (uint32_t)it;
+      if (ok && !mbar_wait(&bar[gi & 1], (gi >> 1) & 1)) {
         ok = false;
         atomicExch(status, HDOG_ERR_TIMEOUT);
       }
-      const float *ib = inb + (it & 1) * C::IN_FLOATS;
+      const float *ib = inb + (gi & 1) * C::IN_FLOATS;
       float2 *xo = xb + (it & 1) * C::BH * kDTX;
       for (int item = t; item < C::XITEMS; item += C::NT) {
         const int row = item / C::XQ, q = item % C::XQ;
@@ -547,6 +574,9 @@ __global__ void __launch_bounds__(DogT<RA, RB, ZA, ZB>::NT, 3)
   };
   for (int base = 0; base < nit; base += C::WIN)
     unroll_steps<C::WIN>(step, base, nit);
+  gbase += (uint32_t)D;
+  if (!PERSIST) break;
+  }
 }
 
 // Central difference of the Hessian stage.  The reference writes ((0 + a) - b) * 0.5; the
@@ -603,10 +633,12 @@ __device__ __forceinline__ void ld_quad(const float *p, float2 &c0, float2 &c1) 
 constexpr int kHStage = 128;
 
 // Moves a warp's `n` staged entries to the substack's list: one slot reservation, then
-// 16-byte stores over consecutive entries.  Entries past the list's capacity are dropped
-// but counted, so the host sees the overflow and redoes the batch.
-__device__ __forceinline__ void flush_stage(const FgEntry *stage, int n, const Sub &S, FgEntry *fg, int32_t *fg_idx,
-                                            unsigned long long *count) {
+// each lane completes whole entries -- the normalized value at the entry's voxel is
+// gathered here, once per flush rather than on every slice -- and stores them as
+// consecutive 32-byte entries.  Entries past the list's capacity are dropped but counted,
+// so the host sees the overflow and redoes the batch.
+__device__ __forceinline__ void flush_stage(const FgEntry *stage, int n, const Sub &S, const float *norm, FgEntry *fg,
+                                            int32_t *fg_idx, unsigned long long *count) {
   __syncwarp();
   const int lane = threadIdx.x & 31;
   unsigned long long base = 0;
@@ -614,10 +646,18 @@ __device__ __forceinline__ void flush_stage(const FgEntry *stage, int n, const S
   base = __shfl_sync(0xFFFFFFFFu, base, 0);
   const int64_t room = S.fg_cap - (int64_t)base;
   const int keep = room <= 0 ? 0 : (room < n ? (int)room : n);
-  const float4 *src = reinterpret_cast<const float4 *>(stage);
-  float4 *dst = reinterpret_cast<float4 *>(fg + S.fg + base);
-  for (int i = lane; i < 2 * keep; i += 32) dst[i] = src[i];
-  for (int i = lane; i < keep; i += 32) fg_idx[S.fg + base + i] = stage[i].idx;
+  const float *nv = norm + S.vox;
+  for (int i = lane; i < keep; i += 32) {
+    const float4 *src = reinterpret_cast<const float4 *>(stage + i);
+    float4 a = src[0];
+    const float4 b = src[1];
+    const int32_t idx = __float_as_int(a.x);
+    a.y = __ldg(nv + idx);
+    float4 *dst = reinterpret_cast<float4 *>(fg + S.fg + base + i);
+    dst[0] = a;
+    dst[1] = b;
+    fg_idx[S.fg + base + i] = idx;
+  }
   __syncwarp();
 }
 
@@ -626,44 +666,69 @@ __device__ __forceinline__ void flush_stage(const FgEntry *stage, int n, const S
 #ifndef HDOG_HESS_BLOCKS
 #define HDOG_HESS_BLOCKS 5
 #endif
+// PERSIST: a grid of a few blocks per SM takes (substack, tile) items from the device work
+// queue `q` until it is empty; otherwise one block per tile (blockIdx.x) and substack
+// (blockIdx.y).  Results are the same either way.
+template <bool PERSIST>
 __global__ void __launch_bounds__(kHThreads, HDOG_HESS_BLOCKS)
     k_hess_sweep(const __grid_constant__ CUtensorMap map, const Sub *subs, const float *norm, uint8_t *mask,
-                 FgEntry *fg, int32_t *fg_idx, unsigned long long *fg_count, int *status) {
+                 FgEntry *fg, int32_t *fg_idx, unsigned long long *fg_count, int *status, WorkQueue q) {
   extern __shared__ __align__(128) unsigned char smem[];
   constexpr int PL = kHPX * kHPY;
   constexpr uint32_t tma_bytes = (uint32_t)(PL * 4);
-  const Sub S = subs[blockIdx.y];
-  const int ntx = (S.W + kHTX - 1) / kHTX, nty = (S.H + kHTY - 1) / kHTY;
-  if ((int64_t)blockIdx.x >= (int64_t)ntx * nty) return;
-  const int x0 = (int)(blockIdx.x % ntx) * kHTX, y0 = (int)(blockIdx.x / ntx) * kHTY;
   float *ring = reinterpret_cast<float *>(smem);
   uint64_t *bar = reinterpret_cast<uint64_t *>(smem + (size_t)kHRing * PL * 4);
-  // done[zh % kHRing] completes when every warp has finished iteration zh, with its last
-  // reads of DoG slice zh-2
+  // done[i % kHRing] completes when every warp has finished the block's i-th iteration, with
+  // its last reads of that iteration's DoG slice zh-2
   uint64_t *done = bar + kHRing;
   const int t = threadIdx.x;
   // this warp's staging of list entries (flushed to the global list kHStage at a time at most)
   FgEntry *stage = reinterpret_cast<FgEntry *>(smem + (size_t)kHRing * PL * 4 + 2 * kHRing * 8) + (t >> 5) * kHStage;
-  int staged = 0;   // entries in this warp's staging buffer (the same in every lane)
-  const int D = S.D, W = S.W, H = S.H;
-  const int32_t WH = W * H;
+  __shared__ int s_item;
   if (t == 0) {
     for (int i = 0; i < kHRing; i++) mbar_init(&bar[i], 1);
     for (int i = 0; i < kHRing; i++) mbar_init(&done[i], kHThreads / 32);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  __syncthreads();
+  bool ok = true;
+  // slices loaded into the ring and iterations run by this block before the current tile:
+  // every tile loads its slices -2 .. D+1 once and runs D iterations, so the barrier phases
+  // continue from tile to tile
+  uint32_t zbase = 0, ibase = 0;
+  for (;;) {
+  int sub, tile;
+  __syncthreads();   // every warp is done with the previous tile's ring slots
+  if (PERSIST) {
+    if (t == 0) s_item = (int)atomicAdd(q.next, 1u);
+    __syncthreads();
+    const int item = s_item;
+    if (item >= q.total) break;
+    sub = item / q.tiles;
+    tile = item % q.tiles;
+  } else {
+    sub = blockIdx.y;
+    tile = blockIdx.x;
+  }
+  const Sub S = subs[sub];
+  const int ntx = (S.W + kHTX - 1) / kHTX, nty = (S.H + kHTY - 1) / kHTY;
+  if (tile >= ntx * nty) {
+    if (PERSIST) continue;
+    break;
+  }
+  const int x0 = (tile % ntx) * kHTX, y0 = (tile / ntx) * kHTY;
+  int staged = 0;   // entries in this warp's staging buffer (the same in every lane)
+  const int D = S.D, W = S.W, H = S.H;
+  const int32_t WH = W * H;
   const int tx = x0 - 4, ty = y0 - 2;
   // ring slot of DoG slice z (z = -2 .. D+1; slices outside the volume arrive zero-filled)
-  auto slot = [](int z) { return (z + 2 * kHRing) % kHRing; };
+  auto slot = [zbase](int z) { return (int)((zbase + (uint32_t)(z + 2)) % kHRing); };
   // use k of slot s (k-th slice loaded into it) completes barrier phase k & 1
-  auto use = [](int z) { return (z + 2) / kHRing; };
+  auto use = [zbase](int z) { return (int)((zbase + (uint32_t)(z + 2)) / kHRing); };
   // slices -2 .. 4 up front, then slice zh + 5 while slice zh is tested: the slot it
   // reuses held slice zh - 3, last read one barrier earlier
-  if (t == 0)
+  if (t == 0 && ok)
     for (int z = -2; z <= 4 && z <= D + 1; z++)
-      tma_slice(&map, ring + slot(z) * PL, &bar[slot(z)], tx, ty, z, blockIdx.y, tma_bytes);
-  bool ok = true;
+      tma_slice(&map, ring + slot(z) * PL, &bar[slot(z)], tx, ty, z, sub, tma_bytes);
   for (int z = -2; z <= 1; z++)
     if (ok && !mbar_wait(&bar[slot(z)], use(z) & 1)) {
       ok = false;
@@ -704,11 +769,12 @@ __global__ void __launch_bounds__(kHThreads, HDOG_HESS_BLOCKS)
     // zh-1: the producer waits until every warp is past it (warps otherwise run up to the
     // ring's depth apart)
     if (t == 0 && ok && zh + 5 <= D + 1) {
-      if (zh >= 1 && !mbar_wait(&done[(zh - 1) % kHRing], ((zh - 1) / kHRing) & 1)) {
+      const uint32_t prev = ibase + (uint32_t)zh - 1u;
+      if (zh >= 1 && !mbar_wait(&done[prev % kHRing], (prev / kHRing) & 1)) {
         ok = false;
         atomicExch(status, HDOG_ERR_TIMEOUT);
       }
-      if (ok) tma_slice(&map, ring + slot(zh + 5) * PL, &bar[slot(zh + 5)], tx, ty, zh + 5, blockIdx.y, tma_bytes);
+      if (ok) tma_slice(&map, ring + slot(zh + 5) * PL, &bar[slot(zh + 5)], tx, ty, zh + 5, sub, tma_bytes);
     }
     // slices zh-2 .. zh+1 were waited for already; zh+2 is new
     if (ok && !mbar_wait(&bar[slot(zh + 2)], use(zh + 2) & 1)) {
@@ -822,14 +888,12 @@ __global__ void __launch_bounds__(kHThreads, HDOG_HESS_BLOCKS)
       }
     }
     // the foreground voxels go to the warp's staging buffer in shared memory; a full buffer
-    // goes to the global list with one slot reservation and coalesced stores.  Warps
-    // without foreground skip all of it; each lane's place comes from three bit-sliced
-    // ballots of its count.  The normalized values of the quad (one 16-byte load, W % 4 ==
-    // 0) are read only by threads with foreground.
+    // goes to the global list with one slot reservation and coalesced stores (and the
+    // entries' normalized values).  Warps without foreground skip all of it; each lane's
+    // place comes from three bit-sliced ballots of its count.
     const int nfg = __popc(mword);
     const unsigned any = __ballot_sync(0xFFFFFFFFu, nfg != 0);
     if (any) {
-      const float4 nq = nfg ? __ldg(reinterpret_cast<const float4 *>(norm + S.vox + i0)) : make_float4(0.f, 0.f, 0.f, 0.f);
       const int lane = t & 31;
       const unsigned b0 = __ballot_sync(0xFFFFFFFFu, nfg & 1), b1 = __ballot_sync(0xFFFFFFFFu, nfg & 2),
                      b2 = __ballot_sync(0xFFFFFFFFu, nfg & 4);
@@ -837,25 +901,28 @@ __global__ void __launch_bounds__(kHThreads, HDOG_HESS_BLOCKS)
       const int excl = __popc(b0 & lt) + 2 * __popc(b1 & lt) + 4 * __popc(b2 & lt);
       const int tot = __popc(b0) + 2 * __popc(b1) + 4 * __popc(b2);
       if (staged + tot > kHStage) {
-        flush_stage(stage, staged, S, fg, fg_idx, &fg_count[blockIdx.y * kFgCountStride]);
+        flush_stage(stage, staged, S, norm, fg, fg_idx, &fg_count[sub * kFgCountStride]);
         staged = 0;
       }
-      const float nv[4] = {nq.x, nq.y, nq.z, nq.w};
       int k = staged + excl;
 #pragma unroll
       for (int o = 0; o < 4; o++) {
         if (!((mword >> (8 * o)) & 1u)) continue;
         float4 *dst = reinterpret_cast<float4 *>(stage + k);
-        dst[0] = make_float4(__int_as_float(i0 + o), nv[o], hv[o][0], hv[o][1]);
+        dst[0] = make_float4(__int_as_float(i0 + o), 0.0f, hv[o][0], hv[o][1]);
         dst[1] = make_float4(hv[o][2], hv[o][3], hv[o][4], hv[o][5]);
         k++;
       }
       staged += tot;
     }
     __syncwarp();
-    if ((t & 31) == 0) mbar_arrive(&done[zh % kHRing]);
+    if ((t & 31) == 0) mbar_arrive(&done[(ibase + (uint32_t)zh) % kHRing]);
   }
-  if (staged) flush_stage(stage, staged, S, fg, fg_idx, &fg_count[blockIdx.y * kFgCountStride]);
+  if (staged) flush_stage(stage, staged, S, norm, fg, fg_idx, &fg_count[sub * kFgCountStride]);
+  zbase += (uint32_t)(D + 4);
+  ibase += (uint32_t)D;
+  if (!PERSIST) break;
+  }
 }
 
 // ------------------------------------------------------------------ host side
@@ -877,17 +944,18 @@ static EncodeTiledFn encode_fn() {
 
 // Radius-specialised instantiations: (small xy, large xy, small z, large z) tap radii.
 // (4, 6, 3, 5): sigma (2.0, 1.5) / (3.2, 2.4); (8, 12, 4, 5): sigma (4.0, 1.8) / (6.0, 2.7).
-typedef void (*DogSweepKernel)(CUtensorMap, DogTaps, const Sub *, float *, int *);
+typedef void (*DogSweepKernel)(CUtensorMap, DogTaps, const Sub *, float *, int *, WorkQueue);
 struct SweepInst {
   int ra, rb, za, zb;
-  DogSweepKernel fn;
+  DogSweepKernel fn, fn_persist;
   size_t smem;
   int threads, bw, bh, hx, rxy;
 };
 template <int RA, int RB, int ZA, int ZB>
 constexpr SweepInst sweep_inst() {
   using C = DogT<RA, RB, ZA, ZB>;
-  return SweepInst{RA, RB, ZA, ZB, k_dog_sweep<RA, RB, ZA, ZB>, C::SMEM, C::NT, C::BW, C::BH, C::HX, C::RXY};
+  return SweepInst{RA, RB, ZA, ZB, k_dog_sweep<RA, RB, ZA, ZB, false>, k_dog_sweep<RA, RB, ZA, ZB, true>,
+                   C::SMEM, C::NT, C::BW, C::BH, C::HX, C::RXY};
 }
 static const SweepInst kSweepInst[] = {sweep_inst<4, 6, 3, 5>(), sweep_inst<8, 12, 4, 5>()};
 
@@ -921,6 +989,25 @@ static CUresult encode_map(CUtensorMap *map, const float *base, int W, int H, in
                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
 }
 
+// One launch of a radius-specialised DoG sweep: a block per tile and substack, or (per_sm > 0)
+// per_sm blocks per SM over the work queue whose counter is *qctr (zeroed here first).
+static void dog_sweep_launch(const SweepInst *si, const CUtensorMap &map_n, const DogTaps &T, const Sub *d_subs,
+                             int nsub, int W, int H, float *dog, int *d_status, const LaunchShape &ls,
+                             unsigned *qctr, cudaStream_t s) {
+  const unsigned tiles_d = ceil_div(W, kDTX) * ceil_div(H, kDTY);
+  if (ls.dog_per_sm > 0 && qctr) {
+    zero_async(qctr, sizeof(unsigned), s);
+    const WorkQueue q{qctr, (int)(tiles_d * (unsigned)nsub), (int)tiles_d};
+    const unsigned grid = std::min<unsigned>((unsigned)(ls.dog_per_sm * ls.num_sms), tiles_d * (unsigned)nsub);
+    cudaFuncSetAttribute(si->fn_persist, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)si->smem);
+    KLAUNCH("k_dog_sweep", s, (si->fn_persist<<<grid, si->threads, si->smem, s>>>(map_n, T, d_subs, dog, d_status, q)));
+    return;
+  }
+  cudaFuncSetAttribute(si->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)si->smem);
+  KLAUNCH("k_dog_sweep", s, (si->fn<<<dim3(tiles_d, nsub), si->threads, si->smem, s>>>(map_n, T, d_subs, dog, d_status,
+                                                                                        WorkQueue{})));
+}
+
 bool launch_dog_sweep(const Sub *d_subs, int nsub, int W, int H, int D, const DogTaps &T, const float *norm,
                       float *dog, int *d_status, int max_smem, cudaStream_t s) {
   const SweepInst *si = find_inst(T);
@@ -928,16 +1015,13 @@ bool launch_dog_sweep(const Sub *d_subs, int nsub, int W, int H, int D, const Do
   if ((reinterpret_cast<uintptr_t>(norm) & 15) != 0) return false;
   CUtensorMap map_n;
   if (encode_map(&map_n, norm, W, H, D, nsub, si->bw, si->bh) != CUDA_SUCCESS) return false;
-  const unsigned tiles_d = ceil_div(W, kDTX) * ceil_div(H, kDTY);
-  cudaFuncSetAttribute(si->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)si->smem);
-  KLAUNCH("k_dog_sweep", s, (si->fn<<<dim3(tiles_d, nsub), si->threads, si->smem, s>>>(map_n, T, d_subs, dog,
-                                                                                        d_status)));
+  dog_sweep_launch(si, map_n, T, d_subs, nsub, W, H, dog, d_status, LaunchShape{}, nullptr, s);
   return true;
 }
 
 int launch_dog_hess(const Sub *d_subs, int nsub, int W, int H, int D, const DogTaps &T, const float *norm,
                     float *dog, uint8_t *mask, FgEntry *fg, int32_t *fg_idx, unsigned long long *fg_count,
-                    int *d_status, cudaStream_t s) {
+                    int *d_status, const LaunchShape &ls, unsigned *qctr, cudaStream_t s) {
   const int rxy = max(T.r[0], T.r[2]), rz = max(T.r[1], T.r[3]);
   zero_async(fg_count, (size_t)nsub * kFgCountStride * sizeof(unsigned long long), s);
   const SweepInst *si = find_inst(T);
@@ -945,14 +1029,20 @@ int launch_dog_hess(const Sub *d_subs, int nsub, int W, int H, int D, const DogT
     CUtensorMap map_n, map_d;
     if (encode_map(&map_n, norm, W, H, D, nsub, si->bw, si->bh) != CUDA_SUCCESS) return -1;
     if (encode_map(&map_d, dog, W, H, D, nsub, kHPX, kHPY) != CUDA_SUCCESS) return -1;
-    const unsigned tiles_d = ceil_div(W, kDTX) * ceil_div(H, kDTY);
-    cudaFuncSetAttribute(si->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)si->smem);
-    KLAUNCH("k_dog_sweep", s, (si->fn<<<dim3(tiles_d, nsub), si->threads, si->smem, s>>>(map_n, T, d_subs, dog,
-                                                                                          d_status)));
+    dog_sweep_launch(si, map_n, T, d_subs, nsub, W, H, dog, d_status, ls, qctr, s);
     const unsigned tiles_h = ceil_div(W, kHTX) * ceil_div(H, kHTY);
-    cudaFuncSetAttribute(k_hess_sweep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kHessSmem);
-    KLAUNCH("k_hess_sweep", s, (k_hess_sweep<<<dim3(tiles_h, nsub), kHThreads, kHessSmem, s>>>(
-                                   map_d, d_subs, norm, mask, fg, fg_idx, fg_count, d_status)));
+    if (ls.hess_per_sm > 0 && qctr) {
+      zero_async(qctr + 1, sizeof(unsigned), s);
+      const WorkQueue q{qctr + 1, (int)(tiles_h * (unsigned)nsub), (int)tiles_h};
+      const unsigned grid = std::min<unsigned>((unsigned)(ls.hess_per_sm * ls.num_sms), tiles_h * (unsigned)nsub);
+      cudaFuncSetAttribute(k_hess_sweep<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kHessSmem);
+      KLAUNCH("k_hess_sweep", s, (k_hess_sweep<true><<<grid, kHThreads, kHessSmem, s>>>(
+                                     map_d, d_subs, norm, mask, fg, fg_idx, fg_count, d_status, q)));
+    } else {
+      cudaFuncSetAttribute(k_hess_sweep<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kHessSmem);
+      KLAUNCH("k_hess_sweep", s, (k_hess_sweep<false><<<dim3(tiles_h, nsub), kHThreads, kHessSmem, s>>>(
+                                     map_d, d_subs, norm, mask, fg, fg_idx, fg_count, d_status, WorkQueue{})));
+    }
     return 0;
   }
   CUtensorMap map;

@@ -101,6 +101,10 @@ class hdog_stack_in(ctypes.Structure):
     _fields_ = [("data", ctypes.c_void_p), ("on_device", ctypes.c_int), ("length", ctypes.c_int)]
 
 
+class hdog_graph_stack(ctypes.Structure):
+    _fields_ = [("data", ctypes.c_void_p), ("width", ctypes.c_int), ("height", ctypes.c_int), ("length", ctypes.c_int)]
+
+
 class hdog_soft_params(ctypes.Structure):
     _fields_ = [("width", ctypes.c_int), ("height", ctypes.c_int), ("depth", ctypes.c_int),
                 ("radius_norm_xy", ctypes.c_int), ("radius_norm_z", ctypes.c_int),
@@ -132,6 +136,13 @@ _SIGNATURES = {
     "hdog_run_stacks": (ctypes.c_int, [_P, ctypes.POINTER(hdog_stack_in), ctypes.c_int, _P, ctypes.c_int64,
                                        ctypes.POINTER(ctypes.c_int64), _P, _P]),
     "hdog_run_param_file": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int]),
+    "hdog_graph_create": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.c_int, ctypes.POINTER(hdog_graph_stack), ctypes.c_int,
+                                         _P, ctypes.POINTER(_P)]),
+    "hdog_graph_run": (ctypes.c_int, [_P, _P, ctypes.c_int64, ctypes.POINTER(ctypes.c_int64), _P, _P]),
+    "hdog_graph_last_records": (ctypes.c_int, [_P, _P, ctypes.c_int64, ctypes.POINTER(ctypes.c_int64)]),
+    "hdog_graph_destroy": (ctypes.c_int, [_P]),
+    "hdog_autotune": (ctypes.c_int, [_P, _P, ctypes.c_int, _P]),
+    "hdog_ctx_tuning": (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_size_t]),
     "hdog_ctx_set_option": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int]),
     "hdog_ccl_noalloc": (ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P]),
     "hdog_ccl_edge_count": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]),
@@ -451,6 +462,19 @@ class Context:
                                    ctypes.c_void_p(counts.ctypes.data), _stream(stream))
         return self._finish(rc, out, n), counts[:len(stacks)]
 
+    def autotune(self, stack, stream=None):
+        """Picks the sweeps' launch shapes and the substacks per launch of the graph form by
+        timing this context's first batch of `stack` (a CUDA tensor (length, H, W))."""
+        assert stack.is_cuda and stack.is_contiguous()
+        check(lib().hdog_autotune(self._h, _ptr(stack), int(stack.shape[0]), _stream(stream)))
+        return self.tuning()
+
+    def tuning(self):
+        """The autotuner's choice and timings for this context ({} before it ran)."""
+        buf = ctypes.create_string_buffer(4096)
+        check(lib().hdog_ctx_tuning(self._h, buf, len(buf)))
+        return json.loads(buf.value.decode())
+
     def _finish(self, rc, out, n):
         """Records of a whole-chain call.  Without a capacity the call only counts them, and
         one copy from the context's host copy of the result fills an array of exactly that
@@ -461,6 +485,51 @@ class Context:
             rc = lib().hdog_last_records(self._h, _out_ptr(out), len(out), ctypes.byref(n))
         check(rc)
         return out[: n.value]
+
+
+class Graph:
+    """The batched graph form: stacks of uneven depth and frame shape (CUDA tensors
+    (length, H, W)) through one captured CUDA graph, one context per frame shape.
+    run() -> (records stack by stack in the given order, per-stack counts)."""
+
+    def __init__(self, contexts, stacks, stream=None):
+        self._stacks = list(stacks)          # the graph keeps their device addresses
+        self.contexts = list(contexts)
+        ctxs = (ctypes.c_void_p * len(self.contexts))(*[c._h.value for c in self.contexts])
+        descs = (hdog_graph_stack * max(1, len(self._stacks)))()
+        for i, a in enumerate(self._stacks):
+            assert a.is_cuda and a.is_contiguous() and a.dim() == 3
+            descs[i].data = a.data_ptr()
+            descs[i].length, descs[i].height, descs[i].width = (int(x) for x in a.shape)
+        h = ctypes.c_void_p()
+        check(lib().hdog_graph_create(ctxs, len(self.contexts), descs, len(self._stacks), _stream(stream),
+                                      ctypes.byref(h)))
+        self._h = h
+
+    def run(self, cap=None, stream=None, out=None):
+        out = _out_array(out, cap)
+        counts = np.zeros(max(1, len(self._stacks)), np.int64)
+        n = ctypes.c_int64()
+        rc = lib().hdog_graph_run(self._h, _out_ptr(out), len(out), ctypes.byref(n),
+                                  ctypes.c_void_p(counts.ctypes.data), _stream(stream))
+        if rc == HDOG_ERR_CAPACITY:
+            out = np.empty(int(n.value), DT_LOCAL)
+            rc = lib().hdog_graph_last_records(self._h, _out_ptr(out), len(out), ctypes.byref(n))
+        check(rc)
+        return out[: n.value], counts[:len(self._stacks)]
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().hdog_graph_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
 
 
 def _out_ptr(a):

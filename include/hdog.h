@@ -173,6 +173,46 @@ int hdog_last_records(hdog_ctx *ctx, hdog_record *out, int64_t cap, int64_t *n_r
    writes each dst_path (removed first, then appended per substack). */
 int hdog_run_param_file(const char *param_path, int verbose);
 
+/* ---- the batched graph form ----
+   Many stacks of uneven depth and frame shape in one captured CUDA graph.  No counterpart
+   in the reference, whose HDoG3D_main runs its substacks one at a time
+   (src/3D/HDoG3D_main.cpp:294-315); the records are the ones hdog_run_stack gives each stack.
+   The caller gives one context per frame shape (width x height; at most 16 substacks each)
+   and the stacks in device memory.  hdog_graph_create schedules every stack's substacks
+   (HDoG3D_main's schedule), picks each frame shape's launch shapes with the autotuner on its
+   first batch, packs each shape's substacks into batches of its context, and captures all
+   batches of all shapes into one CUDA graph: the two sweeps run as persistent kernels over a
+   device work queue of (substack, tile) items when the autotuner chose that, the records
+   of every batch are placed in one device array of the run, and nothing returns to the host
+   between batches.  hdog_graph_run launches the graph and returns the records stack by stack
+   in the caller's order (stack_counts[i], may be NULL, receives stack i's count); when a
+   batch needs the host's fallback (a full foreground list or region table, or more records
+   than the run's array holds) it reruns the stacks one by one without the graph, with the
+   same results.  The graph keeps the stacks' device addresses and the contexts' scratch: the
+   stacks must stay in place, and the contexts are locked while the graph runs. */
+typedef struct hdog_graph_stack {
+  const uint16_t *data;   /* device memory: length slices of width * height uint16 */
+  int width, height, length;
+} hdog_graph_stack;
+typedef struct hdog_graph hdog_graph;
+int hdog_graph_create(hdog_ctx *const *ctxs, int n_ctx, const hdog_graph_stack *stacks, int n_stacks, void *stream,
+                      hdog_graph **out);
+int hdog_graph_run(hdog_graph *g, hdog_record *out, int64_t cap, int64_t *n_records, int64_t *stack_counts,
+                   void *stream);
+/* The records of the graph's last run (also after HDOG_ERR_CAPACITY). */
+int hdog_graph_last_records(hdog_graph *g, hdog_record *out, int64_t cap, int64_t *n_records);
+int hdog_graph_destroy(hdog_graph *g);
+
+/* ---- autotuner ----
+   Times the context's first batch of a device stack with each candidate launch shape of the
+   two sweeps (one block per tile, or persistent grids of 3 / 2 DoG and 5 / 4 Hessian blocks
+   per SM over the device work queue) and the full batch against half of it, keeps the
+   fastest for the context (and for later contexts of the same frame shape, depth, radii and
+   size in this process), and writes the timings as JSON for hdog_ctx_tuning.  No counterpart
+   in the reference.  Every choice gives the same records. */
+int hdog_autotune(hdog_ctx *ctx, const uint16_t *d_stack, int length, void *stream);
+int hdog_ctx_tuning(hdog_ctx *ctx, char *buf, size_t cap);
+
 /* ---- labelling without any device allocation ----
    No counterpart in the reference.  For callers that may not allocate device memory
    themselves (a host framework that owns all device memory through its own allocator,
