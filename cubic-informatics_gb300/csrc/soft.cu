@@ -174,6 +174,11 @@ __global__ void k_soft_dot(const float *a, const float *b, int64_t N, double *ou
 __device__ __forceinline__ int h_inner(int e) { return e < 3 ? 0 : (e < 5 ? 1 : 2); }   // xx xy xz | yy yz | zz
 __device__ __forceinline__ int h_outer(int e) { return e == 0 ? 0 : (e == 1 || e == 3 ? 1 : 2); }
 
+// Offsets of the three relaxed minor tests (kernel parameter).
+struct SoftThresh {
+  float v[3];
+};
+
 struct SoftPoint {
   int x, y, z;
 };
@@ -224,52 +229,62 @@ __device__ void soft_hessian_adj(float *gf, const SoftGeom &g, SoftPoint p, cons
 
 __device__ __forceinline__ float sigm(float v) { return 1.0f / (1.0f + expf(-v)); }
 
-// Score of Hessian h and, when ds is given, its derivative in h.
-__device__ float soft_score(const float h[6], float tau, float *ds) {
+// Score of Hessian h: sigmoid((b0 - xx) / tau) sigmoid((m2 - b1) / tau^2) sigmoid((b2 - det) /
+// tau^3) with thresholds b (all zero: the reference's test xx < 0, m2 > 0, det < 0).  When
+// ds is given, its derivative in h; when db is given, its derivative in b.
+__device__ float soft_score(const float h[6], float tau, const float b[3], float *ds, float *db) {
   const float xx = h[0], xy = h[1], xz = h[2], yy = h[3], yz = h[4], zz = h[5];
   const float t2 = tau * tau, t3 = t2 * tau;
   const float m2 = xx * yy - xy * xy;
   const float det = xx * yy * zz + 2.0f * xy * yz * xz - xx * yz * yz - yy * xz * xz - zz * xy * xy;
-  const float A = sigm(-xx / tau), B = sigm(m2 / t2), C = sigm(-det / t3);
+  const float A = sigm((b[0] - xx) / tau), B = sigm((m2 - b[1]) / t2), C = sigm((b[2] - det) / t3);
   const float s = A * B * C;
+  const float ca = -(1.0f - A) / tau, cb = (1.0f - B) / t2, cc = -(1.0f - C) / t3;
   if (ds) {
-    const float ca = -(1.0f - A) / tau, cb = (1.0f - B) / t2, cc = -(1.0f - C) / t3;
     // d det / d (xx, xy, xz, yy, yz, zz)
     const float dd[6] = {yy * zz - yz * yz, 2.0f * yz * xz - 2.0f * zz * xy, 2.0f * xy * yz - 2.0f * yy * xz,
                          xx * zz - xz * xz, 2.0f * xy * xz - 2.0f * xx * yz, xx * yy - xy * xy};
     const float dm2[6] = {yy, -2.0f * xy, 0.0f, xx, 0.0f, 0.0f};
     for (int k = 0; k < 6; k++) ds[k] = s * ((k == 0 ? ca : 0.0f) + cb * dm2[k] + cc * dd[k]);
   }
+  if (db) {
+    db[0] = -s * ca;
+    db[1] = -s * cb;
+    db[2] = -s * cc;
+  }
   return s;
 }
 
 // Forward at the points: scores (optional) and the loss (double, out must start at zero).
 __global__ void k_soft_points(const float *dog, SoftGeom g, const int32_t *pos, int n_pos, const int32_t *neg,
-                              int n_neg, float tau, float *scores, double *loss) {
+                              int n_neg, float tau, SoftThresh b, float *scores, double *loss) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n_pos + n_neg) return;
   const int32_t *q = i < n_pos ? pos + 3 * i : neg + 3 * (i - n_pos);
   const SoftPoint p{q[2], q[1], q[0]};
   float h[6];
   soft_hessian(dog, g, p, h);
-  const float s = soft_score(h, tau, nullptr);
+  const float s = soft_score(h, tau, b.v, nullptr, nullptr);
   if (scores) scores[i] = s;
   atomicAdd(loss, i < n_pos ? (double)s / n_pos : -(double)s / n_neg);
 }
 
-// Backward at the points: d loss / d dog scattered into gdog (which must start at zero).
+// Backward at the points: d loss / d dog scattered into gdog (which must start at zero), and
+// d loss / d thresholds summed into gb[0..2] (double, zeroed first) when gb is given.
 __global__ void k_soft_points_adj(const float *dog, SoftGeom g, const int32_t *pos, int n_pos, const int32_t *neg,
-                                  int n_neg, float tau, float grad_loss, float *gdog) {
+                                  int n_neg, float tau, SoftThresh b, float grad_loss, float *gdog, double *gb) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n_pos + n_neg) return;
   const int32_t *q = i < n_pos ? pos + 3 * i : neg + 3 * (i - n_pos);
   const SoftPoint p{q[2], q[1], q[0]};
-  float h[6], ds[6];
+  float h[6], ds[6], db[3];
   soft_hessian(dog, g, p, h);
-  soft_score(h, tau, ds);
+  soft_score(h, tau, b.v, ds, db);
   const float w = i < n_pos ? grad_loss / (float)n_pos : -grad_loss / (float)n_neg;
   for (int k = 0; k < 6; k++) ds[k] *= w;
   soft_hessian_adj(gdog, g, p, ds);
+  if (gb)
+    for (int k = 0; k < 3; k++) atomicAdd(gb + k, (double)db[k] * (double)w);
 }
 
 __global__ void k_soft_to_float(const double *in, float *out, int n) {
@@ -286,7 +301,7 @@ struct SoftRun {
   int64_t N;
   cudaStream_t st;
   float *w;      // workspace slots of N floats (after the accumulators)
-  double *acc;   // 8 doubles at the start of the workspace
+  double *acc;   // 16 doubles at the start of the workspace
   unsigned blocks() const { return ceil_div(N, 256); }
   float *slot(int k) const { return w + (int64_t)k * N; }
 };
@@ -361,6 +376,12 @@ void forward_chain(const SoftRun &R, const float *vol) {
                                                                         nrm, R.N)));
 }
 
+SoftThresh thresh_of(const hdog_soft_params &p) {
+  SoftThresh b;
+  for (int k = 0; k < 3; k++) b.v[k] = p.thresh[k];
+  return b;
+}
+
 int check_params(const hdog_soft_params *p, const float *vol, const int32_t *pos, int n_pos, const int32_t *neg,
                  int n_neg, void *work) {
   if (!p || !vol || !work || n_pos < 0 || n_neg < 0 || (n_pos && !pos) || (n_neg && !neg))
@@ -376,7 +397,7 @@ int check_params(const hdog_soft_params *p, const float *vol, const int32_t *pos
 }  // namespace
 
 size_t soft_workspace_bytes(const hdog_soft_params &p) {
-  return 8 * sizeof(double) + (size_t)kSoftSlots * p.width * p.height * p.depth * sizeof(float);
+  return 16 * sizeof(double) + (size_t)kSoftSlots * p.width * p.height * p.depth * sizeof(float);
 }
 
 int soft_forward(const hdog_soft_params *p, const float *vol, const int32_t *pos, int n_pos, const int32_t *neg,
@@ -386,31 +407,37 @@ int soft_forward(const hdog_soft_params *p, const float *vol, const int32_t *pos
   SoftRun R{*p, SoftGeom{p->width, p->height, p->depth}, (int64_t)p->width * p->height * p->depth, st,
             static_cast<float *>(work), nullptr};
   R.acc = static_cast<double *>(work);
-  R.w = reinterpret_cast<float *>(R.acc + 8);
+  R.w = reinterpret_cast<float *>(R.acc + 16);
   forward_chain(R, vol);
   cudaMemsetAsync(R.acc, 0, sizeof(double), st);
   if (n_pos + n_neg > 0)
     KLAUNCH("k_soft_points", st, (k_soft_points<<<ceil_div(n_pos + n_neg, 128), 128, 0, st>>>(
-                                     R.slot(S_DOG), R.g, pos, n_pos, neg, n_neg, p->tau, scores, R.acc)));
+                                     R.slot(S_DOG), R.g, pos, n_pos, neg, n_neg, p->tau, thresh_of(*p), scores,
+                                     R.acc)));
   k_soft_to_float<<<1, 32, 0, st>>>(R.acc, loss, 1);
   return HDOG_OK;
 }
 
 int soft_backward(const hdog_soft_params *p, const float *vol, const int32_t *pos, int n_pos, const int32_t *neg,
-                  int n_neg, float grad_loss, float *grad_vol, float *grad_sigma, void *work, cudaStream_t st) {
+                  int n_neg, float grad_loss, float *grad_vol, float *grad_sigma, float *grad_thresh, void *work,
+                  cudaStream_t st) {
   const int rc = check_params(p, vol, pos, n_pos, neg, n_neg, work);
   if (rc != HDOG_OK) return rc;
   SoftRun R{*p, SoftGeom{p->width, p->height, p->depth}, (int64_t)p->width * p->height * p->depth, st,
             static_cast<float *>(work), nullptr};
   R.acc = static_cast<double *>(work);
-  R.w = reinterpret_cast<float *>(R.acc + 8);
+  R.w = reinterpret_cast<float *>(R.acc + 16);
   const unsigned nb = R.blocks();
   forward_chain(R, vol);
   float *gdog = R.slot(S_GDOG);
   cudaMemsetAsync(gdog, 0, R.N * sizeof(float), st);
+  double *gb = R.acc + 8;   // threshold gradients
+  cudaMemsetAsync(gb, 0, 3 * sizeof(double), st);
   if (n_pos + n_neg > 0)
     KLAUNCH("k_soft_points_adj", st, (k_soft_points_adj<<<ceil_div(n_pos + n_neg, 128), 128, 0, st>>>(
-                                         R.slot(S_DOG), R.g, pos, n_pos, neg, n_neg, p->tau, grad_loss, gdog)));
+                                         R.slot(S_DOG), R.g, pos, n_pos, neg, n_neg, p->tau, thresh_of(*p), grad_loss,
+                                         gdog, gb)));
+  if (grad_thresh) k_soft_to_float<<<1, 32, 0, st>>>(gb, grad_thresh, 3);
   const float *s = p->sigma;
   const float nrm = (float)pow((double)s[0] * s[1] * s[2], (double)p->gamma);
   if (grad_sigma) {

@@ -109,7 +109,7 @@ class hdog_soft_params(ctypes.Structure):
     _fields_ = [("width", ctypes.c_int), ("height", ctypes.c_int), ("depth", ctypes.c_int),
                 ("radius_norm_xy", ctypes.c_int), ("radius_norm_z", ctypes.c_int),
                 ("min_intensity", ctypes.c_float), ("sigma", ctypes.c_float * 6), ("gamma", ctypes.c_float),
-                ("tau", ctypes.c_float)]
+                ("tau", ctypes.c_float), ("thresh", ctypes.c_float * 3)]
 
 
 _SIGNATURES = {
@@ -155,7 +155,7 @@ _SIGNATURES = {
     "hdog_soft_forward": (ctypes.c_int, [ctypes.POINTER(hdog_soft_params), _P, _P, ctypes.c_int, _P, ctypes.c_int,
                                          _P, _P, _P, _P]),
     "hdog_soft_backward": (ctypes.c_int, [ctypes.POINTER(hdog_soft_params), _P, _P, ctypes.c_int, _P, ctypes.c_int,
-                                          ctypes.c_float, _P, _P, _P, _P]),
+                                          ctypes.c_float, _P, _P, _P, _P, _P]),
     "hdog_memcpy": (ctypes.c_int, [_P, _P, ctypes.c_size_t, _P]),
     "hdog_stream_sync": (ctypes.c_int, [_P]),
     "hdog_device_alloc": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.c_size_t]),

@@ -43,7 +43,7 @@
 extern "C" {
 #endif
 
-#define HDOG_ABI_VERSION 4
+#define HDOG_ABI_VERSION 5
 
 enum {
   HDOG_OK = 0,
@@ -303,12 +303,13 @@ int hdog_classifier_features(const hdog_record *d_records, int64_t n, const hdog
    (NormalizeFilter.cu:537-654, DoG3DFilter.cu:70-437, Hessian3DFilter_element.cu:22-388)
    without its bit-exact summation orders; each axis and scale has its own sigma; the mask
    test xx < 0, xx yy - xy^2 > 0, det < 0 (Hessian3DFilter_element.cu:317-321) becomes
-   sigmoid(-xx / tau) * sigmoid((xx yy - xy^2) / tau^2) * sigmoid(-det / tau^3).  Loss = mean
-   score at the positive points - mean score at the negative points.  Points are int32
-   (z, y, x) triples.  Backward recomputes the forward from the input (the workspace holds
-   nothing between calls) and returns d loss / d volume and d loss / d sigma (either may be
-   NULL); tap radii (int)(2 sigma + 0.5) are held fixed for the derivatives.  Sigmas up to
-   15.7 (radius 31).  The workspace is device memory of hdog_soft_workspace_bytes bytes. */
+   sigmoid((b0 - xx) / tau) * sigmoid((xx yy - xy^2 - b1) / tau^2) * sigmoid((b2 - det) / tau^3)
+   with thresholds b (zero: the reference's test).  Loss = mean score at the positive points -
+   mean score at the negative points.  Points are int32 (z, y, x) triples.  Backward
+   recomputes the forward from the input (the workspace holds nothing between calls) and
+   returns d loss / d volume, d loss / d sigma and d loss / d thresholds (any may be NULL);
+   tap radii (int)(2 sigma + 0.5) are held fixed for the derivatives.  Sigmas up to 15.7
+   (radius 31).  The workspace is device memory of hdog_soft_workspace_bytes bytes. */
 typedef struct hdog_soft_params {
   int width, height, depth;
   int radius_norm_xy, radius_norm_z;
@@ -316,6 +317,7 @@ typedef struct hdog_soft_params {
   float sigma[6];                        /* x1, y1, z1 (small scale), x2, y2, z2 (large scale) */
   float gamma;                           /* normalizer (sx1 sy1 sz1)^gamma */
   float tau;                             /* scale of the relaxed minor tests (> 0) */
+  float thresh[3];                       /* b0, b1, b2: offsets of the three minor tests */
 } hdog_soft_params;
 size_t hdog_soft_workspace_bytes(const hdog_soft_params *p);
 int hdog_soft_forward(const hdog_soft_params *p, const float *d_volume, const int32_t *d_pos, int n_pos,
@@ -323,7 +325,7 @@ int hdog_soft_forward(const hdog_soft_params *p, const float *d_volume, const in
                       void *stream);
 int hdog_soft_backward(const hdog_soft_params *p, const float *d_volume, const int32_t *d_pos, int n_pos,
                        const int32_t *d_neg, int n_neg, float grad_loss, float *d_grad_volume,
-                       float *d_grad_sigma, void *d_workspace, void *stream);
+                       float *d_grad_sigma, float *d_grad_thresh, void *d_workspace, void *stream);
 
 /* ---- context options ---- */
 enum {

@@ -31,8 +31,9 @@ def build_oracle():
     os.makedirs(BUILD, exist_ok=True)
     stamp = os.path.join(BUILD, "ARCH")
     if not os.path.exists(stamp) or open(stamp).read().strip() != platform.machine():
-        if os.path.exists(LIB):
-            os.remove(LIB)
+        for f in (LIB, os.path.join(BUILD, "libref_features.so")):
+            if os.path.exists(f):
+                os.remove(f)
         with open(stamp, "w") as fh:
             fh.write(platform.machine() + "\n")
     src = os.path.join(HERE, "hdog_oracle.c")
@@ -43,6 +44,23 @@ def build_oracle():
             flags.append("-mfma")   # hardware fmaf; results are IEEE fma either way
         subprocess.run(["gcc"] + flags + ["-o", LIB, src, "-lm"], check=True)
     return LIB
+
+
+def build_ref_features():
+    """oracle/_build/libref_features.so: the reference's region reductions restated with CUB
+    (ref_features.cu), for oracle/ref_records.py on a GPU host."""
+    os.makedirs(BUILD, exist_ok=True)
+    out = os.path.join(BUILD, "libref_features.so")
+    src = os.path.join(HERE, "ref_features.cu")
+    if _stale(out, [src]) or not _same_arch():
+        subprocess.run(["nvcc", "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17", "-Xcompiler",
+                        "-fPIC", "-shared", "-o", out, src], check=True)
+    return out
+
+
+def _same_arch():
+    stamp = os.path.join(BUILD, "ARCH")
+    return os.path.exists(stamp) and open(stamp).read().strip() == platform.machine()
 
 
 def build_reference_cubins():
@@ -69,4 +87,5 @@ def build_reference_cubins():
 
 if __name__ == "__main__":
     print(build_oracle())
+    print(build_ref_features())
     print(build_reference_cubins())

@@ -16,8 +16,9 @@ differentiable relaxation of its mask):
               values outside the volume 0 and first derivatives at positions outside the
               volume 0; element order xx, xy, xz, yy, yz, zz
   soft score  the leading-principal-minor test xx < 0, xx yy - xy^2 > 0, det < 0
-              (PositiveDefiniteKernel, Hessian3DFilter_element.cu:317-321) relaxed to
-              sigmoid(-xx / tau) * sigmoid((xx yy - xy^2) / tau^2) * sigmoid(-det / tau^3)
+              (PositiveDefiniteKernel, Hessian3DFilter_element.cu:317-321) with thresholds
+              b relaxed to sigmoid((b0 - xx) / tau) * sigmoid((xx yy - xy^2 - b1) / tau^2) *
+              sigmoid((b2 - det) / tau^3)
   loss        mean score at the positive points minus mean score at the negative points
 The tap radius is a step function of sigma and is held fixed for derivatives.
 """
@@ -96,18 +97,21 @@ def hessian(f):
     return [grad1(gx, 2), grad1(gx, 1), grad1(gx, 0), grad1(gy, 1), grad1(gy, 0), grad1(gz, 0)]
 
 
-def soft_score(h, tau):
+def soft_score(h, tau, b=(0.0, 0.0, 0.0)):
+    """The three tests with thresholds b: xx < b0, xx yy - xy^2 > b1, det < b2 (b = 0: the
+    reference's), each a sigmoid of its margin over tau, tau^2, tau^3."""
     xx, xy, xz, yy, yz, zz = h
     m2 = xx * yy - xy * xy
     det = xx * yy * zz + 2 * xy * yz * xz - xx * yz * yz - yy * xz * xz - zz * xy * xy
-    return torch.sigmoid(-xx / tau) * torch.sigmoid(m2 / tau ** 2) * torch.sigmoid(-det / tau ** 3)
+    return torch.sigmoid((b[0] - xx) / tau) * torch.sigmoid((m2 - b[1]) / tau ** 2) * \
+        torch.sigmoid((b[2] - det) / tau ** 3)
 
 
-def loss(I, sigma, pos, neg, rxy, rz, min_intensity, tau, gamma=1.0):
+def loss(I, sigma, pos, neg, rxy, rz, min_intensity, tau, gamma=1.0, b=(0.0, 0.0, 0.0)):
     """I: (D, H, W) float64; sigma: 6 float64 scalars (x1, y1, z1, x2, y2, z2); pos / neg:
-    (n, 3) integer (z, y, x) voxel indices."""
+    (n, 3) integer (z, y, x) voxel indices; b: the 3 test thresholds (float64 scalars)."""
     h = hessian(dog(normalize(I, rxy, rz, min_intensity), sigma, gamma))
 
     def at(p):
         return [e[p[:, 0], p[:, 1], p[:, 2]] for e in h]
-    return soft_score(at(pos), tau).mean() - soft_score(at(neg), tau).mean()
+    return soft_score(at(pos), tau, b).mean() - soft_score(at(neg), tau, b).mean()

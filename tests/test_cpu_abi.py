@@ -32,8 +32,8 @@ def test_library_exports_every_declared_symbol():
 def test_struct_layouts():
     assert hdog.DT_LOCAL.itemsize == 28          # FeatureVector, src/3D/utils.h:188-197
     assert ctypes.sizeof(hdog.hdog_params) == 21 * 4
-    assert hdog.lib().hdog_abi_version() == 4
-    assert ctypes.sizeof(hdog.hdog_soft_params) == 5 * 4 + 4 + 6 * 4 + 2 * 4
+    assert hdog.lib().hdog_abi_version() == 5
+    assert ctypes.sizeof(hdog.hdog_soft_params) == 5 * 4 + 4 + 6 * 4 + 2 * 4 + 3 * 4
     # the record post-processing types: packed NumPy records, plain parameter blocks
     assert hdog.DT_GLOBAL.itemsize == 15 and hdog.DT_SCALEMERGED.itemsize == 13
     assert ctypes.sizeof(hdog.hdog_global_params) == 6 * 8 + 6 * 4

@@ -71,3 +71,31 @@ def test_oracle_sylvester_form_matches_reference_on_near_singular_matrices():
     counts = g["mismatches_by_variant"]
     assert counts[str(orc.PD_VARIANT_REFERENCE)] == 0
     assert sorted(counts.values())[1] > 0
+
+
+REF_RECORDS = os.path.join(os.path.dirname(__file__), "golden", "ref_records_camera.json")
+EXACT = ("local_x", "local_y", "local_z", "intensity", "size", "padding")
+
+
+@pytest.mark.skipif(not os.path.exists(REF_RECORDS), reason="reference-path record digests not recorded")
+def test_oracle_reproduces_the_reference_path_on_a_full_camera_substack():
+    """Substack 0 of the 2560 x 2160 x 128 camera stack (depth 32): the oracle's stage
+    outputs and records against digests of the reference's own path
+    (tests/golden/make_ref_records_golden.py: its kernels, its CUB reductions, its record
+    filter, on a GB300)."""
+    from types import SimpleNamespace
+    g = json.load(open(REF_RECORDS))["camera"]
+    p = SimpleNamespace(**g["params"])
+    vol = synth.volume(synth.camera_spec(depth=128))
+    sub = np.ascontiguousarray(vol[:p.depth])
+    del vol
+    norm = orc.normalize(sub, p.radius_norm_xy, p.radius_norm_z, float(p.min_intensity))
+    assert sha(norm) == g["substack0_stage_sha256"]["norm"]
+    dog = orc.dog(norm, p.sigma_xy_small, p.sigma_z_small, p.sigma_xy_large, p.sigma_z_large, p.gamma_n)
+    assert sha(dog) == g["substack0_stage_sha256"]["dog"]
+    del norm, dog
+    rec, _, mask, labels = orc.substack(orc.params_from(p), sub, p.depth, 0)
+    assert sha(mask) == g["substack0_stage_sha256"]["pd"]
+    assert sha(labels) == g["substack0_stage_sha256"]["labels"]
+    assert len(rec) == g["substack0_records"]
+    assert sha(np.ascontiguousarray(rec[list(EXACT)])) == g["substack0_exact_fields_sha256"]
