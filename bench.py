@@ -564,8 +564,10 @@ def main():
     clocks = ClockSampler(local)
     with clocks:
         ms, recs = time_steps(batched, stack_dev, args.steps, args.warmup, stream, dist)
-    ktimes = batched.timing_read()
+    kt_all = batched.timing_read()
     batched.timing(False)
+    ktimes = {k: v for k, v in kt_all.items() if not k.startswith("host_")}
+    host_phases = {k: round(v[1] / args.steps, 3) for k, v in kt_all.items() if k.startswith("host_")}
     ms = max_over_ranks(ms, dist)
     ms_step = ms / args.steps
     value = unique * ws / (ms_step * 1e-3) / 1e9
@@ -585,6 +587,14 @@ def main():
     e2e_ms = (time.perf_counter() - t0) * 1e3
     e2e_ms = max_over_ranks(e2e_ms, dist) / args.steps
     assert recs_e2e.tobytes() == recs.tobytes(), "host-input run differs from device-input run"
+    # where an end-to-end call spends its time (one more call, outside the timed loop, with
+    # kernel and host-phase timing on)
+    batched.timing(True)
+    batched.timing_read()
+    batched.run_stack(host_np, out=e2e_out)
+    e2e_phases = {k: round(v[1], 3) for k, v in batched.timing_read().items()}
+    batched.timing(False)
+    e2e_kernel_ms = round(sum(v for k, v in e2e_phases.items() if not k.startswith("host_")), 3)
     # the pinned host -> device copy rate of this machine, for reading the end-to-end figure
     h2d_ms = []
     for _ in range(3):
@@ -635,9 +645,12 @@ def main():
         "batched_over_plain": value / plain_value,
         "e2e": {"value": unique * ws / (e2e_ms * 1e-3) / 1e9, "unit": "Gvox/s",
                 "h2d_bytes_per_step": unique * 2, "d2h_bytes_per_step": n_records * 28,
-                "ms_per_step": e2e_ms, "pinned_h2d_gbs": round(h2d_gbs, 1)},
+                "ms_per_step": e2e_ms, "pinned_h2d_gbs": round(h2d_gbs, 1),
+                "one_call": {"kernel_ms": e2e_kernel_ms,
+                             "host_ms": {k: v for k, v in e2e_phases.items() if k.startswith("host_")}}},
         "gpu_launches": int(launches),
         "kernel_ms_per_step": {k: round(v[1] / args.steps, 4) for k, v in sorted(ktimes.items(), key=lambda kv: -kv[1][1])},
+        "host_ms_per_step": host_phases,
         # algorithmic GB/s of each dense kernel (its per-voxel bytes over its event time)
         "kernel_alg_gbs": {k: round(KERNEL_BYTES_PER_VOXEL[k] * processed * v[0] / (v[1] * 1e-3) / 1e9, 1)
                            for k, v in ktimes.items() if k in KERNEL_BYTES_PER_VOXEL and v[1] > 0},

@@ -5,6 +5,7 @@
 // processSubstack :134-257, main :260-319) and src/3D/utils.h (loadParamFile :95-157,
 // loadImage :160-173, saveFeatureVector :204-250).
 #include <algorithm>
+#include <chrono>
 #include <cerrno>
 #include <cmath>
 #include <cstdio>
@@ -56,6 +57,18 @@ struct EventTimer : KernelTimer {
   }
   void end(cudaStream_t s) override {
     if (!pending.empty()) cudaEventRecord(pending.back().b, s);
+  }
+  // Host-side wall time of a phase of a call (names starting with "host_"), in milliseconds.
+  void add_host(const char *name, double ms) {
+    for (auto &t : totals)
+      if (t.first == name) {
+        t.second.count++;
+        t.second.ms += ms;
+        return;
+      }
+    totals.emplace_back(name, Acc());
+    totals.back().second.count = 1;
+    totals.back().second.ms = ms;
   }
   void collect() {
     for (Rec &r : pending) {
@@ -253,6 +266,18 @@ struct hdog_ctx {
 struct TimerScope {
   explicit TimerScope(hdog_ctx *c) { g_timer = c->timer; }
   ~TimerScope() { g_timer = nullptr; }
+};
+
+// Wall time of a host phase of a call, added to the context's timing report when timing is on.
+struct HostPhase {
+  hdog_ctx *c;
+  const char *name;
+  std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+  HostPhase(hdog_ctx *c_, const char *n) : c(c_), name(n) {}
+  ~HostPhase() {
+    if (c->timer)
+      c->timer->add_host(name, std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count());
+  }
 };
 
 static size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
@@ -622,8 +647,14 @@ static int enqueue_batch(hdog_ctx *c, int nsub, bool fused, cudaStream_t st) {
 
 static int run_batch(hdog_ctx *c, int nsub, cudaStream_t st) {
   const bool fused = fused_ok(c);
-  TRY(enqueue_batch(c, nsub, fused, st));
-  TRY(readback(c, nsub, st));
+  {
+    HostPhase ph(c, "host_enqueue_batch");
+    TRY(enqueue_batch(c, nsub, fused, st));
+  }
+  {
+    HostPhase ph(c, "host_wait_batch");
+    TRY(readback(c, nsub, st));
+  }
   if (fused) {
     bool over = false;
     for (int s = 0; s < nsub; s++) over |= c->h_counts[2 * c->max_sub + s] > c->fg_cap;
@@ -639,6 +670,7 @@ static int run_batch(hdog_ctx *c, int nsub, cudaStream_t st) {
 
 // Appends the records of substacks [0, nsub) to out, in substack order.
 static int collect_records(hdog_ctx *c, int nsub, RecordBuf &out, cudaStream_t st) {
+  HostPhase ph(c, "host_collect_records");
   size_t n = out.n, total = n;
   for (int s = 0; s < nsub; s++) total += (size_t)c->h_counts[s];
   if (!out.reserve(total)) return fail(HDOG_ERR_NOMEM, "page-locked host buffer for the records failed");
@@ -923,6 +955,11 @@ static int run_stack_locked(hdog_ctx *c, const uint16_t *stack, int on_device, i
   for (size_t b = 0; b < nbatch; b++) {
     const size_t first = starts[b];
     const int nsub = (int)(starts[b + 1] - first);
+    if (!on_device && c->timer) {
+      // time the GPU would wait for this batch's chunk: sync on it while timing
+      HostPhase ph(c, "host_wait_chunk");
+      HDOG_CUDA_TRY(cudaEventSynchronize(c->chunk_ev[b]));
+    }
     if (!on_device) HDOG_CUDA_TRY(cudaStreamWaitEvent(st, c->chunk_ev[b], 0));
     for (int s = 0; s < nsub; s++) {
       const int z0 = z0s[first + s];
@@ -941,6 +978,7 @@ extern "C" int hdog_run_stack(hdog_ctx *c, const uint16_t *stack, int stack_on_d
   if (!stack || !n_records || length < 0 || (cap > 0 && !out)) return fail(HDOG_ERR_ARG, "hdog_run_stack: bad argument");
   c->last.clear();
   TRY(run_stack_locked(c, stack, stack_on_device, length, c->last, (cudaStream_t)stream));
+  HostPhase ph(c, "host_copy_out");
   return copy_out(c->last, out, cap, n_records);
 }
 

@@ -328,6 +328,13 @@ constexpr int kHPY = kHTY + 4;
 constexpr int kHRing = 8;              // ring slots; a slot is 40 x 20 floats = 25 x 128 bytes
 constexpr int kHThreads = kHTX / 4 * kHTY;   // one x quad per thread
 
+// Input slices of the DoG sweep in flight: slice it + kDogIn - 1 is requested while slice it
+// is filtered.
+#ifndef HDOG_DOG_STAGES
+#define HDOG_DOG_STAGES 3
+#endif
+constexpr int kDogIn = HDOG_DOG_STAGES;
+
 template <int RA, int RB, int ZA, int ZB>
 struct DogT {
   static constexpr int RXY = RA > RB ? RA : RB;
@@ -342,7 +349,7 @@ struct DogT {
   static constexpr int OFF = HX - RXY;                        // item q reads from column 4q + OFF
   static constexpr int NV = (OFF + 2 * RXY + 4 + 3) / 4 * 4;  // inputs staged per item
   static constexpr int NT = kDTX * kDTY / 2;                  // 256: two z columns per thread
-  static constexpr size_t SMEM = (size_t)2 * IN_FLOATS * 4 + (size_t)2 * BH * kDTX * 8 + 64;
+  static constexpr size_t SMEM = (size_t)kDogIn * IN_FLOATS * 4 + (size_t)2 * BH * kDTX * 8 + 8 * kDogIn + 64;
 };
 
 // Coefficient pairs (small, large) of the taps both scales share, |j| <= min(RA, RB),
@@ -466,21 +473,20 @@ __global__ void __launch_bounds__(DogT<RA, RB, ZA, ZB>::NT, 3)
   using C = DogT<RA, RB, ZA, ZB>;
   extern __shared__ __align__(128) unsigned char smem[];
   float *inb = reinterpret_cast<float *>(smem);
-  float2 *xb = reinterpret_cast<float2 *>(smem + (size_t)2 * C::IN_FLOATS * 4);
-  uint64_t *bar = reinterpret_cast<uint64_t *>(smem + (size_t)2 * C::IN_FLOATS * 4 + (size_t)2 * C::BH * kDTX * 8);
+  float2 *xb = reinterpret_cast<float2 *>(smem + (size_t)kDogIn * C::IN_FLOATS * 4);
+  uint64_t *bar = reinterpret_cast<uint64_t *>(smem + (size_t)kDogIn * C::IN_FLOATS * 4 + (size_t)2 * C::BH * kDTX * 8);
   const int t = threadIdx.x;
   __shared__ float2 tap_sh[TapPairs<RA, RB>::N + TapPairs<ZA, ZB>::N];
   __shared__ int s_item;
   if (t == 0) {
-    mbar_init(&bar[0], 1);
-    mbar_init(&bar[1], 1);
+    for (int i = 0; i < kDogIn; i++) mbar_init(&bar[i], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     TapPairs<RA, RB>::stage(T, 0, 2, tap_sh);
     TapPairs<ZA, ZB>::stage(T, 1, 3, tap_sh + TapPairs<RA, RB>::N);
   }
   bool ok = true;
   // slices loaded by this block before the current tile: slice `it` of a tile is the block's
-  // (gbase + it)-th, which picks its input buffer and barrier phase
+  // (gbase + it)-th, which picks its input buffer (g mod kDogIn) and barrier phase
   uint32_t gbase = 0;
   for (;;) {
   int sub, tile;
@@ -506,7 +512,11 @@ __global__ void __launch_bounds__(DogT<RA, RB, ZA, ZB>::NT, 3)
   const int D = S.D, W = S.W, H = S.H;
   constexpr uint32_t tma_bytes = (uint32_t)(C::BW * C::BH * 4);
   const int tx = x0 - C::HX, ty = y0 - C::RXY;
-  if (t == 0 && ok && D > 0) tma_slice(&map, inb + (gbase & 1) * C::IN_FLOATS, &bar[gbase & 1], tx, ty, 0, sub, tma_bytes);
+  if (t == 0 && ok)
+    for (int z = 0; z < kDogIn - 1 && z < D; z++) {
+      const uint32_t g = gbase + (uint32_t)z;
+      tma_slice(&map, inb + (g % kDogIn) * C::IN_FLOATS, &bar[g % kDogIn], tx, ty, z, sub, tma_bytes);
+    }
   // stage B ownership: columns (cx, cy) and (cx, cy + 1) of the tile
   const int cx = t % kDTX, cy = 2 * (t / kDTX);
   const int gx = x0 + cx, gy = y0 + cy;
@@ -526,9 +536,10 @@ __global__ void __launch_bounds__(DogT<RA, RB, ZA, ZB>::NT, 3)
   // is a fixed register (the loop below runs WIN steps per trip).
   auto step = [&](int it, auto PC) {
     constexpr int PH = (decltype(PC)::value + C::WIN - 1) % C::WIN;
-    const uint32_t gn = gbase + (uint32_t)it + 1u;   // the block's count of slice it + 1
-    if (t == 0 && ok && it + 1 < D)
-      tma_slice(&map, inb + (gn & 1) * C::IN_FLOATS, &bar[gn & 1], tx, ty, it + 1, sub, tma_bytes);
+    // slice it + kDogIn - 1 goes to the buffer of slice it - 1, read before the last barrier
+    const uint32_t gn = gbase + (uint32_t)(it + kDogIn - 1);
+    if (t == 0 && ok && it + kDogIn - 1 < D)
+      tma_slice(&map, inb + (gn % kDogIn) * C::IN_FLOATS, &bar[gn % kDogIn], tx, ty, it + kDogIn - 1, sub, tma_bytes);
     // ---- B: y pass of slice zy (zero past the volume: the border taps still multiply),
     // z shift register, DoG slice zy - RZ
     const int zy = it - 1;
@@ -548,11 +559,11 @@ __global__ void __launch_bounds__(DogT<RA, RB, ZA, ZB>::NT, 3)
     // ---- A: x pass of slice it
     if (it < D) {
       const uint32_t gi = gbase + (uint32_t)it;
-      if (ok && !mbar_wait(&bar[gi & 1], (gi >> 1) & 1)) {
+      if (ok && !mbar_wait(&bar[gi % kDogIn], (gi / kDogIn) & 1)) {
         ok = false;
         atomicExch(status, HDOG_ERR_TIMEOUT);
       }
-      const float *ib = inb + (gi & 1) * C::IN_FLOATS;
+      const float *ib = inb + (gi % kDogIn) * C::IN_FLOATS;
       float2 *xo = xb + (it & 1) * C::BH * kDTX;
       for (int item = t; item < C::XITEMS; item += C::NT) {
         const int row = item / C::XQ, q = item % C::XQ;

@@ -78,6 +78,7 @@ def soft_loss(vol, sigma, pos, neg, thresh=None, radius_norm_xy=20, radius_norm_
     """Mean relaxed mask score at pos minus that at neg (see the module docstring)."""
     if thresh is None:
         thresh = torch.zeros(3, dtype=torch.float32)
+    pos, neg = pos.contiguous(), neg.contiguous()
     return SoftLoss.apply(vol, sigma, thresh, pos, neg, (radius_norm_xy, radius_norm_z, min_intensity, tau, gamma))
 
 

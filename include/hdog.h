@@ -351,7 +351,10 @@ int hdog_ccl_edge_count(hdog_ctx *ctx, int64_t *edges, int64_t *capacity);
 /* When on, every kernel launch of the context's calls is bracketed by two events. */
 int hdog_timing_enable(hdog_ctx *ctx, int on);
 /* Writes "kernel_name launches total_ms\n" lines accumulated since the last read
-   (waiting for the recorded events), then resets the accumulators. */
+   (waiting for the recorded events), then resets the accumulators.  Names starting with
+   "host_" are wall times of host phases of the whole-chain calls (enqueueing a batch,
+   waiting for it, collecting its records, waiting for a host stack's chunk, the final copy
+   to the caller's buffer). */
 int hdog_timing_read(hdog_ctx *ctx, char *buf, size_t cap);
 
 /* ---- small helpers for bindings without a CUDA runtime of their own ---- */

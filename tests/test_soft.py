@@ -164,7 +164,7 @@ def test_gpu_adjoint_on_a_crop_of_the_workload_volume():
     inside = nuc[(nuc[:, 0] >= x0 + 4) & (nuc[:, 0] < x0 + W_ - 4) & (nuc[:, 1] >= y0 + 4) &
                  (nuc[:, 1] < y0 + H_ - 4) & (nuc[:, 2] >= z0 + 3) & (nuc[:, 2] < z0 + D_ - 3)]
     assert len(inside) >= 3
-    pos = np.rint(inside[:, [2, 1, 0]] - [z0, y0, x0]).astype(np.int32)
+    pos = np.ascontiguousarray(np.rint(inside[:, [2, 1, 0]] - [z0, y0, x0]).astype(np.int32))
     rng = np.random.default_rng(8)
     neg = np.stack([rng.integers(0, D_, 40), rng.integers(0, H_, 40), rng.integers(0, W_, 40)], 1).astype(np.int32)
     rxy, rz = 6, 3
