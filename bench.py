@@ -246,20 +246,19 @@ def camera_config(n_gpus):
 
 
 def profile_case():
-    """A small case of the same kernels for multi-pass ncu captures: one 1280 x 1080 x 32
-    substack (15000 seeded nuclei, the workload's parameters), run twice."""
+    """The small case of the ncu captures: substack 0 of the camera stack (2560 x 2160 x 32,
+    177 M voxels, the workload's density of nuclei and parameters) through the whole chain,
+    one warm-up run and one captured run."""
     import torch
     import hdog
-    from hdog import synth
-    w, h, d = 1280, 1080, 32
-    vol = synth.volume(synth.spec(w, h, d, 15000, synth.SEED_BASE + 21, pair_fraction=0.1))
-    p = hdog.make_params(**dict(PARAMS, width=w, height=h, depth=d))
+    vol, _ = make_stack()
+    p = hdog.make_params(**PARAMS)
     with hdog.Context(p) as ctx:
-        dv = torch.from_numpy(vol).cuda()
+        dv = torch.from_numpy(np.ascontiguousarray(vol[:DEPTH])).cuda()
         for _ in range(2):
-            r = ctx.run_substack(dv, d, 0)
+            r = ctx.run_substack(dv, DEPTH, 0)
     torch.cuda.synchronize()
-    print(json.dumps({"profile_case": "1280x1080x32 substack", "records": int(len(r))}))
+    print(json.dumps({"profile_case": "camera substack 0, 2560x2160x32", "records": int(len(r))}))
     return 0
 
 
@@ -521,7 +520,7 @@ def main():
                     help="camera: the 2560x2160x128 stack (default); uneven: the 40-stack mix; "
                          "stream: the 17 GB stack from host memory; soft: the differentiable chain")
     ap.add_argument("--profile-case", action="store_true",
-                    help="run one 1280x1080x32 substack twice (the small case the ncu summaries capture)")
+                    help="run substack 0 of the camera stack twice (the small case the ncu summaries capture)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

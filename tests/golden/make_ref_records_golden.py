@@ -47,6 +47,18 @@ def compare(ours, ref, st64, bl64):
         out["exact_fields_equal"] = False
         return out
     out["exact_fields_equal"] = bool(exact_fields(ours).tobytes() == exact_fields(ref).tobytes())
+    def bits(a):
+        return a.view(np.uint32) if a.dtype.itemsize == 4 else a.view(np.uint16)
+    diff = {f: bits(ours[f]) != bits(ref[f]) for f in EXACT}
+    out["exact_field_mismatches"] = {f: int(d.sum()) for f, d in diff.items()}
+    bad = np.zeros(len(ours), bool)
+    for d in diff.values():
+        bad |= d
+    if bad.any():
+        idx = np.nonzero(bad)[0]
+        out["mismatch_region_sizes"] = sorted(int(x) for x in ref["size"][idx])[-20:]
+        out["mismatch_examples"] = [dict([(f, float(ours[f][i])) for f in EXACT] +
+                                         [("reference_" + f, float(ref[f][i])) for f in EXACT]) for i in idx[:5]]
     for f, f64 in (("structureness", st64), ("blobness", bl64)):
         out[f + "_max_rel_vs_reference"] = rel(ours[f], ref[f])
         out[f + "_max_rel_ours_vs_fp64"] = rel(ours[f], f64)
