@@ -658,16 +658,29 @@ __device__ __forceinline__ void flush_stage(const FgEntry *stage, int n, const S
   const int64_t room = S.fg_cap - (int64_t)base;
   const int keep = room <= 0 ? 0 : (room < n ? (int)room : n);
   const float *nv = norm + S.vox;
-  for (int i = lane; i < keep; i += 32) {
-    const float4 *src = reinterpret_cast<const float4 *>(stage + i);
-    float4 a = src[0];
-    const float4 b = src[1];
-    const int32_t idx = __float_as_int(a.x);
-    a.y = __ldg(nv + idx);
-    float4 *dst = reinterpret_cast<float4 *>(fg + S.fg + base + i);
-    dst[0] = a;
-    dst[1] = b;
-    fg_idx[S.fg + base + i] = idx;
+  // every lane's gathers are issued before any of them is used, so a flush waits for one
+  // global-load latency rather than one per entry
+  constexpr int kPer = kHStage / 32;
+  int32_t idx[kPer];
+  float nvv[kPer];
+#pragma unroll
+  for (int u = 0; u < kPer; u++) {
+    const int i = lane + 32 * u;
+    idx[u] = i < keep ? stage[i].idx : 0;
+    nvv[u] = i < keep ? __ldg(nv + idx[u]) : 0.0f;
+  }
+#pragma unroll
+  for (int u = 0; u < kPer; u++) {
+    const int i = lane + 32 * u;
+    if (i < keep) {
+      const float4 *src = reinterpret_cast<const float4 *>(stage + i);
+      float4 a = src[0];
+      a.y = nvv[u];
+      float4 *dst = reinterpret_cast<float4 *>(fg + S.fg + base + i);
+      dst[0] = a;
+      dst[1] = src[1];
+      fg_idx[S.fg + base + i] = idx[u];
+    }
   }
   __syncwarp();
 }

@@ -30,7 +30,9 @@ def sha(a):
 
 
 def exact_fields(rec):
-    return np.ascontiguousarray(rec[list(EXACT)])
+    """The exact fields alone, packed (a multi-field view keeps the other fields' bytes)."""
+    from numpy.lib import recfunctions as rfn
+    return np.ascontiguousarray(rfn.repack_fields(rec[list(EXACT)]))
 
 
 def rel(a, b):

@@ -98,4 +98,5 @@ def test_oracle_reproduces_the_reference_path_on_a_full_camera_substack():
     assert sha(mask) == g["substack0_stage_sha256"]["pd"]
     assert sha(labels) == g["substack0_stage_sha256"]["labels"]
     assert len(rec) == g["substack0_records"]
-    assert sha(np.ascontiguousarray(rec[list(EXACT)])) == g["substack0_exact_fields_sha256"]
+    from numpy.lib import recfunctions as rfn
+    assert sha(rfn.repack_fields(rec[list(EXACT)])) == g["substack0_exact_fields_sha256"]
