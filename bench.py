@@ -377,24 +377,8 @@ STREAM = ("dense stack uint16 2560x2160x1536 (17 GB) in pinned host memory, 1.5M
 
 
 def stream_nuclei(w, h, d, total, seed):
-    """total nuclei, 30% of them in clusters of 2-6: each cluster's extra members touch its
-    first one, at centre distance 0.8 (sigma_a + sigma_b) along a random direction."""
     from hdog import synth
-    rng = np.random.default_rng(seed)
-    sizes = rng.integers(2, 7, size=int(0.3 * total) // 2 + 1)
-    sizes = sizes[: np.searchsorted(np.cumsum(sizes), int(0.3 * total)) + 1]
-    n_seed = total - int(sizes.sum()) + len(sizes)
-    base = synth.nuclei(synth.spec(w, h, d, n_seed, seed))   # (x, y, z, sigma_xy, sigma_z, peak)
-    first = np.repeat(np.arange(len(sizes)), sizes - 1)       # the cluster each extra member joins
-    extra = base[rng.integers(len(base), size=len(first))].copy()
-    v = rng.normal(size=(len(first), 3))
-    v /= np.linalg.norm(v, axis=1, keepdims=True)
-    a = base[first]
-    dist = 0.8 * (a[:, 3] + extra[:, 3])
-    extra[:, :3] = a[:, :3] + v * np.stack([dist, dist, dist * a[:, 4] / a[:, 3]], axis=1)
-    keep = (extra[:, 0] >= 0) & (extra[:, 0] < w) & (extra[:, 1] >= 0) & (extra[:, 1] < h) & \
-           (extra[:, 2] >= 0) & (extra[:, 2] < d)
-    return np.concatenate([base, extra[keep]])
+    return synth.clustered_nuclei(w, h, d, total, seed)
 
 
 def stream_workload(args):

@@ -329,9 +329,10 @@ constexpr int kHRing = 8;              // ring slots; a slot is 40 x 20 floats =
 constexpr int kHThreads = kHTX / 4 * kHTY;   // one x quad per thread
 
 // Input slices of the DoG sweep in flight: slice it + kDogIn - 1 is requested while slice it
-// is filtered.
+// is filtered (2, 3 and 4 measured the same on the camera stack; 2 keeps the buffer index a
+// bit mask).
 #ifndef HDOG_DOG_STAGES
-#define HDOG_DOG_STAGES 3
+#define HDOG_DOG_STAGES 2
 #endif
 constexpr int kDogIn = HDOG_DOG_STAGES;
 
@@ -388,6 +389,24 @@ __device__ __forceinline__ void tap2(const DogTaps &T, const TapPairs<RA, RB> &K
   else if (b) acc.y = __fmaf_rn(T.k[kb][RB - J], v.y, acc.y);
   else if (a) acc.x = __fmaf_rn(T.k[ka][RA - J], v.x, acc.x);
 }
+
+// x pass input by input: staged input w[I] is tap I - BASE - o of output o (o = 0..3), so its
+// duplicated pair (one value for both scales of an f32x2 FMA) is formed once and used by up
+// to four consecutive FMAs.  Every output still takes its taps in ascending order.
+template <int RA, int RB, int BASE, int I, int NV>
+struct XIn {
+  __device__ __forceinline__ static void run(const DogTaps &T, const TapPairs<RA, RB> &K, const float (&w)[NV],
+                                             float2 (&a)[4]) {
+    if constexpr (I < NV) {
+      const float2 d = make_float2(w[I], w[I]);
+      tap2<RA, RB, I - BASE>(T, K, 0, 2, d, a[0]);
+      tap2<RA, RB, I - BASE - 1>(T, K, 0, 2, d, a[1]);
+      tap2<RA, RB, I - BASE - 2>(T, K, 0, 2, d, a[2]);
+      tap2<RA, RB, I - BASE - 3>(T, K, 0, 2, d, a[3]);
+      XIn<RA, RB, BASE, I + 1, NV>::run(T, K, w, a);
+    }
+  }
+};
 
 template <int RA, int RB, int J, int N>
 struct TapLoop {
@@ -565,7 +584,8 @@ __global__ void __launch_bounds__(DogT<RA, RB, ZA, ZB>::NT, 3)
       }
       const float *ib = inb + (gi % kDogIn) * C::IN_FLOATS;
       float2 *xo = xb + (it & 1) * C::BH * kDTX;
-      for (int item = t; item < C::XITEMS; item += C::NT) {
+      // one item per thread when the items fit the block (no loop, no reconvergence)
+      for (int item = t; item < C::XITEMS; item += (C::XITEMS <= C::NT ? C::XITEMS : C::NT)) {
         const int row = item / C::XQ, q = item % C::XQ;
         const float *in = ib + row * C::BW + 4 * q;
         float w[C::NV];
@@ -575,7 +595,7 @@ __global__ void __launch_bounds__(DogT<RA, RB, ZA, ZB>::NT, 3)
           w[i] = f.x; w[i + 1] = f.y; w[i + 2] = f.z; w[i + 3] = f.w;
         }
         float2 a[4] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
-        TapLoop<RA, RB, -C::RXY, 2 * C::RXY + 1>::x4(T, kxy, w, C::OFF + C::RXY, a);
+        XIn<RA, RB, C::OFF + C::RXY, 0, C::NV>::run(T, kxy, w, a);
         float4 *o = reinterpret_cast<float4 *>(xo + row * kDTX + 4 * q);
         o[0] = make_float4(a[0].x, a[0].y, a[1].x, a[1].y);
         o[1] = make_float4(a[2].x, a[2].y, a[3].x, a[3].y);

@@ -90,3 +90,26 @@ def volume(s, z_begin=0, z_end=None, nuc=None):
     if rc != 0:
         raise HDoGError(HDOG_ERR_ARG, "render failed")
     return out
+
+
+def clustered_nuclei(w, h, d, total, seed, cluster_fraction=0.3, sizes=(2, 6)):
+    """`total` nuclei, `cluster_fraction` of them in clusters of sizes[0]..sizes[1] members
+    (the dense streaming stack): a cluster's extra members touch its first one, at centre
+    distance 0.8 (sigma_a + sigma_b) along a random direction (the z offset scaled by
+    sigma_z / sigma_xy).  Rows as nuclei(): x, y, z, sigma_xy, sigma_z, peak."""
+    rng = np.random.default_rng(seed)
+    n_cl = int(cluster_fraction * total)
+    cs = rng.integers(sizes[0], sizes[1] + 1, size=n_cl // sizes[0] + 1)
+    cs = cs[: np.searchsorted(np.cumsum(cs), n_cl) + 1]
+    n_seed = total - int(cs.sum()) + len(cs)
+    base = nuclei(spec(w, h, d, n_seed, seed))
+    first = np.repeat(np.arange(len(cs)), cs - 1)            # the cluster each extra member joins
+    extra = base[rng.integers(len(base), size=len(first))].copy()
+    v = rng.normal(size=(len(first), 3))
+    v /= np.linalg.norm(v, axis=1, keepdims=True)
+    a = base[first]
+    dist = 0.8 * (a[:, 3] + extra[:, 3])
+    extra[:, :3] = a[:, :3] + v * np.stack([dist, dist, dist * a[:, 4] / a[:, 3]], axis=1)
+    keep = (extra[:, 0] >= 0) & (extra[:, 0] < w) & (extra[:, 1] >= 0) & (extra[:, 1] < h) & \
+           (extra[:, 2] >= 0) & (extra[:, 2] < d)
+    return np.concatenate([base, extra[keep]])
