@@ -564,8 +564,11 @@ def main():
     if dist:
         dist.barrier()
     t0 = time.perf_counter()
+    call_ms = []
     for _ in range(args.steps):
-        recs_e2e = batched.run_stack(host_np, out=e2e_out)
+        tc = time.perf_counter()
+        recs_e2e = batched.run_stack(host_np, out=e2e_out)   # returns after its records are in e2e_out
+        call_ms.append((time.perf_counter() - tc) * 1e3)
     torch.cuda.synchronize()
     e2e_ms = (time.perf_counter() - t0) * 1e3
     e2e_ms = max_over_ranks(e2e_ms, dist) / args.steps
@@ -629,6 +632,8 @@ def main():
         "e2e": {"value": unique * ws / (e2e_ms * 1e-3) / 1e9, "unit": "Gvox/s",
                 "h2d_bytes_per_step": unique * 2, "d2h_bytes_per_step": n_records * 28,
                 "ms_per_step": e2e_ms, "pinned_h2d_gbs": round(h2d_gbs, 1),
+                "call_ms": {"median": round(statistics.median(call_ms), 2), "min": round(min(call_ms), 2),
+                            "max": round(max(call_ms), 2)},
                 "one_call": {"kernel_ms": e2e_kernel_ms,
                              "host_ms": {k: v for k, v in e2e_phases.items() if k.startswith("host_")}}},
         "gpu_launches": int(launches),
