@@ -18,6 +18,8 @@
 #include <thread>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "json_min.hpp"
 #include "kernels.cuh"
 
@@ -259,6 +261,7 @@ struct hdog_ctx {
   std::vector<cudaEvent_t> chunk_ev;
   cudaEvent_t start_ev = nullptr;
   int host_batch = 1;   // substacks in the first batch of a host-input stack (0: max_sub)
+  int64_t walk_limit = 0;   // HDOG_OPT_WALK_LIMIT (0: the substack's voxel count)
   EventTimer *timer = nullptr;
 };
 
@@ -480,6 +483,7 @@ static void set_sub(hdog_ctx *c, int s, const uint16_t *src, int depth_valid, in
   S.fg = (int64_t)s * c->fg_cap;
   S.fg_cap = c->fg_cap;
   S.src = src;
+  S.walk_limit = c->walk_limit;
   const int ms = c->max_sub;
   c->h_seg[0 * ms + s] = S.blk;
   c->h_seg[1 * ms + s] = (c->nvox + kScanBlock - 1) / kScanBlock;
@@ -646,6 +650,10 @@ static int enqueue_batch(hdog_ctx *c, int nsub, bool fused, cudaStream_t st) {
 }
 
 static int run_batch(hdog_ctx *c, int nsub, cudaStream_t st) {
+  nvtxRangePushA("hdog batch");
+  struct Pop {
+    ~Pop() { nvtxRangePop(); }
+  } pop;
   const bool fused = fused_ok(c);
   {
     HostPhase ph(c, "host_enqueue_batch");
@@ -1491,7 +1499,8 @@ struct StackSpec {
   std::string dst;
 };
 
-static int load_param_file(const char *path, hdog_params *p, std::vector<StackSpec> *stacks, int *verbose) {
+static int load_param_file(const char *path, hdog_params *p, std::vector<StackSpec> *stacks, int *verbose,
+                           int *skip_existing = nullptr) {
   if (!path || !p) return fail(HDOG_ERR_ARG, "null argument");
   std::ifstream f(path, std::ios::binary);
   if (!f.is_open()) return fail(HDOG_ERR_IO, std::string("Unable to open file ") + path);
@@ -1546,6 +1555,10 @@ static int load_param_file(const char *path, hdog_params *p, std::vector<StackSp
     if (jnum(er, "z", v, false, w) == HDOG_OK) p->erosion_radius_z = (int)v;
   }
   if (jnum(&root, "is_ave_mode", v, false, "") == HDOG_OK) p->is_ave_mode = v != 0;
+  if (skip_existing) {
+    *skip_existing = 0;
+    if (jnum(&root, "skip_existing", v, false, "") == HDOG_OK) *skip_existing = v != 0;
+  }
   if (stacks) {
     stacks->clear();
     const json::Value *st = root.get("stacks");
@@ -1572,7 +1585,8 @@ extern "C" int hdog_params_load_json(const char *path, hdog_params *p) {
 }
 
 // loadImage (utils.h:160-173): the first W*H uint16 values of the file.  A file with
-// no data is an error; a short file leaves the rest of the slice zero.
+// no data is an error; a short file leaves the rest of the slice zero, where the reference
+// leaves whatever its reused pinned buffer held from an earlier slice.
 static int load_slice(const std::string &path, uint16_t *dst, size_t n) {
   FILE *f = fopen(path.c_str(), "rb");
   if (!f) return fail(HDOG_ERR_IO, "Unable to open " + path);
@@ -1583,11 +1597,18 @@ static int load_slice(const std::string &path, uint16_t *dst, size_t n) {
   return HDOG_OK;
 }
 
+// Each stack's records go to "<dst_path>.part" and are renamed to dst_path once the stack is
+// complete, so an interrupted run leaves no truncated result (the reference removes dst_path
+// and appends substack by substack, HDoG3D_main.cpp:295-300, utils.h:216,246; the finished
+// file is the same).  With the top-level key "skip_existing" (not a reference key; default
+// false) a stack whose dst_path exists is skipped, which resumes an interrupted run.  With
+// verbose, a JSON metrics line closes the run.
 extern "C" int hdog_run_param_file(const char *param_path, int verbose) {
+  const auto t_start = std::chrono::steady_clock::now();
   hdog_params p;
   std::vector<StackSpec> stacks;
-  int file_verbose = 0;
-  TRY(load_param_file(param_path, &p, &stacks, &file_verbose));
+  int file_verbose = 0, skip_existing = 0;
+  TRY(load_param_file(param_path, &p, &stacks, &file_verbose, &skip_existing));
   verbose = verbose || file_verbose;
   int margin = 0;
   TRY(validate(&p));
@@ -1605,45 +1626,78 @@ extern "C" int hdog_run_param_file(const char *param_path, int verbose) {
   size_t h_cap = 0;
   RecordBuf &recs = ctx->last;
   int rc = HDOG_OK;
+  int64_t n_done = 0, n_skipped = 0, slices = 0, records = 0;
+  double io_s = 0.0;
   for (size_t i = 0; i < stacks.size() && rc == HDOG_OK; i++) {
     const StackSpec &sp = stacks[i];
-    remove(sp.dst.c_str());   // the result is written in append mode (HDoG3D_main.cpp:295-300)
+    if (skip_existing) {
+      if (FILE *e = fopen(sp.dst.c_str(), "rb")) {
+        fclose(e);
+        n_skipped++;
+        continue;
+      }
+    }
+    remove(sp.dst.c_str());
     const int length = (int)sp.src.size();
     TRY(schedule(length, p.depth, margin, z0s));
     if (z0s.empty()) continue;
+    nvtxRangePushA("hdog stack");
     const size_t need = (size_t)length * plane;
     if (need > h_cap) {
       if (h_stack) cudaFreeHost(h_stack);
       h_stack = nullptr;
       if (cudaMallocHost(&h_stack, need * sizeof(uint16_t)) != cudaSuccess) {
         rc = fail(HDOG_ERR_NOMEM, "pinned host buffer for the stack failed");
+        nvtxRangePop();
         break;
       }
       h_cap = need;
     }
     // only the slices some substack reads
+    const auto t_io = std::chrono::steady_clock::now();
     const int last = std::min(length, z0s.back() + p.depth);
     for (int z = 0; z < last && rc == HDOG_OK; z++) rc = load_slice(sp.src[z], h_stack + (size_t)z * plane, plane);
-    if (rc != HDOG_OK) break;
+    io_s += std::chrono::duration<double>(std::chrono::steady_clock::now() - t_io).count();
+    if (rc != HDOG_OK) { nvtxRangePop(); break; }
     recs.clear();
     {
       std::lock_guard<std::mutex> lock(ctx->mu);
       rc = run_stack_locked(ctx, h_stack, 0, last, recs, nullptr);
     }
+    nvtxRangePop();
     if (rc != HDOG_OK) break;
     const int64_t n = (int64_t)recs.n;
-    FILE *f = fopen(sp.dst.c_str(), "ab");
-    if (!f) { rc = fail(HDOG_ERR_IO, "Unable to open " + sp.dst); break; }
+    const std::string part = sp.dst + ".part";
+    FILE *f = fopen(part.c_str(), "wb");
+    if (!f) { rc = fail(HDOG_ERR_IO, "Unable to open " + part); break; }
     if (n > 0 && fwrite(recs.p, sizeof(hdog_record), (size_t)n, f) != (size_t)n) {
       fclose(f);
+      remove(part.c_str());
+      rc = fail(HDOG_ERR_IO, "Unable to write " + part);
+      break;
+    }
+    if (fclose(f) != 0 || rename(part.c_str(), sp.dst.c_str()) != 0) {
+      remove(part.c_str());
       rc = fail(HDOG_ERR_IO, "Unable to write " + sp.dst);
       break;
     }
-    fclose(f);
+    n_done++;
+    slices += length;
+    records += n;
     if (verbose) printf("stack %zu: %d slices, %zu substacks, saved count:%lld\n", i, length, z0s.size(), (long long)n);
   }
   if (h_stack) cudaFreeHost(h_stack);
   hdog_ctx_destroy(ctx);
+  if (verbose) {
+    const double t = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+    const double vox = (double)slices * (double)plane;
+    printf("{\"hdog_main\": {\"status\": %d, \"stacks_done\": %lld, \"stacks_skipped\": %lld, \"slices\": %lld, "
+           "\"voxels\": %.0f, \"records\": %lld, \"seconds\": %.3f, \"slice_read_seconds\": %.3f, "
+           "\"gvox_per_s\": %.3f}}\n",
+           rc, (long long)n_done, (long long)n_skipped, (long long)slices, vox, (long long)records, t, io_s,
+           t > 0 ? vox / t / 1e9 : 0.0);
+    fflush(stdout);
+  }
   return rc;
 }
 
@@ -1656,6 +1710,10 @@ extern "C" int hdog_ctx_set_option(hdog_ctx *c, int option, int value) {
     case HDOG_OPT_HOST_BATCH:
       if (value < 0) return fail(HDOG_ERR_ARG, "HDOG_OPT_HOST_BATCH must be >= 0");
       c->host_batch = value;
+      return HDOG_OK;
+    case HDOG_OPT_WALK_LIMIT:
+      if (value < 0) return fail(HDOG_ERR_ARG, "HDOG_OPT_WALK_LIMIT must be >= 0");
+      c->walk_limit = value;
       return HDOG_OK;
     default: return fail(HDOG_ERR_ARG, "unknown option");
   }

@@ -560,7 +560,7 @@ __global__ void k_ccl_edges(const Sub *subs, const int2 *edges, const unsigned l
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < (int64_t)cnt;
        e += (int64_t)gridDim.x * blockDim.x) {
     const int2 ab = edges[S.edge + e];
-    uf_union(L, ab.x, ab.y, n, status);
+    uf_union(L, ab.x, ab.y, S.walk_limit > 0 ? S.walk_limit : n, status);
   }
 }
 
@@ -589,7 +589,7 @@ __global__ void __launch_bounds__(kCclThreads) k_ccl_cross_direct(const Sub *sub
         back_offset(o, dz, dy, dx);
         if (!leaves_tile(S, T, x + k, y, z, lx0 + k, ly, lz, dz, dy, dx)) continue;
         const int64_t gn = g + dz * WH + dy * (int64_t)S.W + dx;
-        if (gn >= 1 && m[gn]) uf_union(L, (int32_t)g, (int32_t)gn, n, status);
+        if (gn >= 1 && m[gn]) uf_union(L, (int32_t)g, (int32_t)gn, S.walk_limit > 0 ? S.walk_limit : n, status);
       }
     }
   }
@@ -628,7 +628,7 @@ __global__ void __launch_bounds__(256) k_ccl_flatten(const Sub *subs, uint8_t *m
 #pragma unroll
     for (int k = 0; k < 16; k++) {
       if (l[k] < 0) continue;
-      const int32_t r = p[k] == l[k] ? l[k] : uf_root(L, p[k], n, status);
+      const int32_t r = p[k] == l[k] ? l[k] : uf_root(L, p[k], S.walk_limit > 0 ? S.walk_limit : n, status);
       if (r != l[k]) L[i0 + k] = r;
       if (r == (int32_t)(i0 + k)) bits |= 1u << k;
     }
@@ -690,7 +690,7 @@ __global__ void __launch_bounds__(256) k_ccl_flatten_fg(const Sub *subs, const u
 #pragma unroll
     for (int k = 0; k < kFlatFgPerThread; k++) {
       if (l[k] < 0) continue;
-      const int32_t r = p[k] == l[k] ? l[k] : uf_root(L, p[k], n, status);
+      const int32_t r = p[k] == l[k] ? l[k] : uf_root(L, p[k], S.walk_limit > 0 ? S.walk_limit : n, status);
       if (r != l[k]) L[idx[k]] = r;
       fg_root[S.fg + e0 + 32 * k] = r;   // the entry's root, read by the region accumulation
       if (r == idx[k]) {

@@ -22,6 +22,7 @@ struct Sub {
   int64_t fg;             // offset of its foreground list (fused DoG/Hessian sweep)
   int64_t fg_cap;         // foreground list capacity
   const uint16_t *src;    // slice 0 of the raw input (device); slices are W*H apart
+  int64_t walk_limit;     // bound of the labelling's union-find walks and retries (0: W*H*D)
 };
 
 // A device work queue of (substack, tile) items for a persistent launch: item i is tile

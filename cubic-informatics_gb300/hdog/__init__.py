@@ -23,7 +23,7 @@ MAIN_PATH = os.path.join(BUILD_DIR, "hdog_main")
 
 HDOG_OK, HDOG_ERR_ARG, HDOG_ERR_SHAPE, HDOG_ERR_CUDA, HDOG_ERR_IO = 0, 1, 2, 3, 4
 HDOG_ERR_PARAM, HDOG_ERR_CAPACITY, HDOG_ERR_TIMEOUT, HDOG_ERR_NOMEM = 5, 6, 7, 8
-HDOG_OPT_FUSED_SWEEP, HDOG_OPT_HOST_BATCH = 1, 2
+HDOG_OPT_FUSED_SWEEP, HDOG_OPT_HOST_BATCH, HDOG_OPT_WALK_LIMIT = 1, 2, 3
 
 # The 28-byte candidate record (FeatureVector, src/3D/utils.h:188-197).
 DT_LOCAL = np.dtype([
@@ -331,6 +331,11 @@ class Context:
         e, c = ctypes.c_int64(), ctypes.c_int64()
         check(lib().hdog_ccl_edge_count(self._h, ctypes.byref(e), ctypes.byref(c)))
         return e.value, c.value
+
+    def set_walk_limit(self, n):
+        """Bound of the labelling's union-find walks (0: the default, no walk reaches it); a
+        walk past it makes the call raise HDoGError with HDOG_ERR_TIMEOUT."""
+        check(lib().hdog_ctx_set_option(self._h, HDOG_OPT_WALK_LIMIT, int(n)))
 
     def timing(self, on=True):
         """Per-kernel CUDA-event timing of this context's launches."""

@@ -331,13 +331,18 @@ int hdog_soft_backward(const hdog_soft_params *p, const float *d_volume, const i
 enum {
   HDOG_OPT_FUSED_SWEEP = 1,  /* 1 (default): DoG, Hessian and the PD test in one z-sweep kernel
                                 when the radii allow; 0: separate passes (same results) */
-  HDOG_OPT_HOST_BATCH = 2    /* substacks in the first batch when hdog_run_stack gets its stack
+  HDOG_OPT_HOST_BATCH = 2,   /* substacks in the first batch when hdog_run_stack gets its stack
                                 in host memory (default 1; 0: as many as the context holds);
                                 each later batch holds at most twice as many as the one before
                                 (and at most what the context holds): the stack is copied in
                                 chunks on a second stream and each batch waits only for its own
                                 slices, so the copy of each chunk overlaps the batch before it.
                                 Records are the same for every value. */
+  HDOG_OPT_WALK_LIMIT = 3    /* bound of the labelling's union-find walks and link retries
+                                (default 0: the substack's voxel count, which no walk reaches).
+                                A smaller bound makes a walk that passes it give up and the call
+                                return HDOG_ERR_TIMEOUT instead of running on; the context stays
+                                usable.  For tests of that error path. */
 };
 int hdog_ctx_set_option(hdog_ctx *ctx, int option, int value);
 

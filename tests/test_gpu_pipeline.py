@@ -101,6 +101,57 @@ def test_hdog_main_executable_writes_reference_records(tmp_path):
     assert_records_match(got, ref, "hdog_main")
 
 
+def test_hdog_main_resume_metrics_and_a_short_slice(tmp_path):
+    """Two stacks; one slice file holds only half a slice (its tail reads as zero, where the
+    reference leaves its buffer's stale contents).  With verbose a JSON metrics line closes
+    the run; no ".part" file is left; with "skip_existing" a rerun recomputes only the stack
+    whose result was deleted, and gives the same file."""
+    import json
+    W, H, L, D = 128, 96, 40, 32
+    p = params(W, H, D, margins=3)
+    vols, stacks = [], []
+    for k in range(2):
+        vol = volume(W, H, L, n_nuclei=60, seed=70 + k)
+        d = tmp_path / ("src%d" % k)
+        d.mkdir()
+        src = []
+        for z in range(L):
+            f = d / ("%06d.bin" % z)
+            vol[z].tofile(f)
+            src.append(str(f))
+        if k == 1:   # slice 17 of stack 1: its first half only
+            short = vol[17].reshape(-1)[: W * H // 2]
+            short.tofile(src[17])
+            vol = vol.copy()
+            vol[17].reshape(-1)[W * H // 2:] = 0
+        vols.append(vol)
+        stacks.append((str(tmp_path / "out" / ("stack%d.bin" % k)), src))
+    (tmp_path / "out").mkdir()
+    pf = tmp_path / "param.json"
+    hdog.write_param_file(str(pf), p, stacks)
+    d = json.load(open(pf))
+    d["verbose"] = True
+    pf.write_text(json.dumps(d))
+    r = subprocess.run([hdog.MAIN_PATH, str(pf)], stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True)
+    assert r.returncode == 0, r.stderr
+    metrics = json.loads([l for l in r.stdout.splitlines() if l.startswith('{"hdog_main"')][-1])["hdog_main"]
+    assert metrics["stacks_done"] == 2 and metrics["slices"] == 2 * L and metrics["status"] == 0
+    assert not list((tmp_path / "out").glob("*.part"))
+    first = [np.fromfile(s[0], dtype=hdog.DT_LOCAL) for s in stacks]
+    for got, vol in zip(first, vols):
+        assert_records_match(got, orc.stack(orc.params_from(p), vol), "hdog_main stack")
+    assert metrics["records"] == sum(len(x) for x in first)
+    import os
+    os.remove(stacks[1][0])
+    d["skip_existing"] = True
+    pf.write_text(json.dumps(d))
+    r = subprocess.run([hdog.MAIN_PATH, str(pf)], stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True)
+    assert r.returncode == 0, r.stderr
+    metrics = json.loads([l for l in r.stdout.splitlines() if l.startswith('{"hdog_main"')][-1])["hdog_main"]
+    assert metrics["stacks_done"] == 1 and metrics["stacks_skipped"] == 1
+    assert np.fromfile(stacks[1][0], dtype=hdog.DT_LOCAL).tobytes() == first[1].tobytes()
+
+
 def test_erosion_opt_in_pipeline():
     W, H, D = 128, 128, 16
     vol = volume(W, H, D, n_nuclei=40, seed=5)

@@ -70,3 +70,20 @@ def test_ccl_edge_list_overflow_merges_from_the_mask(kind):
         assert 0 < edges <= cap, (edges, cap)
     ref, _ = orc.ccl(mask)
     assert np.array_equal(labels, ref), kind
+
+
+def test_bounded_union_find_walks_report_a_timeout_and_the_context_stays_usable():
+    """A walk bound of 1 on a full mask, whose tile roots merge across many tiles: a walk
+    passes the bound, the call reports HDOG_ERR_TIMEOUT (no hang), and with the default
+    bound restored the same context labels the mask as the oracle does."""
+    W, H, D = 256, 256, 32
+    mask = torch.from_numpy(np.ones((D, H, W), np.uint8)).cuda()
+    with hdog.Context(params(W, H, D)) as ctx:
+        ctx.set_walk_limit(1)
+        with pytest.raises(hdog.HDoGError) as e:
+            ctx.ccl(mask)
+        assert e.value.code == hdog.HDOG_ERR_TIMEOUT
+        ctx.set_walk_limit(0)
+        labels = ctx.ccl(mask).cpu().numpy()
+    ref, _ = orc.ccl(np.ones((D, H, W), np.uint8))
+    assert np.array_equal(labels, ref)
