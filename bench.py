@@ -371,63 +371,71 @@ def synth_seed(k):
     return synth.SEED_BASE + k
 
 
-STREAM = ("dense stack uint16 2560x2160x1536 (17 GB) in pinned host memory, 1.5M nuclei, 30% of them in "
-          "touching clusters of 2-6; HDoG depth 32 (96 overlapping substacks), sigma_dog (2,1.5,3.2,2.4), "
-          "radius_norm (20,5); per-substack labels as the reference")
-
 
 def stream_nuclei(w, h, d, total, seed):
     from hdog import synth
     return synth.clustered_nuclei(w, h, d, total, seed)
 
 
-def stream_workload(args):
-    """The 17 GB stack from pinned host memory through hdog_run_stack: its chunks are copied
-    on a second stream while the first batches run.  Batched (8 substacks per launch) and
-    plain (one per launch) forms, records compared."""
+def run_stream(d, total_nuclei, steps, warmup, dev_id=0):
+    """A dense stack of d slices (2560 x 2160) in pinned host memory, `total_nuclei` nuclei with
+    30% of them in touching clusters of 2-6, through hdog_run_stack: its chunks are copied on a
+    second stream while the first batches run.  Batched (8 substacks per launch) and plain (one
+    per launch) forms, end to end, records compared byte for byte."""
     import torch
     import hdog
     from hdog import synth
-    torch.cuda.set_device(0)
-    w, h, d = 2560, 2160, 1536
+    w, h = 2560, 2160
     t0 = time.time()
-    nuc = stream_nuclei(w, h, d, 1_500_000, synth.SEED_BASE + 4)
+    nuc = stream_nuclei(w, h, d, total_nuclei, synth.SEED_BASE + 4)
     spec = synth.spec(w, h, d, len(nuc), synth.SEED_BASE + 4)
     host = torch.empty((d, h, w), dtype=torch.uint16).pin_memory()
     hn = host.numpy()
     for z0 in range(0, d, 128):
         hn[z0:z0 + 128] = synth.volume(spec, z0, min(d, z0 + 128), nuc=nuc)
     gen_s = time.time() - t0
-    p = hdog.make_params(**PARAMS)
+    p = hdog.make_params(dev_id=dev_id, **PARAMS)
     unique = w * h * d
     res = {}
-    for name, max_sub, steps in (("batched", 8, args.steps), ("plain", 1, max(1, min(args.steps, 2)))):
+    for name, max_sub, n in (("batched", 8, steps), ("plain", 1, max(1, min(steps, 2)))):
         with hdog.Context(p, max_substacks=max_sub) as ctx:
             out = np.empty(0, hdog.DT_LOCAL)
-            for _ in range(max(1, args.warmup)):
+            for _ in range(max(1, warmup)):
                 r = ctx.run_stack(hn, out=out)
                 if len(r) > len(out):
                     out = np.empty(len(r), hdog.DT_LOCAL)
             torch.cuda.synchronize()
             t = time.perf_counter()
-            for _ in range(steps):
+            for _ in range(n):
                 r = ctx.run_stack(hn, out=out)
             torch.cuda.synchronize()
-            res[name] = ((time.perf_counter() - t) * 1e3 / steps, r.copy())
+            res[name] = ((time.perf_counter() - t) * 1e3 / n, r.copy())
     assert res["batched"][1].tobytes() == res["plain"][1].tobytes(), "batched and plain records differ"
     bms, pms = res["batched"][0], res["plain"][0]
     nsub = len(hdog.substack_schedule(d, DEPTH, hdog.depth_margin(p)))
-    line = {"metric": METRIC, "value": unique / (bms * 1e-3) / 1e9, "unit": "Gvox/s", "n_gpus": 1,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": bms, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": STREAM, "substacks": nsub, "nuclei": int(len(nuc)),
+    return {"value": unique / (bms * 1e-3) / 1e9, "ms_per_step": bms,
+            "config": {"workload": "dense stack uint16 2560x2160x%d in pinned host memory, %d nuclei, 30%% of them "
+                                   "in touching clusters of 2-6; HDoG depth 32 (%d overlapping substacks), sigma_dog "
+                                   "(2,1.5,3.2,2.4), radius_norm (20,5); per-substack labels as the reference"
+                                   % (d, len(nuc), nsub),
                        "unique_voxels_per_step": unique, "records_per_step": int(len(res["batched"][1])),
-                       "mode": "end to end: pinned host stack, chunked H2D overlapping the batches, records D2H",
                        "generator_s": round(gen_s, 1)},
+            "mode": "end to end: pinned host stack, chunked H2D overlapping the batches, records D2H",
             "plain": {"value": unique / (pms * 1e-3) / 1e9, "ms_per_step": pms, "mode": "one substack per launch"},
             "batched_over_plain": pms / bms,
             "e2e": {"value": unique / (bms * 1e-3) / 1e9, "unit": "Gvox/s", "h2d_bytes_per_step": unique * 2,
                     "d2h_bytes_per_step": int(len(res["batched"][1])) * 28}}
+
+
+def stream_workload(args):
+    """The 17 GB dense stack (2560 x 2160 x 1536, 1.5 M nuclei) end to end from host memory."""
+    import torch
+    torch.cuda.set_device(0)
+    r = run_stream(1536, 1_500_000, args.steps, args.warmup)
+    line = {"metric": METRIC, "value": r["value"], "unit": "Gvox/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": r["config"]}
+    line.update({k: v for k, v in r.items() if k not in ("value", "ms_per_step", "config")})
     print(json.dumps(line), flush=True)
     return 0
 
@@ -500,6 +508,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-uneven", action="store_true", help="skip the uneven-stack subset of the default line")
+    ap.add_argument("--no-stream", action="store_true", help="skip the dense-stack subset of the default line")
     ap.add_argument("--workload", default="camera", choices=["camera", "uneven", "stream", "soft"],
                     help="camera: the 2560x2160x128 stack (default); uneven: the 40-stack mix; "
                          "stream: the 17 GB stack from host memory; soft: the differentiable chain")
@@ -660,6 +669,11 @@ def main():
         u["plain"]["value"] = u["plain"]["value"] * ws
         line["uneven"] = u
         del ustacks
+    if not args.no_stream:
+        # the dense streaming stack at a quarter of its depth (384 slices, the same density of
+        # nuclei and clusters), end to end from host memory, batched against plain
+        torch.cuda.empty_cache()
+        line["stream"] = run_stream(384, 375_000, max(2, min(args.steps, 3)), 1, local)
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(vol)
     if rank == 0:
