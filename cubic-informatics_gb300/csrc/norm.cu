@@ -514,6 +514,24 @@ __device__ __forceinline__ void box_chain(int L, LoadF load, float2 (&acc)[K]) {
   }
 }
 
+// The y box chain with a compile-time window: K outputs from a window of K registers
+// (input j + k feeds output k at step j, in the reference's order: 0 + s0 + s1 + ...).
+template <int K, int L, class LoadF>
+__device__ __forceinline__ void box_chain_t(LoadF load, float2 (&acc)[K]) {
+  float2 win[K];
+#pragma unroll
+  for (int k = 0; k < K; k++) {
+    win[k] = load(k);
+    acc[k] = make_float2(0.f, 0.f);
+  }
+#pragma unroll
+  for (int j = 0; j < L; j++) {
+#pragma unroll
+    for (int k = 0; k < K; k++) acc[k] = add2(acc[k], win[(j + k) % K]);
+    if (j + K < L + K - 1) win[j % K] = load(j + K);
+  }
+}
+
 constexpr int kBoxYK = 12;   // y outputs per thread
 
 __global__ void __launch_bounds__(128) k_box_y(const Sub *subs, int r, const float2 *in, float2 *out) {
@@ -541,6 +559,42 @@ __global__ void __launch_bounds__(128) k_box_y(const Sub *subs, int r, const flo
 #pragma unroll
   for (int k = 0; k < kBoxYK; k++)
     if (y0 + k < H) o[(int64_t)(y0 + k) * W] = mul2(acc[k], make_float2(inv, inv));
+}
+
+// The y box with a compile-time radius: K outputs of one column per thread from a register
+// window (box_chain_t), loads and stores walking running pointers, so that no address
+// arithmetic joins the f32x2 adds in the FMA pipe.
+template <int R, int K>
+__global__ void __launch_bounds__(128, 6) k_box_y_t(const Sub *subs, const float2 *in, float2 *out) {
+  constexpr int L = 2 * R + 1;
+  const Sub S = subs[blockIdx.y];
+  const int rows_per_blk = blockDim.y * K;
+  const int tx_n = (S.W + 31) / 32, ty_n = (S.H + rows_per_blk - 1) / rows_per_blk;
+  const int64_t bid = blockIdx.x;
+  if (bid >= (int64_t)tx_n * ty_n * S.D) return;
+  const int z = (int)(bid / ((int64_t)tx_n * ty_n));
+  const int rem = (int)(bid % ((int64_t)tx_n * ty_n));
+  const int x = (rem % tx_n) * 32 + threadIdx.x;
+  const int y0 = (rem / tx_n) * rows_per_blk + threadIdx.y * K;
+  if (x >= S.W || y0 >= S.H) return;
+  const int H = S.H, W = S.W;
+  const float2 *col = in + S.vox + (int64_t)z * W * H + x;
+  float2 acc[K];
+  if (y0 - R >= 0 && y0 + K + R <= H) {
+    const float2 *q = col + (int64_t)(y0 - R) * W;   // box_chain_t loads its inputs in order
+    box_chain_t<K, L>([&](int) {
+      const float2 v = __ldg(q);
+      q += W;
+      return v;
+    }, acc);
+  } else {
+    box_chain_t<K, L>([&](int i) { return __ldg(col + (int64_t)clampi(y0 - R + i, 0, H - 1) * W); }, acc);
+  }
+  const float inv = 1.0f / (float)L;
+  float2 *o = out + S.vox + (int64_t)z * W * H + (int64_t)y0 * W + x;
+#pragma unroll
+  for (int k = 0; k < K; k++, o += W)
+    if (y0 + k < H) *o = mul2(acc[k], make_float2(inv, inv));
 }
 
 // z pass of the box mean fused with Normalize3DKernel (NormalizeFilter.cu:571-586).
@@ -742,8 +796,14 @@ void launch_normalize(const Sub *d_subs, int nsub, int W, int H, int D, int rxy,
                                     d_subs, rxy, ma, fa)));
   }
   const int by = 4;
-  dim3 gy((unsigned)((int64_t)ceil_div(W, 32) * ceil_div(H, by * kBoxYK) * D), nsub);
-  KLAUNCH("k_box_y", s, (k_box_y<<<gy, dim3(32, by), 0, s>>>(d_subs, rxy, fa, fb)));
+  if (rxy == 20) {   // the workload's radius: compile-time window, 16 outputs a thread
+    constexpr int K = 16;
+    dim3 gy((unsigned)((int64_t)ceil_div(W, 32) * ceil_div(H, by * K) * D), nsub);
+    KLAUNCH("k_box_y", s, (k_box_y_t<20, K><<<gy, dim3(32, by), 0, s>>>(d_subs, fa, fb)));
+  } else {
+    dim3 gy((unsigned)((int64_t)ceil_div(W, 32) * ceil_div(H, by * kBoxYK) * D), nsub);
+    KLAUNCH("k_box_y", s, (k_box_y<<<gy, dim3(32, by), 0, s>>>(d_subs, rxy, fa, fb)));
+  }
   const dim3 gz(ceil_div(plane, 32), ceil_div(D, 4 * kBoxZK), nsub), bz(32, 4);
   switch (rz) {
 #define HDOG_BOXZ_CASE(R)                                                                                   \

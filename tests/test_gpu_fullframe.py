@@ -1,7 +1,7 @@
-"""Full camera-frame checks (2560 x 2160): the sizes where races in the labelling would
-show.  Labels of a 2560x2160x32 substack equal the oracle's; the whole 128-slice stack
-gives byte-identical records run after run, from device or host input, batched or one
-substack at a time."""
+"""Full camera-frame checks (2560 x 2160): the sizes where races in the normalization tiles
+or the labelling would show.  The normalized volume, DoG and labels of a 2560x2160x32
+substack equal the oracle's; the whole 128-slice stack gives byte-identical records run
+after run, from device or host input, batched or one substack at a time."""
 import numpy as np
 import pytest
 import torch
@@ -33,6 +33,14 @@ def test_fullframe_substack_stages_match_oracle(stack):
         mask, _ = ctx.hessian_pd(dog)
         labels = ctx.ccl(mask)
         g = [t.cpu().numpy() for t in (norm, dog, mask, labels)]
+    # normalized volume and DoG of the full frame, bit for bit against the oracle's
+    o_norm = orc.normalize(sub, P["radius_norm_xy"], P["radius_norm_z"], float(P["min_intensity"]))
+    bad = np.count_nonzero(o_norm.view(np.uint32) != g[0].view(np.uint32))
+    assert bad == 0, "normalized volume: %d of %d values differ" % (bad, o_norm.size)
+    o_dog = orc.dog(o_norm, P["sigma_xy_small"], P["sigma_z_small"], P["sigma_xy_large"], P["sigma_z_large"],
+                    P["gamma_n"])
+    bad = np.count_nonzero(o_dog.view(np.uint32) != g[1].view(np.uint32))
+    assert bad == 0, "DoG: %d of %d values differ" % (bad, o_dog.size)
     o_mask, _ = orc.hessian_pd(g[1])
     assert np.array_equal(o_mask, g[2])
     o_labels, n = orc.ccl(g[2])
