@@ -410,6 +410,23 @@ def run_stream(d, total_nuclei, steps, warmup, dev_id=0):
                 r = ctx.run_stack(hn, out=out)
             torch.cuda.synchronize()
             res[name] = ((time.perf_counter() - t) * 1e3 / n, r.copy())
+            if name == "batched":   # where one more call spends its time (host phases, kernels)
+                ctx.timing(True)
+                ctx.timing_read()
+                ctx.run_stack(hn, out=out)
+                ph = ctx.timing_read()
+                ctx.timing(False)
+                phases = {k: round(v[1], 2) for k, v in ph.items() if k.startswith("host_")}
+                phases["kernels"] = round(sum(v[1] for k, v in ph.items() if not k.startswith("host_")), 2)
+    # the pinned host -> device copy rate of the whole stack on this machine
+    dev = torch.empty((d, h, w), dtype=torch.uint16, device="cuda")
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    dev.copy_(host, non_blocking=True)
+    b.record()
+    torch.cuda.synchronize()
+    h2d_gbs = unique * 2 / (a.elapsed_time(b) * 1e-3) / 1e9
+    del dev
     assert res["batched"][1].tobytes() == res["plain"][1].tobytes(), "batched and plain records differ"
     bms, pms = res["batched"][0], res["plain"][0]
     nsub = len(hdog.substack_schedule(d, DEPTH, hdog.depth_margin(p)))
@@ -421,6 +438,7 @@ def run_stream(d, total_nuclei, steps, warmup, dev_id=0):
                        "unique_voxels_per_step": unique, "records_per_step": int(len(res["batched"][1])),
                        "generator_s": round(gen_s, 1)},
             "mode": "end to end: pinned host stack, chunked H2D overlapping the batches, records D2H",
+            "one_call_ms": phases, "pinned_h2d_gbs": round(h2d_gbs, 1),
             "plain": {"value": unique / (pms * 1e-3) / 1e9, "ms_per_step": pms, "mode": "one substack per launch"},
             "batched_over_plain": pms / bms,
             "e2e": {"value": unique / (bms * 1e-3) / 1e9, "unit": "Gvox/s", "h2d_bytes_per_step": unique * 2,
@@ -588,6 +606,15 @@ def main():
     batched.timing_read()
     batched.run_stack(host_np, out=e2e_out)
     e2e_phases = {k: round(v[1], 3) for k, v in batched.timing_read().items()}
+    # six more timed calls, each with its host phases, to show where a slow call spends its time
+    diag = []
+    for _ in range(6):
+        batched.timing_read()
+        tc = time.perf_counter()
+        batched.run_stack(host_np, out=e2e_out)
+        ph = batched.timing_read()
+        diag.append({"call_ms": round((time.perf_counter() - tc) * 1e3, 2),
+                     **{k: round(v[1], 2) for k, v in ph.items() if k.startswith("host_")}})
     batched.timing(False)
     e2e_kernel_ms = round(sum(v for k, v in e2e_phases.items() if not k.startswith("host_")), 3)
     # the pinned host -> device copy rate of this machine, for reading the end-to-end figure
@@ -644,7 +671,8 @@ def main():
                 "call_ms": {"median": round(statistics.median(call_ms), 2), "min": round(min(call_ms), 2),
                             "max": round(max(call_ms), 2)},
                 "one_call": {"kernel_ms": e2e_kernel_ms,
-                             "host_ms": {k: v for k, v in e2e_phases.items() if k.startswith("host_")}}},
+                             "host_ms": {k: v for k, v in e2e_phases.items() if k.startswith("host_")}},
+                "phased_calls": diag},
         "gpu_launches": int(launches),
         "kernel_ms_per_step": {k: round(v[1] / args.steps, 4) for k, v in sorted(ktimes.items(), key=lambda kv: -kv[1][1])},
         "host_ms_per_step": host_phases,
