@@ -15,6 +15,7 @@ N > 1 runs as one process per GPU under torch.distributed.run, each rank on its 
 copy of the stack (replicas, no collective on the data path; weak scaling).
 """
 import argparse
+import gc
 import json
 import os
 import statistics
@@ -108,6 +109,19 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+class no_gc:
+    """The interpreter's cyclic garbage collector is off inside a timed region (as timeit
+    does): a full collection of this process's objects takes 50-90 ms and would be charged
+    to whichever call it interrupts."""
+
+    def __enter__(self):
+        gc.collect()
+        gc.disable()
+
+    def __exit__(self, *a):
+        gc.enable()
+
+
 def make_stack():
     from hdog import synth
     s = synth.camera_spec(depth=L)
@@ -142,11 +156,12 @@ def time_steps(ctx, stack, steps, warmup, stream, dist=None):
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     recs = None
-    e0.record(stream)
-    for _ in range(steps):
-        recs = ctx.run_stack(stack, stream=stream, out=out)
-    e1.record(stream)
-    torch.cuda.synchronize()
+    with no_gc():
+        e0.record(stream)
+        for _ in range(steps):
+            recs = ctx.run_stack(stack, stream=stream, out=out)
+        e1.record(stream)
+        torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
     if dist:
         dist.barrier()
@@ -308,11 +323,12 @@ def run_uneven(stacks, unique, steps, warmup, max_sub, dev_id=0):
     torch.cuda.synchronize()
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     psteps = max(1, min(steps, 2))
-    a.record()
-    for _ in range(psteps):
-        prec = run_plain()
-    b.record()
-    torch.cuda.synchronize()
+    with no_gc():
+        a.record()
+        for _ in range(psteps):
+            prec = run_plain()
+        b.record()
+        torch.cuda.synchronize()
     pms = a.elapsed_time(b) / psteps
     for c in plain_ctx.values():
         c.close()
@@ -326,11 +342,12 @@ def run_uneven(stacks, unique, steps, warmup, max_sub, dev_id=0):
     for _ in range(max(1, warmup)):
         grec, counts = graph.run()
     torch.cuda.synchronize()
-    a.record()
-    for _ in range(steps):
-        grec, counts = graph.run()
-    b.record()
-    torch.cuda.synchronize()
+    with no_gc():
+        a.record()
+        for _ in range(steps):
+            grec, counts = graph.run()
+        b.record()
+        torch.cuda.synchronize()
     gms = a.elapsed_time(b) / steps
     tuning = {"%dx%d" % k: c.tuning() for k, c in zip(shapes, ctxs)}
     graph.close()
@@ -405,11 +422,13 @@ def run_stream(d, total_nuclei, steps, warmup, dev_id=0):
                 if len(r) > len(out):
                     out = np.empty(len(r), hdog.DT_LOCAL)
             torch.cuda.synchronize()
-            t = time.perf_counter()
-            for _ in range(n):
-                r = ctx.run_stack(hn, out=out)
-            torch.cuda.synchronize()
-            res[name] = ((time.perf_counter() - t) * 1e3 / n, r.copy())
+            with no_gc():
+                t = time.perf_counter()
+                for _ in range(n):
+                    r = ctx.run_stack(hn, out=out)
+                torch.cuda.synchronize()
+                elapsed = time.perf_counter() - t
+            res[name] = (elapsed * 1e3 / n, r.copy())
             if name == "batched":   # where one more call spends its time (host phases, kernels)
                 ctx.timing(True)
                 ctx.timing_read()
@@ -590,14 +609,15 @@ def main():
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
-    t0 = time.perf_counter()
     call_ms = []
-    for _ in range(args.steps):
-        tc = time.perf_counter()
-        recs_e2e = batched.run_stack(host_np, out=e2e_out)   # returns after its records are in e2e_out
-        call_ms.append((time.perf_counter() - tc) * 1e3)
-    torch.cuda.synchronize()
-    e2e_ms = (time.perf_counter() - t0) * 1e3
+    with no_gc():
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            tc = time.perf_counter()
+            recs_e2e = batched.run_stack(host_np, out=e2e_out)   # returns after its records are in e2e_out
+            call_ms.append((time.perf_counter() - tc) * 1e3)
+        torch.cuda.synchronize()
+        e2e_ms = (time.perf_counter() - t0) * 1e3
     e2e_ms = max_over_ranks(e2e_ms, dist) / args.steps
     assert recs_e2e.tobytes() == recs.tobytes(), "host-input run differs from device-input run"
     # where an end-to-end call spends its time (one more call, outside the timed loop, with
@@ -669,7 +689,7 @@ def main():
                 "h2d_bytes_per_step": unique * 2, "d2h_bytes_per_step": n_records * 28,
                 "ms_per_step": e2e_ms, "pinned_h2d_gbs": round(h2d_gbs, 1),
                 "call_ms": {"median": round(statistics.median(call_ms), 2), "min": round(min(call_ms), 2),
-                            "max": round(max(call_ms), 2)},
+                            "max": round(max(call_ms), 2), "all": [round(x, 2) for x in call_ms]},
                 "one_call": {"kernel_ms": e2e_kernel_ms,
                              "host_ms": {k: v for k, v in e2e_phases.items() if k.startswith("host_")}},
                 "phased_calls": diag},
