@@ -5,12 +5,14 @@
 // processSubstack :134-257, main :260-319) and src/3D/utils.h (loadParamFile :95-157,
 // loadImage :160-173, saveFeatureVector :204-250).
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cerrno>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <fstream>
+#include <future>
 #include <memory>
 #include <mutex>
 #include <sstream>
@@ -1597,12 +1599,63 @@ static int load_slice(const std::string &path, uint16_t *dst, size_t n) {
   return HDOG_OK;
 }
 
+// Slices [0, last) of one stack read into `dst` by several threads: the slice files are
+// independent, and one thread's fread of 11 MB slices moves a few GB/s, well below what the
+// page cache or a disk array gives several readers.  Every slice is attempted; the error
+// reported is that of the first failing slice, as a reader going in order would report it.
+struct SliceRead {
+  int rc = HDOG_OK;
+  std::string msg;
+  double seconds = 0.0;
+};
+
+static SliceRead read_slices(const std::vector<std::string> &src, int last, uint16_t *dst, size_t plane) {
+  SliceRead r;
+  const auto t0 = std::chrono::steady_clock::now();
+  std::vector<std::string> err((size_t)std::max(0, last));
+  std::vector<char> bad((size_t)std::max(0, last), 0);
+  std::atomic<int> next{0};
+  auto work = [&]() {
+    for (int z; (z = next.fetch_add(1)) < last;)
+      if (load_slice(src[(size_t)z], dst + (size_t)z * plane, plane) != HDOG_OK) {
+        err[(size_t)z] = g_last_error;   // this thread's message
+        bad[(size_t)z] = 1;
+      }
+  };
+  const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
+  const int nt = std::max(1, std::min({last, hw, 16}));
+  std::vector<std::thread> th;
+  for (int i = 1; i < nt; i++) {
+    try {
+      th.emplace_back(work);
+    } catch (...) {
+      break;   // the threads that started and this one share the slices
+    }
+  }
+  work();
+  for (std::thread &t : th) t.join();
+  for (int z = 0; z < last; z++)
+    if (bad[(size_t)z]) {
+      r.rc = HDOG_ERR_IO;
+      r.msg = err[(size_t)z];
+      break;
+    }
+  r.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  return r;
+}
+
 // Each stack's records go to "<dst_path>.part" and are renamed to dst_path once the stack is
 // complete, so an interrupted run leaves no truncated result (the reference removes dst_path
 // and appends substack by substack, HDoG3D_main.cpp:295-300, utils.h:216,246; the finished
 // file is the same).  With the top-level key "skip_existing" (not a reference key; default
 // false) a stack whose dst_path exists is skipped, which resumes an interrupted run.  With
 // verbose, a JSON metrics line closes the run.
+//
+// The slices of the next stack are read into a second page-locked buffer while the current
+// stack runs on the GPU (the reference reads each substack's slices between its GPU passes,
+// HDoG3D_main.cpp:134-170).  The order of results, files and errors is the serial one: a
+// stack whose slices fail to read is reported when its turn comes, after the stacks before
+// it were written, and whether a stack is skipped is decided when its turn comes.
 extern "C" int hdog_run_param_file(const char *param_path, int verbose) {
   const auto t_start = std::chrono::steady_clock::now();
   hdog_params p;
@@ -1619,50 +1672,91 @@ extern "C" int hdog_run_param_file(const char *param_path, int verbose) {
   std::vector<int> z0s;
   TRY(schedule(max_len, p.depth, margin, z0s));
   int max_sub = std::max(1, std::min((int)z0s.size(), 8));
+  // the slices some substack of stack i reads (0 when it has no substack), and its substacks
+  std::vector<int> last_slice(stacks.size(), 0), n_subs(stacks.size(), 0);
+  for (size_t i = 0; i < stacks.size(); i++) {
+    const int length = (int)stacks[i].src.size();
+    TRY(schedule(length, p.depth, margin, z0s));
+    n_subs[i] = (int)z0s.size();
+    if (!z0s.empty()) last_slice[i] = std::min(length, z0s.back() + p.depth);
+  }
   hdog_ctx *ctx = nullptr;
   TRY(hdog_ctx_create(&p, max_sub, &ctx));
   const size_t plane = (size_t)p.width * p.height;
-  uint16_t *h_stack = nullptr;
-  size_t h_cap = 0;
-  RecordBuf &recs = ctx->last;
+  auto skipped = [&](size_t i) {
+    if (!skip_existing) return false;
+    if (FILE *e = fopen(stacks[i].dst.c_str(), "rb")) {
+      fclose(e);
+      return true;
+    }
+    return false;
+  };
+  // two page-locked stack buffers: one read from disk while the other runs
+  uint16_t *buf[2] = {nullptr, nullptr};
+  size_t cap[2] = {0, 0};
+  std::future<SliceRead> pending;
+  size_t pending_stack = stacks.size();
+  int pending_slot = 0;
   int rc = HDOG_OK;
+  // starts reading the first stack from `from` on that will not be skipped into buffer `slot`
+  auto prefetch = [&](size_t from, int slot) -> int {
+    pending_stack = stacks.size();
+    size_t j = from;
+    while (j < stacks.size() && (last_slice[j] == 0 || skipped(j))) j++;
+    if (j == stacks.size()) return HDOG_OK;
+    const size_t need = (size_t)last_slice[j] * plane;
+    if (need > cap[slot]) {
+      if (buf[slot]) cudaFreeHost(buf[slot]);
+      buf[slot] = nullptr;
+      cap[slot] = 0;
+      if (cudaMallocHost(&buf[slot], need * sizeof(uint16_t)) != cudaSuccess)
+        return fail(HDOG_ERR_NOMEM, "pinned host buffer for the stack failed");
+      cap[slot] = need;
+    }
+    try {
+      pending = std::async(std::launch::async, read_slices, std::cref(stacks[j].src), last_slice[j], buf[slot], plane);
+    } catch (...) {   // no thread to spare: the read runs when its result is asked for
+      pending = std::async(std::launch::deferred, read_slices, std::cref(stacks[j].src), last_slice[j], buf[slot], plane);
+    }
+    pending_stack = j;
+    pending_slot = slot;
+    return HDOG_OK;
+  };
+  RecordBuf &recs = ctx->last;
   int64_t n_done = 0, n_skipped = 0, slices = 0, records = 0;
-  double io_s = 0.0;
+  double read_s = 0.0, wait_s = 0.0;
+  rc = prefetch(0, 0);
   for (size_t i = 0; i < stacks.size() && rc == HDOG_OK; i++) {
     const StackSpec &sp = stacks[i];
-    if (skip_existing) {
-      if (FILE *e = fopen(sp.dst.c_str(), "rb")) {
-        fclose(e);
-        n_skipped++;
-        continue;
-      }
+    if (skipped(i)) {
+      n_skipped++;
+      continue;
     }
     remove(sp.dst.c_str());
     const int length = (int)sp.src.size();
-    TRY(schedule(length, p.depth, margin, z0s));
-    if (z0s.empty()) continue;
+    if (last_slice[i] == 0) continue;
     nvtxRangePushA("hdog stack");
-    const size_t need = (size_t)length * plane;
-    if (need > h_cap) {
-      if (h_stack) cudaFreeHost(h_stack);
-      h_stack = nullptr;
-      if (cudaMallocHost(&h_stack, need * sizeof(uint16_t)) != cudaSuccess) {
-        rc = fail(HDOG_ERR_NOMEM, "pinned host buffer for the stack failed");
-        nvtxRangePop();
-        break;
-      }
-      h_cap = need;
+    if (pending_stack != i) {
+      // the stack ahead was skipped when its read was planned but not now: read it here
+      if (pending.valid()) pending.wait();
+      if ((rc = prefetch(i, pending_slot)) != HDOG_OK) { nvtxRangePop(); break; }
     }
-    // only the slices some substack reads
-    const auto t_io = std::chrono::steady_clock::now();
-    const int last = std::min(length, z0s.back() + p.depth);
-    for (int z = 0; z < last && rc == HDOG_OK; z++) rc = load_slice(sp.src[z], h_stack + (size_t)z * plane, plane);
-    io_s += std::chrono::duration<double>(std::chrono::steady_clock::now() - t_io).count();
-    if (rc != HDOG_OK) { nvtxRangePop(); break; }
+    const auto t_wait = std::chrono::steady_clock::now();
+    const SliceRead got = pending.get();
+    wait_s += std::chrono::duration<double>(std::chrono::steady_clock::now() - t_wait).count();
+    read_s += got.seconds;
+    const int slot = pending_slot;
+    if (got.rc != HDOG_OK) {
+      rc = fail(got.rc, got.msg);
+      nvtxRangePop();
+      break;
+    }
+    // the next stack's slices land in the other buffer while this one runs
+    if ((rc = prefetch(i + 1, 1 - slot)) != HDOG_OK) { nvtxRangePop(); break; }
     recs.clear();
     {
       std::lock_guard<std::mutex> lock(ctx->mu);
-      rc = run_stack_locked(ctx, h_stack, 0, last, recs, nullptr);
+      rc = run_stack_locked(ctx, buf[slot], 0, last_slice[i], recs, nullptr);
     }
     nvtxRangePop();
     if (rc != HDOG_OK) break;
@@ -1684,18 +1778,20 @@ extern "C" int hdog_run_param_file(const char *param_path, int verbose) {
     n_done++;
     slices += length;
     records += n;
-    if (verbose) printf("stack %zu: %d slices, %zu substacks, saved count:%lld\n", i, length, z0s.size(), (long long)n);
+    if (verbose) printf("stack %zu: %d slices, %d substacks, saved count:%lld\n", i, length, n_subs[i], (long long)n);
   }
-  if (h_stack) cudaFreeHost(h_stack);
+  if (pending.valid()) pending.wait();   // a read still filling a buffer
+  for (uint16_t *b : buf)
+    if (b) cudaFreeHost(b);
   hdog_ctx_destroy(ctx);
   if (verbose) {
     const double t = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
     const double vox = (double)slices * (double)plane;
     printf("{\"hdog_main\": {\"status\": %d, \"stacks_done\": %lld, \"stacks_skipped\": %lld, \"slices\": %lld, "
            "\"voxels\": %.0f, \"records\": %lld, \"seconds\": %.3f, \"slice_read_seconds\": %.3f, "
-           "\"gvox_per_s\": %.3f}}\n",
-           rc, (long long)n_done, (long long)n_skipped, (long long)slices, vox, (long long)records, t, io_s,
-           t > 0 ? vox / t / 1e9 : 0.0);
+           "\"slice_read_wait_seconds\": %.3f, \"gvox_per_s\": %.3f}}\n",
+           rc, (long long)n_done, (long long)n_skipped, (long long)slices, vox, (long long)records, t, read_s,
+           wait_s, t > 0 ? vox / t / 1e9 : 0.0);
     fflush(stdout);
   }
   return rc;

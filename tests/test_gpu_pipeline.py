@@ -152,6 +152,50 @@ def test_hdog_main_resume_metrics_and_a_short_slice(tmp_path):
     assert np.fromfile(stacks[1][0], dtype=hdog.DT_LOCAL).tobytes() == first[1].tobytes()
 
 
+def test_hdog_main_reads_ahead_in_the_serial_order(tmp_path):
+    """hdog_main reads the next stack's slices while the current one runs.  Four stacks: the
+    second is skipped (its result exists, skip_existing), the fourth has a missing slice
+    file.  The results and the error are those of a run that reads stack after stack: the
+    first and third stacks are written and equal the oracle, the skipped result is left as
+    it was, the fourth stack has no result and the run exits with status 2."""
+    import json
+    W, H, L, D = 128, 96, 40, 32
+    p = params(W, H, D, margins=3)
+    (tmp_path / "out").mkdir()
+    vols, stacks = [], []
+    for k in range(4):
+        vol = volume(W, H, L, n_nuclei=60, seed=90 + k)
+        d = tmp_path / ("src%d" % k)
+        d.mkdir()
+        src = []
+        for z in range(L):
+            f = d / ("%06d.bin" % z)
+            vol[z].tofile(f)
+            src.append(str(f))
+        vols.append(vol)
+        stacks.append((str(tmp_path / "out" / ("stack%d.bin" % k)), src))
+    os.remove(stacks[3][1][21])
+    with open(stacks[1][0], "wb") as f:
+        f.write(b"kept")
+    pf = tmp_path / "param.json"
+    hdog.write_param_file(str(pf), p, stacks)
+    d = json.load(open(pf))
+    d["verbose"] = True
+    d["skip_existing"] = True
+    pf.write_text(json.dumps(d))
+    r = subprocess.run([hdog.MAIN_PATH, str(pf)], stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True)
+    assert r.returncode == 2, (r.returncode, r.stderr)
+    assert "000021.bin" in r.stderr
+    metrics = json.loads([l for l in r.stdout.splitlines() if l.startswith('{"hdog_main"')][-1])["hdog_main"]
+    assert metrics["stacks_done"] == 2 and metrics["stacks_skipped"] == 1 and metrics["status"] == hdog.HDOG_ERR_IO
+    for k in (0, 2):
+        got = np.fromfile(stacks[k][0], dtype=hdog.DT_LOCAL)
+        assert_records_match(got, orc.stack(orc.params_from(p), vols[k]), "hdog_main stack %d" % k)
+    assert open(stacks[1][0], "rb").read() == b"kept"
+    assert not os.path.exists(stacks[3][0])
+    assert not list((tmp_path / "out").glob("*.part"))
+
+
 def test_erosion_opt_in_pipeline():
     W, H, D = 128, 128, 16
     vol = volume(W, H, D, n_nuclei=40, seed=5)
