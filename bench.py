@@ -50,6 +50,11 @@ KERNEL_BYTES_PER_VOXEL = {
     "k_accumulate": 1,
 }
 E2E_ALG_BYTES_PER_VOXEL = 6      # 2 B uint16 in + 4 B labels out per processed voxel
+# FP32 lane operations (an FMA or an add counts one) the DoG sweep spends per output voxel
+# with the workload's tap radii (xy 4 / 6, z 3 / 5): the x pass of both scales (9 + 13 taps)
+# over the 16-row tile and its 12 halo rows, the y pass (9 + 13), the z pass (7 + 11), the
+# difference and the scale.
+DOG_FP32_LANE_OPS_PER_VOXEL = (9 + 13) * (16 + 12) / 16 + (9 + 13) + (7 + 11) + 2
 
 
 def peaks():
@@ -675,6 +680,19 @@ def main():
         if kname in t.get("bytes_per_voxel", {}):
             traffic = t["bytes_per_voxel"][kname] * per_launch_voxels
     e2e_alg_gbs = E2E_ALG_BYTES_PER_VOXEL * processed / (ms_step * 1e-3) / 1e9
+    # the DoG sweep against the FP32 pipe: its FMA chains are fixed by the reference's
+    # rounding, so the kernel is bound by FP32 issue, not by its 8 bytes per voxel
+    fp32 = None
+    clk = clocks.summary()
+    if "k_dog_sweep" in ktimes and clk:
+        cnt, tot = ktimes["k_dog_sweep"]
+        ops = DOG_FP32_LANE_OPS_PER_VOXEL * processed
+        sms = torch.cuda.get_device_properties(dev).multi_processor_count
+        peak_ops = 128 * sms * clk["sm_mhz"] * 1e6
+        fp32 = {"kernel": "k_dog_sweep", "lane_ops_per_voxel": DOG_FP32_LANE_OPS_PER_VOXEL,
+                "achieved_tops": ops / (tot / cnt * 1e-3) / 1e12, "peak_tops": peak_ops / 1e12,
+                "frac": ops / (tot / cnt * 1e-3) / peak_ops,
+                "peak_source": "nominal: 128 FP32 lanes per SM x %d SMs x %.0f MHz sampled" % (sms, clk["sm_mhz"])}
 
     line = {
         "metric": METRIC, "value": value, "unit": "Gvox/s", "n_gpus": ws, "steps": args.steps,
@@ -702,8 +720,9 @@ def main():
         "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                      "alg_bytes_per_launch": alg, "avg_launch_ms": avg_ms,
-                     "end_to_end_alg_gbs": e2e_alg_gbs, "end_to_end_frac": e2e_alg_gbs / peak},
-        "clocks": clocks.summary(),
+                     "end_to_end_alg_gbs": e2e_alg_gbs, "end_to_end_frac": e2e_alg_gbs / peak,
+                     "fp32_pipe": fp32},
+        "clocks": clk,
     }
     if not args.no_uneven:
         # the uneven-stack subset: the batched graph form against the plain loop
