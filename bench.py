@@ -292,18 +292,29 @@ UNEVEN = ("40 uneven stacks: z ~ U{64..512}, xy 2560x2160 / 1280x2160 / 2560x108
           "HDoG depth 32, sigma_dog (2,1.5,3.2,2.4), radius_norm (20,5)")
 
 
-def uneven_stacks(n, seed, dev):
+# The same kind of mix with small frames (a 256 x 256 tile and its two half-size edge tiles,
+# nuclei at the 256 x 256 x 64 case's density): each substack is a few milliseconds of work
+# or less, so the plain loop's per-substack launches and host synchronisation show.
+SMALL_SHAPES = [(256, 256), (128, 256), (256, 128)]
+SMALL_N = 40
+SMALL_DENSITY = 400.0 / (256 * 256 * 64)
+SMALL = ("40 uneven small stacks: z ~ U{64..512}, xy 256x256 / 128x256 / 256x128 with p = 1/3 each, nuclei "
+         "at the 256x256x64 case's density (400 per 4.2 M voxels); HDoG depth 32, sigma_dog (2,1.5,3.2,2.4), "
+         "radius_norm (20,5), margins 10")
+
+
+def uneven_stacks(n, seed, dev, shapes=UNEVEN_SHAPES, density=2e-5):
     """n seeded stacks of the uneven mix on the device: z ~ U{64..512}, a frame shape each
-    with p = 1/3, nuclei at 2e-5 per voxel.  -> (list of (shape, tensor), unique voxels, s)."""
+    with p = 1/3, nuclei at `density` per voxel.  -> (list of (shape, tensor), unique voxels, s)."""
     import torch
     from hdog import synth
     rng = np.random.default_rng(seed)
     stacks, unique = [], 0
     t0 = time.time()
     for i in range(n):
-        w, h = UNEVEN_SHAPES[int(rng.integers(3))]
+        w, h = shapes[int(rng.integers(3))]
         length = int(rng.integers(64, 513))
-        nn = max(1, int(round(2e-5 * w * h * length)))
+        nn = max(1, int(round(density * w * h * length)))
         vol = synth.volume(synth.spec(w, h, length, nn, synth.SEED_BASE + 1000 + i))
         stacks.append(((w, h), torch.from_numpy(vol).to(dev)))
         unique += w * h * length
@@ -311,7 +322,7 @@ def uneven_stacks(n, seed, dev):
     return stacks, unique, time.time() - t0
 
 
-def run_uneven(stacks, unique, steps, warmup, max_sub, dev_id=0):
+def run_uneven(stacks, unique, steps, warmup, max_sub, dev_id=0, params=PARAMS):
     """The batched graph form (one captured CUDA graph over all stacks, one context per frame
     shape, autotuned launch shapes) against the plain loop (one substack per launch sequence,
     stack after stack, as the reference runs them); records compared byte for byte."""
@@ -320,7 +331,7 @@ def run_uneven(stacks, unique, steps, warmup, max_sub, dev_id=0):
     shapes = sorted({s for s, _ in stacks})
     tensors = [t for _, t in stacks]
     # plain: one context of one substack per frame shape
-    plain_ctx = {k: hdog.Context(hdog.make_params(dev_id=dev_id, **dict(PARAMS, width=k[0], height=k[1])), 1)
+    plain_ctx = {k: hdog.Context(hdog.make_params(dev_id=dev_id, **dict(params, width=k[0], height=k[1])), 1)
                  for k in shapes}
     run_plain = lambda: [plain_ctx[s].run_stack(t) for s, t in stacks]
     for _ in range(1):
@@ -340,7 +351,7 @@ def run_uneven(stacks, unique, steps, warmup, max_sub, dev_id=0):
     prec = np.concatenate(prec)
     # graph form
     t0 = time.time()
-    ctxs = [hdog.Context(hdog.make_params(dev_id=dev_id, **dict(PARAMS, width=k[0], height=k[1])), max_sub)
+    ctxs = [hdog.Context(hdog.make_params(dev_id=dev_id, **dict(params, width=k[0], height=k[1])), max_sub)
             for k in shapes]
     graph = hdog.Graph(ctxs, tensors)
     create_s = time.time() - t0
@@ -736,6 +747,16 @@ def main():
         u["plain"]["value"] = u["plain"]["value"] * ws
         line["uneven"] = u
         del ustacks
+        # the same forms on small frames, where per-substack launch and host costs matter
+        sstacks, sunique, sgen = uneven_stacks(SMALL_N, synth_seed(5), dev, SMALL_SHAPES, SMALL_DENSITY)
+        small_params = dict(PARAMS, left_margin=10, right_margin=10, top_margin=10, bottom_margin=10)
+        su = run_uneven(sstacks, sunique, max(3, min(args.steps, 5)), 2, 16, local, small_params)
+        su["config"] = {"workload": SMALL, "unique_voxels_per_step": sunique,
+                        "frames": sorted({"%dx%d" % sh for sh, _ in sstacks}), "generator_s": round(sgen, 1)}
+        su["value"] = su["value"] * ws
+        su["plain"]["value"] = su["plain"]["value"] * ws
+        line["uneven_small"] = su
+        del sstacks
     if not args.no_stream:
         # the dense streaming stack at a quarter of its depth (384 slices, the same density of
         # nuclei and clusters), end to end from host memory, batched against plain
