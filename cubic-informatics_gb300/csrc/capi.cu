@@ -1644,6 +1644,31 @@ static SliceRead read_slices(const std::vector<std::string> &src, int last, uint
   return r;
 }
 
+// One stack's records written to "<dst>.part" and renamed to dst once complete.
+static SliceRead write_records(const std::string &dst, const hdog_record *rec, int64_t n) {
+  SliceRead w;
+  const std::string part = dst + ".part";
+  FILE *f = fopen(part.c_str(), "wb");
+  if (!f) {
+    w.rc = HDOG_ERR_IO;
+    w.msg = "Unable to open " + part;
+    return w;
+  }
+  if (n > 0 && fwrite(rec, sizeof(hdog_record), (size_t)n, f) != (size_t)n) {
+    fclose(f);
+    remove(part.c_str());
+    w.rc = HDOG_ERR_IO;
+    w.msg = "Unable to write " + part;
+    return w;
+  }
+  if (fclose(f) != 0 || rename(part.c_str(), dst.c_str()) != 0) {
+    remove(part.c_str());
+    w.rc = HDOG_ERR_IO;
+    w.msg = "Unable to write " + dst;
+  }
+  return w;
+}
+
 // Each stack's records go to "<dst_path>.part" and are renamed to dst_path once the stack is
 // complete, so an interrupted run leaves no truncated result (the reference removes dst_path
 // and appends substack by substack, HDoG3D_main.cpp:295-300, utils.h:216,246; the finished
@@ -1651,11 +1676,14 @@ static SliceRead read_slices(const std::vector<std::string> &src, int last, uint
 // false) a stack whose dst_path exists is skipped, which resumes an interrupted run.  With
 // verbose, a JSON metrics line closes the run.
 //
-// The slices of the next stack are read into a second page-locked buffer while the current
-// stack runs on the GPU (the reference reads each substack's slices between its GPU passes,
-// HDoG3D_main.cpp:134-170).  The order of results, files and errors is the serial one: a
-// stack whose slices fail to read is reported when its turn comes, after the stacks before
-// it were written, and whether a stack is skipped is decided when its turn comes.
+// Host work overlaps the GPU (the reference reads each substack's slices and writes its
+// records between its GPU passes, HDoG3D_main.cpp:134-170,246-255): the slices of the next
+// stack are read into a second page-locked buffer, and the previous stack's records are
+// written from a second record buffer, while the current stack runs.  What a run leaves
+// behind is that of a run going stack after stack: a stack's result file is removed only
+// after the stack before it was written, whether a stack is skipped is decided after that
+// write, and a failing stack (its slices, its GPU work, its write) ends the run after the
+// stacks before it were written, with its own error.
 extern "C" int hdog_run_param_file(const char *param_path, int verbose) {
   const auto t_start = std::chrono::steady_clock::now();
   hdog_params p;
@@ -1682,6 +1710,7 @@ extern "C" int hdog_run_param_file(const char *param_path, int verbose) {
   }
   hdog_ctx *ctx = nullptr;
   TRY(hdog_ctx_create(&p, max_sub, &ctx));
+  const int dev = ctx->dev;
   const size_t plane = (size_t)p.width * p.height;
   auto skipped = [&](size_t i) {
     if (!skip_existing) return false;
@@ -1691,98 +1720,127 @@ extern "C" int hdog_run_param_file(const char *param_path, int verbose) {
     }
     return false;
   };
-  // two page-locked stack buffers: one read from disk while the other runs
+  // two page-locked stack buffers (one read from disk while the other runs) and two record
+  // buffers (one written to disk while the other fills)
   uint16_t *buf[2] = {nullptr, nullptr};
   size_t cap[2] = {0, 0};
-  std::future<SliceRead> pending;
-  size_t pending_stack = stacks.size();
+  RecordBuf rbuf[2];
+  int rb = 0;
+  std::future<SliceRead> pending, writing;
+  size_t pending_stack = stacks.size(), writing_stack = 0;
   int pending_slot = 0;
-  int rc = HDOG_OK;
-  // starts reading the first stack from `from` on that will not be skipped into buffer `slot`
-  auto prefetch = [&](size_t from, int slot) -> int {
+  int64_t n_done = 0, n_skipped = 0, slices = 0, records = 0;
+  double read_s = 0.0, wait_s = 0.0;
+  auto launch = [](auto &&fn) -> std::future<SliceRead> {
+    try {
+      return std::async(std::launch::async, fn);
+    } catch (...) {   // no thread to spare: the task runs when its result is asked for
+      return std::async(std::launch::deferred, fn);
+    }
+  };
+  // starts reading the first stack from `from` on that will not be skipped into buffer
+  // `slot` (allocated there first if too small)
+  auto prefetch = [&](size_t from, int slot) {
     pending_stack = stacks.size();
     size_t j = from;
     while (j < stacks.size() && (last_slice[j] == 0 || skipped(j))) j++;
-    if (j == stacks.size()) return HDOG_OK;
+    if (j == stacks.size()) return;
     const size_t need = (size_t)last_slice[j] * plane;
-    if (need > cap[slot]) {
-      if (buf[slot]) cudaFreeHost(buf[slot]);
-      buf[slot] = nullptr;
-      cap[slot] = 0;
-      if (cudaMallocHost(&buf[slot], need * sizeof(uint16_t)) != cudaSuccess)
-        return fail(HDOG_ERR_NOMEM, "pinned host buffer for the stack failed");
-      cap[slot] = need;
-    }
-    try {
-      pending = std::async(std::launch::async, read_slices, std::cref(stacks[j].src), last_slice[j], buf[slot], plane);
-    } catch (...) {   // no thread to spare: the read runs when its result is asked for
-      pending = std::async(std::launch::deferred, read_slices, std::cref(stacks[j].src), last_slice[j], buf[slot], plane);
-    }
+    const std::vector<std::string> *src = &stacks[j].src;
+    const int last = last_slice[j];
+    uint16_t **b = &buf[slot];
+    size_t *c = &cap[slot];
+    pending = launch([=]() {
+      if (need > *c) {
+        cudaSetDevice(dev);
+        if (*b) cudaFreeHost(*b);
+        *b = nullptr;
+        *c = 0;
+        if (cudaMallocHost(b, need * sizeof(uint16_t)) != cudaSuccess) {
+          SliceRead r;
+          r.rc = HDOG_ERR_NOMEM;
+          r.msg = "pinned host buffer for the stack failed";
+          return r;
+        }
+        *c = need;
+      }
+      return read_slices(*src, last, *b, plane);
+    });
     pending_stack = j;
     pending_slot = slot;
+  };
+  // waits for the stack being written and counts it
+  auto finish_write = [&]() -> int {
+    if (!writing.valid()) return HDOG_OK;
+    const SliceRead w = writing.get();
+    if (w.rc != HDOG_OK) return fail(w.rc, w.msg);
+    const size_t k = writing_stack;
+    const int64_t n = (int64_t)rbuf[rb ^ 1].n;
+    n_done++;
+    slices += (int64_t)stacks[k].src.size();
+    records += n;
+    if (verbose)
+      printf("stack %zu: %zu slices, %d substacks, saved count:%lld\n", k, stacks[k].src.size(), n_subs[k],
+             (long long)n);
     return HDOG_OK;
   };
-  RecordBuf &recs = ctx->last;
-  int64_t n_done = 0, n_skipped = 0, slices = 0, records = 0;
-  double read_s = 0.0, wait_s = 0.0;
-  rc = prefetch(0, 0);
+  int rc = HDOG_OK;
+  prefetch(0, 0);
   for (size_t i = 0; i < stacks.size() && rc == HDOG_OK; i++) {
     const StackSpec &sp = stacks[i];
-    if (skipped(i)) {
+    if (skipped(i)) {   // a result that exists now still exists after the pending write
       n_skipped++;
       continue;
     }
-    remove(sp.dst.c_str());
-    const int length = (int)sp.src.size();
-    if (last_slice[i] == 0) continue;
+    if (last_slice[i] == 0) {
+      if ((rc = finish_write()) != HDOG_OK) break;
+      remove(sp.dst.c_str());
+      continue;
+    }
     nvtxRangePushA("hdog stack");
     if (pending_stack != i) {
       // the stack ahead was skipped when its read was planned but not now: read it here
       if (pending.valid()) pending.wait();
-      if ((rc = prefetch(i, pending_slot)) != HDOG_OK) { nvtxRangePop(); break; }
+      prefetch(i, pending_slot);
     }
     const auto t_wait = std::chrono::steady_clock::now();
     const SliceRead got = pending.get();
     wait_s += std::chrono::duration<double>(std::chrono::steady_clock::now() - t_wait).count();
     read_s += got.seconds;
     const int slot = pending_slot;
-    if (got.rc != HDOG_OK) {
-      rc = fail(got.rc, got.msg);
-      nvtxRangePop();
-      break;
-    }
-    // the next stack's slices land in the other buffer while this one runs
-    if ((rc = prefetch(i + 1, 1 - slot)) != HDOG_OK) { nvtxRangePop(); break; }
-    recs.clear();
-    {
+    int rc_stack = got.rc;
+    if (rc_stack == HDOG_OK) {
+      prefetch(i + 1, 1 - slot);   // the next stack's slices land while this one runs
+      rbuf[rb].clear();
       std::lock_guard<std::mutex> lock(ctx->mu);
-      rc = run_stack_locked(ctx, buf[slot], 0, last_slice[i], recs, nullptr);
+      rc_stack = run_stack_locked(ctx, buf[slot], 0, last_slice[i], rbuf[rb], nullptr);
     }
+    const std::string err_stack = rc_stack != HDOG_OK ? (got.rc != HDOG_OK ? got.msg : g_last_error) : "";
     nvtxRangePop();
-    if (rc != HDOG_OK) break;
-    const int64_t n = (int64_t)recs.n;
-    const std::string part = sp.dst + ".part";
-    FILE *f = fopen(part.c_str(), "wb");
-    if (!f) { rc = fail(HDOG_ERR_IO, "Unable to open " + part); break; }
-    if (n > 0 && fwrite(recs.p, sizeof(hdog_record), (size_t)n, f) != (size_t)n) {
-      fclose(f);
-      remove(part.c_str());
-      rc = fail(HDOG_ERR_IO, "Unable to write " + part);
+    // the stack before this one is complete before anything of this one shows
+    if ((rc = finish_write()) != HDOG_OK) break;
+    if (skipped(i)) {   // the stack before wrote this stack's result path
+      n_skipped++;
+      continue;
+    }
+    remove(sp.dst.c_str());
+    if (rc_stack != HDOG_OK) {
+      rc = fail(rc_stack, err_stack);
       break;
     }
-    if (fclose(f) != 0 || rename(part.c_str(), sp.dst.c_str()) != 0) {
-      remove(part.c_str());
-      rc = fail(HDOG_ERR_IO, "Unable to write " + sp.dst);
-      break;
-    }
-    n_done++;
-    slices += length;
-    records += n;
-    if (verbose) printf("stack %zu: %d slices, %d substacks, saved count:%lld\n", i, length, n_subs[i], (long long)n);
+    const hdog_record *rec = rbuf[rb].p;
+    const int64_t n = (int64_t)rbuf[rb].n;
+    const std::string dst = sp.dst;
+    writing = launch([dst, rec, n]() { return write_records(dst, rec, n); });
+    writing_stack = i;
+    rb ^= 1;
   }
+  if (rc == HDOG_OK) rc = finish_write();
+  if (writing.valid()) writing.wait();
   if (pending.valid()) pending.wait();   // a read still filling a buffer
   for (uint16_t *b : buf)
     if (b) cudaFreeHost(b);
+  for (RecordBuf &r : rbuf) r.release();
   hdog_ctx_destroy(ctx);
   if (verbose) {
     const double t = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
