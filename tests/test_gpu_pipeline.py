@@ -196,6 +196,39 @@ def test_hdog_main_reads_ahead_in_the_serial_order(tmp_path):
     assert not list((tmp_path / "out").glob("*.part"))
 
 
+def test_hdog_main_write_failure_ends_the_run_in_order(tmp_path):
+    """Records are written while the next stack runs; a failed write still ends the run as
+    a serial run would: the second stack's result cannot be written (its directory does not
+    exist), so the run exits with status 2 after the first stack's result was written, and
+    the third stack's earlier result is left untouched (a serial run never reaches it)."""
+    W, H, L, D = 128, 96, 40, 32
+    p = params(W, H, D, margins=3)
+    vols, stacks = [], []
+    (tmp_path / "out").mkdir()
+    for k in range(3):
+        vol = volume(W, H, L, n_nuclei=60, seed=110 + k)
+        d = tmp_path / ("src%d" % k)
+        d.mkdir()
+        src = []
+        for z in range(L):
+            f = d / ("%06d.bin" % z)
+            vol[z].tofile(f)
+            src.append(str(f))
+        vols.append(vol)
+        out = tmp_path / ("missing" if k == 1 else "out") / ("stack%d.bin" % k)
+        stacks.append((str(out), src))
+    with open(stacks[2][0], "wb") as f:
+        f.write(b"earlier")
+    pf = tmp_path / "param.json"
+    hdog.write_param_file(str(pf), p, stacks)
+    r = subprocess.run([hdog.MAIN_PATH, str(pf)], stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True)
+    assert r.returncode == 2, (r.returncode, r.stderr)
+    assert "stack1.bin.part" in r.stderr
+    got = np.fromfile(stacks[0][0], dtype=hdog.DT_LOCAL)
+    assert_records_match(got, orc.stack(orc.params_from(p), vols[0]), "hdog_main stack 0")
+    assert open(stacks[2][0], "rb").read() == b"earlier"
+
+
 def test_erosion_opt_in_pipeline():
     W, H, D = 128, 128, 16
     vol = volume(W, H, D, n_nuclei=40, seed=5)
