@@ -22,9 +22,11 @@ pytestmark = pytest.mark.gpu
 
 EXACT = ("local_x", "local_y", "local_z", "intensity", "size", "padding")
 # Float sums: the reference's CUB reduce-by-key in float32 against this library's 2^-36
-# fixed point; the eigen features amplify their difference where eigenvalues nearly cancel.
+# fixed point.  The eigen features amplify their difference where eigenvalues nearly
+# cancel; on this stack they stay within 1e-5 relative of the reference path's (measured:
+# structureness 4.6e-7, blobness 3.0e-6), the bound the float features are held to.
 SUM_RTOL = 1e-5
-EIGEN_RTOL = 1e-3
+EIGEN_RTOL = 1e-5
 
 
 def _rel(a, b):
