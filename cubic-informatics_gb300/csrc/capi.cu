@@ -727,6 +727,47 @@ static void host_copy(void *dst, const void *src, size_t bytes) {
   for (std::thread &t : th) t.join();
 }
 
+// Records gathered from `src` into `dst` piece by piece, piece k (src offset, count) landing
+// after the pieces before it, split over up to eight threads of at least 4 MB each (a run's
+// records are up to a few GB).  A thread that cannot be started leaves its part to the
+// calling thread.
+static void host_gather(hdog_record *dst, const hdog_record *src, const std::vector<std::pair<size_t, size_t>> &pieces,
+                        size_t total) {
+  constexpr size_t kPart = ((size_t)4 << 20) / sizeof(hdog_record);
+  const size_t hw = std::max(1u, std::thread::hardware_concurrency());
+  const size_t nt = std::max((size_t)1, std::min({(size_t)8, hw, total / kPart}));
+  // thread i copies the records [i * per, (i + 1) * per) of the output, whichever pieces they fall in
+  const size_t per = (total + nt - 1) / nt;
+  std::vector<size_t> dst_off(pieces.size());
+  for (size_t k = 0, o = 0; k < pieces.size(); k++) {
+    dst_off[k] = o;
+    o += pieces[k].second;
+  }
+  auto part = [&](size_t i) {
+    const size_t a = i * per, b = std::min(total, a + per);
+    if (a >= b) return;
+    // first piece that ends after a
+    size_t k = std::upper_bound(dst_off.begin(), dst_off.end(), a) - dst_off.begin();
+    k = k ? k - 1 : 0;
+    for (; k < pieces.size() && dst_off[k] < b; k++) {
+      const size_t lo = std::max(a, dst_off[k]), hi = std::min(b, dst_off[k] + pieces[k].second);
+      if (hi > lo) memcpy(dst + lo, src + pieces[k].first + (lo - dst_off[k]), (hi - lo) * sizeof(hdog_record));
+    }
+  };
+  std::vector<std::thread> th;
+  std::vector<size_t> left;
+  for (size_t i = 1; i < nt; i++) {
+    try {
+      th.emplace_back(part, i);
+    } catch (...) {
+      left.push_back(i);
+    }
+  }
+  part(0);
+  for (size_t i : left) part(i);
+  for (std::thread &t : th) t.join();
+}
+
 static int copy_out(const RecordBuf &v, hdog_record *out, int64_t cap, int64_t *n) {
   *n = (int64_t)v.n;
   if (*n > cap) return fail(HDOG_ERR_CAPACITY, "record buffer too small: " + std::to_string(*n) + " records");
@@ -1394,14 +1435,18 @@ extern "C" int hdog_graph_run(hdog_graph *g, hdog_record *out, int64_t cap, int6
       HDOG_CUDA_TRY(cudaStreamSynchronize(st));
       g->staged.n = (size_t)total;
       const GraphSlot *table = reinterpret_cast<const GraphSlot *>(g->h_hdr + 2);
+      // the substacks' records in the caller's order: stack by stack, substack by substack
+      std::vector<std::pair<size_t, size_t>> pieces;
+      pieces.reserve((size_t)g->n_sub);
       size_t n = 0;
       for (size_t i = 0; i < nst; i++)
         for (int64_t j = 0; j < g->stack_nsub[i]; j++) {
           const GraphSlot &sl = table[g->stack_first[i] + j];
-          if (sl.count > 0) memcpy(g->last.p + n, g->staged.p + sl.off, (size_t)sl.count * sizeof(hdog_record));
+          if (sl.count > 0) pieces.emplace_back((size_t)sl.off, (size_t)sl.count);
           n += (size_t)sl.count;
           g->last_counts[i] += sl.count;
         }
+      host_gather(g->last.p, g->staged.p, pieces, n);
       g->last.n = n;
     }
   }
