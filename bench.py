@@ -750,7 +750,7 @@ def main():
         # the same forms on small frames, where per-substack launch and host costs matter
         sstacks, sunique, sgen = uneven_stacks(SMALL_N, synth_seed(5), dev, SMALL_SHAPES, SMALL_DENSITY)
         small_params = dict(PARAMS, left_margin=10, right_margin=10, top_margin=10, bottom_margin=10)
-        su = run_uneven(sstacks, sunique, max(3, min(args.steps, 5)), 2, 16, local, small_params)
+        su = run_uneven(sstacks, sunique, max(3, min(args.steps, 5)), 2, 64, local, small_params)
         su["config"] = {"workload": SMALL, "unique_voxels_per_step": sunique,
                         "frames": sorted({"%dx%d" % sh for sh, _ in sstacks}), "generator_s": round(sgen, 1)}
         su["value"] = su["value"] * ws

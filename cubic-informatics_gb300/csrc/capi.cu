@@ -503,33 +503,38 @@ static bool srcs_aligned8(const hdog_ctx *c, int nsub) {
   return true;
 }
 
-// Descriptors of up to kParamSubs substacks travel as a kernel parameter and a one-block
-// kernel stores them: no host-to-device copy on the compute stream, where it would queue on
-// the copy engine behind a stack chunk that hdog_run_stack is copying on its copy stream.
+// The batch's descriptors travel as kernel parameters, kParamSubs substacks per launch, and a
+// one-block kernel stores them: no host-to-device copy on the compute stream, where it would
+// queue on the copy engine behind a stack chunk that hdog_run_stack is copying on its copy
+// stream, and nothing that a captured graph would read from host memory at replay (a
+// captured copy reads its source when the graph runs, by then the last batch's descriptors).
 constexpr int kParamSubs = 16;
 struct SubsParam {
   Sub subs[kParamSubs];
-  int64_t seg[6 * kParamSubs];
+  int64_t seg[6][kParamSubs];
 };
 
-__global__ void k_store_subs(const __grid_constant__ SubsParam P, int nsub, int ms, Sub *subs, int64_t *seg) {
+// substacks [s0, s0 + n) of the context's ms slots: the first nsub of them get descriptors,
+// every slot its six scan-segment entries (seg is [6][ms])
+__global__ void k_store_subs(const __grid_constant__ SubsParam P, int s0, int n, int nsub, int ms, Sub *subs,
+                             int64_t *seg) {
   const int t = threadIdx.x;
-  if (t < nsub) subs[t] = P.subs[t];
-  if (t < 6 * ms) seg[t] = P.seg[t];
+  if (t < n && s0 + t < nsub) subs[s0 + t] = P.subs[t];
+  if (t < 6 * n) seg[(int64_t)(t / n) * ms + s0 + t % n] = P.seg[t / n][t % n];
 }
 
 static int upload_subs(hdog_ctx *c, int nsub, cudaStream_t st) {
   const int ms = c->max_sub;
-  if (ms <= kParamSubs) {
+  for (int s0 = 0; s0 < ms; s0 += kParamSubs) {
+    const int n = std::min(kParamSubs, ms - s0);
     SubsParam P;
-    memcpy(P.subs, c->h_subs, nsub * sizeof(Sub));
-    memcpy(P.seg, c->h_seg, 6 * ms * sizeof(int64_t));
-    KLAUNCH("k_store_subs", st, (k_store_subs<<<1, 6 * kParamSubs, 0, st>>>(P, nsub, ms, c->d_subs, c->d_seg)));
+    memset(&P, 0, sizeof(P));
+    const int ns = std::max(0, std::min(n, nsub - s0));
+    if (ns > 0) memcpy(P.subs, c->h_subs + s0, ns * sizeof(Sub));
+    for (int k = 0; k < 6; k++) memcpy(P.seg[k], c->h_seg + (size_t)k * ms + s0, n * sizeof(int64_t));
+    KLAUNCH("k_store_subs", st, (k_store_subs<<<1, 6 * kParamSubs, 0, st>>>(P, s0, n, nsub, ms, c->d_subs, c->d_seg)));
     HDOG_CUDA_TRY(cudaGetLastError());
-    return HDOG_OK;
   }
-  HDOG_CUDA_TRY(cudaMemcpyAsync(c->d_subs, c->h_subs, nsub * sizeof(Sub), cudaMemcpyHostToDevice, st));
-  HDOG_CUDA_TRY(cudaMemcpyAsync(c->d_seg, c->h_seg, 6 * ms * sizeof(int64_t), cudaMemcpyHostToDevice, st));
   return HDOG_OK;
 }
 
@@ -1298,7 +1303,7 @@ extern "C" int hdog_graph_create(hdog_ctx *const *ctxs, int n_ctx, const hdog_gr
     if (!ctxs[i]) return fail(HDOG_ERR_ARG, "hdog_graph_create: null context");
     if (ctxs[i]->dev != ctxs[0]->dev) return fail(HDOG_ERR_ARG, "hdog_graph_create: contexts on different devices");
     if (ctxs[i]->max_sub > kGraphMaxBatch)
-      return fail(HDOG_ERR_ARG, "hdog_graph_create: contexts of at most 16 substacks");
+      return fail(HDOG_ERR_ARG, "hdog_graph_create: contexts of at most " + std::to_string(kGraphMaxBatch) + " substacks");
     for (int j = 0; j < i; j++)
       if (ctxs[j] == ctxs[i] || (ctxs[j]->W == ctxs[i]->W && ctxs[j]->H == ctxs[i]->H))
         return fail(HDOG_ERR_ARG, "hdog_graph_create: one context per frame shape");

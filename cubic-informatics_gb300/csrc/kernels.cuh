@@ -164,7 +164,7 @@ void launch_finalize(const Sub *d_subs, int nsub, int64_t max_reg_cap, const Sca
                      int64_t *d_num_records, hdog_record *records, int64_t blk_stride, cudaStream_t s);
 
 // ---- graph.cu: record placement of the batched graph form ----
-constexpr int kGraphMaxBatch = 16;   // substacks per batch in the graph form
+constexpr int kGraphMaxBatch = 64;   // substacks per batch in the graph form
 struct GraphIds {
   int id[kGraphMaxBatch];            // the run's index of each batch substack
 };

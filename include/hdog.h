@@ -177,7 +177,7 @@ int hdog_run_param_file(const char *param_path, int verbose);
    Many stacks of uneven depth and frame shape in one captured CUDA graph.  No counterpart
    in the reference, whose HDoG3D_main runs its substacks one at a time
    (src/3D/HDoG3D_main.cpp:294-315); the records are the ones hdog_run_stack gives each stack.
-   The caller gives one context per frame shape (width x height; at most 16 substacks each)
+   The caller gives one context per frame shape (width x height; at most 64 substacks each)
    and the stacks in device memory.  hdog_graph_create schedules every stack's substacks
    (HDoG3D_main's schedule), picks each frame shape's launch shapes with the autotuner on its
    first batch, packs each shape's substacks into batches of its context, and captures all

@@ -94,3 +94,25 @@ def test_autotune_reports_its_choice():
     with hdog.Context(_p(W, H), max_substacks=1) as plain:
         b = plain.run_stack(v)
     assert a.tobytes() == b.tobytes()
+
+
+def test_graph_with_contexts_of_more_substacks_than_one_descriptor_launch_holds():
+    """Contexts of 40 substacks (the batch descriptors then take three launches of 16): the
+    graph's records equal the per-stack calls' on many short stacks of small frames, where
+    a batch spans several stacks."""
+    rng = np.random.default_rng(21)
+    vols = []
+    for i in range(12):
+        w, h = SHAPES[i % 3]
+        vols.append(volume(w // 2, h // 2, int(rng.integers(40, 160)), seed=2000 + i))
+    shapes = sorted({(v.shape[2], v.shape[1]) for v in vols})
+    ref, ref_counts = _plain(_p, vols)
+    assert ref_counts.sum() > 50
+    ctxs = [hdog.Context(_p(w, h), max_substacks=40) for w, h in shapes]
+    with hdog.Graph(ctxs, [torch.from_numpy(v).cuda() for v in vols]) as g:
+        for _ in range(2):
+            got, counts = g.run()
+            assert np.array_equal(counts, ref_counts)
+            assert got.tobytes() == ref.tobytes()
+    for c in ctxs:
+        c.close()
