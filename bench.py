@@ -385,7 +385,7 @@ def uneven_workload(args):
     import torch
     torch.cuda.set_device(0)
     stacks, unique, gen_s = uneven_stacks(40, synth_seed(2), "cuda:0")
-    res = run_uneven(stacks, unique, args.steps, args.warmup, 4)
+    res = run_uneven(stacks, unique, args.steps, args.warmup, 8)
     shapes = {}
     for s, _ in stacks:
         shapes["%dx%d" % s] = shapes.get("%dx%d" % s, 0) + 1
