@@ -74,3 +74,18 @@ def test_fullframe_stack_records_match_oracle(stack):
     ref = orc.stack(orc.params_from(p), stack)
     assert len(ref) > 1000000
     assert_records_match(got, ref, "camera stack")
+
+
+def test_fullframe_depth64_substacks_match_oracle(stack):
+    """Substacks of depth 64 at the full frame (353.9 M voxels each, the largest the
+    reference's 32-bit plane offsets allow at 2560 x 2160): the stack's three substacks,
+    batched, against the oracle."""
+    from test_gpu_pipeline import assert_records_match
+    p = hdog.make_params(**dict(P, depth=64))
+    with hdog.Context(p, max_substacks=3) as ctx:
+        got = ctx.run_stack(torch.from_numpy(stack).cuda())
+    op = orc.params_from(p)
+    assert len(orc.schedule(stack.shape[0], 64, orc.depth_margin(op))) == 3
+    ref = orc.stack(op, stack)
+    assert len(ref) > 500000
+    assert_records_match(got, ref, "camera stack, depth 64")
