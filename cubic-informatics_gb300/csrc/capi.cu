@@ -220,6 +220,7 @@ struct hdog_ctx {
   int max_smem = 48 * 1024;
   bool use_sweep = true;   // fused DoG + Hessian sweep when the parameters allow it
   RecordBuf last;   // records of the last whole-chain call (hdog_last_records)
+  RecordBuf aside;  // records of a host-input stack's last substack when it runs first
   int margin = 0;
   DogTaps taps;
   std::mutex mu;
@@ -375,6 +376,7 @@ extern "C" int hdog_ctx_destroy(hdog_ctx *ctx) {
   if (ctx->copy_st) cudaStreamDestroy(ctx->copy_st);
   if (ctx->h_subs) cudaFreeHost(ctx->h_subs);
   ctx->last.release();
+  ctx->aside.release();
   delete ctx->timer;
   delete ctx;
   return HDOG_OK;
@@ -961,6 +963,16 @@ static int run_stack_locked(hdog_ctx *c, const uint16_t *stack, int on_device, i
     starts.push_back(n);
   }
   const size_t nbatch = starts.size() - 1;
+  // With host input and a first batch of one substack, a short last substack (one whose
+  // slices end before its depth, the rest being the zero tail) runs first: it needs only its
+  // own slices, so the GPU starts after fewer of them are copied (16 instead of 32 for a
+  // 128-slice stack in substacks of 32).  Its records are held aside and appended after the
+  // others, so they come out in the schedule's order.
+  const size_t n_sub_all = z0s.size();
+  const bool last_first = !on_device && nbatch >= 2 && starts[1] == 1 &&
+                          length - z0s.back() < std::min(c->D, length - z0s.front());
+  std::vector<int> order(n_sub_all);
+  for (size_t k = 0; k < n_sub_all; k++) order[k] = z0s[last_first ? (k + n_sub_all - 1) % n_sub_all : k];
   // on an early error return the chunk copies may still be reading the caller's host
   // stack: wait for them, so the caller can free or reuse it once the call returns
   struct CopyWait {
@@ -994,15 +1006,23 @@ static int run_stack_locked(hdog_ctx *c, const uint16_t *stack, int on_device, i
     HDOG_CUDA_TRY(cudaStreamWaitEvent(c->copy_st, c->start_ev, 0));
     copy_wait.st = c->copy_st;
     copy_wait.armed = true;
-    size_t z_done = 0;
+    // slices [0, z_done) and [tail_from, length) are on their way
+    size_t z_done = 0, tail_from = (size_t)length;
     for (size_t b = 0; b < nbatch; b++) {
-      const size_t last = starts[b + 1] - 1;
-      const size_t z_end = std::min((size_t)length, (size_t)z0s[last] + (size_t)c->D);
-      if (z_end > z_done) {
-        HDOG_CUDA_TRY(cudaMemcpyAsync(c->stack_buf + z_done * plane, stack + z_done * plane,
-                                      (z_end - z_done) * plane * sizeof(uint16_t), cudaMemcpyHostToDevice,
-                                      c->copy_st));
-        z_done = z_end;
+      if (b == 0 && last_first) {
+        tail_from = (size_t)z0s.back();
+        HDOG_CUDA_TRY(cudaMemcpyAsync(c->stack_buf + tail_from * plane, stack + tail_from * plane,
+                                      ((size_t)length - tail_from) * plane * sizeof(uint16_t),
+                                      cudaMemcpyHostToDevice, c->copy_st));
+      } else {
+        const size_t last = starts[b + 1] - 1;
+        const size_t z_end = std::min(tail_from, (size_t)order[last] + (size_t)c->D);
+        if (z_end > z_done) {
+          HDOG_CUDA_TRY(cudaMemcpyAsync(c->stack_buf + z_done * plane, stack + z_done * plane,
+                                        (z_end - z_done) * plane * sizeof(uint16_t), cudaMemcpyHostToDevice,
+                                        c->copy_st));
+          z_done = z_end;
+        }
       }
       HDOG_CUDA_TRY(cudaEventRecord(c->chunk_ev[b], c->copy_st));
     }
@@ -1018,13 +1038,23 @@ static int run_stack_locked(hdog_ctx *c, const uint16_t *stack, int on_device, i
     }
     if (!on_device) HDOG_CUDA_TRY(cudaStreamWaitEvent(st, c->chunk_ev[b], 0));
     for (int s = 0; s < nsub; s++) {
-      const int z0 = z0s[first + s];
+      const int z0 = order[first + s];
       set_sub(c, s, dev + (size_t)z0 * plane, std::min(c->D, length - z0), z0);
     }
     TRY(run_batch(c, nsub, st));
-    TRY(collect_records(c, nsub, out, st));
+    if (b == 0 && last_first) {
+      c->aside.clear();
+      TRY(collect_records(c, nsub, c->aside, st));
+    } else {
+      TRY(collect_records(c, nsub, out, st));
+    }
   }
   copy_wait.armed = false;   // every batch waited for its chunk, so the copies are done
+  if (last_first && c->aside.n > 0) {
+    if (!out.reserve(out.n + c->aside.n)) return fail(HDOG_ERR_NOMEM, "page-locked host buffer for the records failed");
+    memcpy(out.p + out.n, c->aside.p, c->aside.n * sizeof(hdog_record));
+    out.n += c->aside.n;
+  }
   return HDOG_OK;
 }
 
