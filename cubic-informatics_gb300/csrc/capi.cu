@@ -686,16 +686,22 @@ static int run_batch(hdog_ctx *c, int nsub, cudaStream_t st) {
 }
 
 // Appends the records of substacks [0, nsub) to out, in substack order.
-static int collect_records(hdog_ctx *c, int nsub, RecordBuf &out, cudaStream_t st) {
+// The batch's records appended to `out`; with `direct`, a page-locked caller buffer of
+// `direct_cap` records, they are also copied to the same positions there while they fit.
+static int collect_records(hdog_ctx *c, int nsub, RecordBuf &out, cudaStream_t st, hdog_record *direct = nullptr,
+                           int64_t direct_cap = 0) {
   HostPhase ph(c, "host_collect_records");
   size_t n = out.n, total = n;
   for (int s = 0; s < nsub; s++) total += (size_t)c->h_counts[s];
   if (!out.reserve(total)) return fail(HDOG_ERR_NOMEM, "page-locked host buffer for the records failed");
   for (int s = 0; s < nsub; s++) {
     const int64_t k = c->h_counts[s];
-    if (k > 0)
-      HDOG_CUDA_TRY(cudaMemcpyAsync(out.p + n, c->records + (int64_t)s * c->reg_cap, k * sizeof(hdog_record),
-                                    cudaMemcpyDeviceToHost, st));
+    if (k > 0) {
+      const hdog_record *src = c->records + (int64_t)s * c->reg_cap;
+      HDOG_CUDA_TRY(cudaMemcpyAsync(out.p + n, src, k * sizeof(hdog_record), cudaMemcpyDeviceToHost, st));
+      if (direct && (int64_t)n + k <= direct_cap)
+        HDOG_CUDA_TRY(cudaMemcpyAsync(direct + n, src, k * sizeof(hdog_record), cudaMemcpyDeviceToHost, st));
+    }
     n += (size_t)k;
   }
   HDOG_CUDA_TRY(cudaStreamSynchronize(st));
@@ -935,7 +941,7 @@ static int schedule(int length, int D, int m, std::vector<int> &z0s) {
 }
 
 static int run_stack_locked(hdog_ctx *c, const uint16_t *stack, int on_device, int length, RecordBuf &out,
-                            cudaStream_t st) {
+                            cudaStream_t st, hdog_record *direct = nullptr, int64_t direct_cap = 0) {
   std::vector<int> z0s;
   TRY(schedule(length, c->D, c->margin, z0s));
   if (z0s.empty()) return HDOG_OK;
@@ -1046,13 +1052,15 @@ static int run_stack_locked(hdog_ctx *c, const uint16_t *stack, int on_device, i
       c->aside.clear();
       TRY(collect_records(c, nsub, c->aside, st));
     } else {
-      TRY(collect_records(c, nsub, out, st));
+      TRY(collect_records(c, nsub, out, st, direct, direct_cap));
     }
   }
   copy_wait.armed = false;   // every batch waited for its chunk, so the copies are done
   if (last_first && c->aside.n > 0) {
     if (!out.reserve(out.n + c->aside.n)) return fail(HDOG_ERR_NOMEM, "page-locked host buffer for the records failed");
     memcpy(out.p + out.n, c->aside.p, c->aside.n * sizeof(hdog_record));
+    if (direct && (int64_t)(out.n + c->aside.n) <= direct_cap)
+      memcpy(direct + out.n, c->aside.p, c->aside.n * sizeof(hdog_record));
     out.n += c->aside.n;
   }
   return HDOG_OK;
@@ -1063,7 +1071,19 @@ extern "C" int hdog_run_stack(hdog_ctx *c, const uint16_t *stack, int stack_on_d
   CTX_GUARD(c);
   if (!stack || !n_records || length < 0 || (cap > 0 && !out)) return fail(HDOG_ERR_ARG, "hdog_run_stack: bad argument");
   c->last.clear();
-  TRY(run_stack_locked(c, stack, stack_on_device, length, c->last, (cudaStream_t)stream));
+  // a page-locked output buffer receives the records straight from the device, batch by
+  // batch, so the copy out of the library's own buffer is skipped when they all fit
+  hdog_record *direct = nullptr;
+  if (cap > 0) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, out) == cudaSuccess && a.type == cudaMemoryTypeHost) direct = out;
+    cudaGetLastError();   // a pointer unknown to CUDA is not an error here
+  }
+  TRY(run_stack_locked(c, stack, stack_on_device, length, c->last, (cudaStream_t)stream, direct, cap));
+  if (direct && (int64_t)c->last.n <= cap) {
+    *n_records = (int64_t)c->last.n;
+    return HDOG_OK;
+  }
   HostPhase ph(c, "host_copy_out");
   return copy_out(c->last, out, cap, n_records);
 }

@@ -441,7 +441,8 @@ class Context:
     def run_stack(self, stack, cap=None, stream=None, out=None):
         """All substacks of one stack (length, H, W) in the reference's schedule.  out: an
         optional dt_local array to fill, as for run_substack (reusing one array across calls
-        saves mapping fresh pages for every result)."""
+        saves mapping fresh pages for every result; in page-locked memory, e.g. a view of a
+        pinned torch tensor, the records are copied into it straight from the device)."""
         on_dev, ptr = _buffer(stack)
         length = int(stack.shape[0])
         out = _out_array(out, cap)

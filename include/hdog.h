@@ -147,7 +147,9 @@ int hdog_run_substack(hdog_ctx *ctx, const uint16_t *img, int img_on_device, int
                       int z0, hdog_record *out, int64_t cap, int64_t *n_records, void *stream);
 /* One stack of `length` slices: the overlapping substack schedule of HDoG3D_main
    (z0 = 0, D-2m, ... while z0 < length - m), the substacks run as one batch when the
-   context has room, records appended in substack order. */
+   context has room, records appended in substack order.  A host stack is copied in chunks
+   that overlap the work (page-locked memory copies fastest); an out array in page-locked
+   memory receives the records straight from the device. */
 int hdog_run_stack(hdog_ctx *ctx, const uint16_t *stack, int stack_on_device, int length,
                    hdog_record *out, int64_t cap, int64_t *n_records, void *stream);
 /* Many stacks of the context's width and height in one call: the substacks of all stacks

@@ -80,6 +80,33 @@ def test_run_stack_matches_substack_loop(max_sub):
     assert got.tobytes() == got_dev.tobytes()
 
 
+def test_run_stack_into_a_page_locked_record_array():
+    """A page-locked output array receives the records straight from the device (the last
+    substack of this stack is short, so it runs first and its records are appended last):
+    the same records as a pageable array; one that is too small gives HDOG_ERR_CAPACITY and
+    the kept result is fetched with hdog_last_records."""
+    W, H, L, D = 192, 160, 100, 32
+    vol = volume(W, H, L, n_nuclei=250, seed=98)
+    p = params(W, H, D, margins=5)
+    with hdog.Context(p, max_substacks=4) as ctx:
+        ref = ctx.run_stack(vol)
+        assert len(ref) > 50
+        pinned = torch.empty(len(ref) * hdog.DT_LOCAL.itemsize, dtype=torch.uint8).pin_memory()
+        out = pinned.numpy().view(hdog.DT_LOCAL)
+        got = ctx.run_stack(vol, out=out)
+        assert got.tobytes() == ref.tobytes()
+        small = torch.empty((len(ref) - 1) * hdog.DT_LOCAL.itemsize, dtype=torch.uint8).pin_memory()
+        n = ctypes.c_int64()
+        rc = hdog.lib().hdog_run_stack(ctx._h, vol.ctypes.data, 0, L, small.data_ptr(), len(ref) - 1,
+                                       ctypes.byref(n), None)
+        assert rc == hdog.HDOG_ERR_CAPACITY and n.value == len(ref)
+        again = np.empty(len(ref), hdog.DT_LOCAL)
+        assert hdog.lib().hdog_last_records(ctx._h, again.ctypes.data, len(again), ctypes.byref(n)) == hdog.HDOG_OK
+        assert again.tobytes() == ref.tobytes()
+    ref_o = orc.stack(orc.params_from(p), vol)
+    assert_records_match(got, ref_o, "page-locked output")
+
+
 def test_hdog_main_executable_writes_reference_records(tmp_path):
     W, H, L, D = 128, 96, 40, 32
     vol = volume(W, H, L, n_nuclei=60, seed=7)
