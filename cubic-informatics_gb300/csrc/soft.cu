@@ -75,6 +75,82 @@ __global__ void k_soft_pass(const float *in, float *out, SoftGeom g, int axis, i
   out[i] = acc;
 }
 
+// The same pass from a shared-memory tile: a block stages the inputs of its outputs once
+// (along x a row segment of kSoftTileX outputs plus the window's reach on each side; along y
+// or z a 32-column slab of kSoftTileYZ outputs plus the reach), out-of-line positions already
+// clamped (min / max / box) or zero (conv), and every output folds its window in the same
+// order and with the same operations as k_soft_pass, so the results are identical; only
+// the repeated global loads of overlapping windows are gone.  For reaches up to
+// kSoftTileMaxR.
+constexpr int kSoftTileX = 256, kSoftTileYZ = 64, kSoftTileMaxR = 64;
+
+__device__ __forceinline__ float soft_fold(const float *w, int step, int c, int n, int mode, int R, const SoftTaps &T) {
+  // w[k * step] is the input at line position c - R + k
+  float acc;
+  if (mode == kConv) {
+    acc = 0.0f;
+    for (int j = -R; j <= R; j++) {
+      const int p = c + j;
+      if (p >= 0 && p < n) acc = __fmaf_rn(T.k[j + R], w[(j + R) * step], acc);
+    }
+  } else if (mode == kBox) {
+    acc = 0.0f;
+    for (int j = -R; j <= R; j++) acc += w[(j + R) * step];
+    acc = acc / (float)(2 * R + 1);
+  } else {
+    acc = w[0];
+    for (int j = -R + 1; j <= R; j++) {
+      const float v = w[(j + R) * step];
+      acc = mode == kMin ? fminf(acc, v) : fmaxf(acc, v);
+    }
+  }
+  return acc;
+}
+
+__device__ __forceinline__ float soft_stage(const float *line, int64_t s, int p, int n, int mode) {
+  if (mode == kConv) return (p >= 0 && p < n) ? line[(int64_t)p * s] : 0.0f;
+  return line[(int64_t)clampi(p, 0, n - 1) * s];
+}
+
+// along x: one block per row segment, one output per thread
+__global__ void __launch_bounds__(kSoftTileX) k_soft_pass_x(const float *in, float *out, SoftGeom g, int mode, int R,
+                                                            SoftTaps T) {
+  __shared__ float tile[kSoftTileX + 2 * kSoftTileMaxR];
+  const int nseg = (g.W + kSoftTileX - 1) / kSoftTileX;
+  const int64_t row = blockIdx.x / nseg;
+  const int x0 = (int)(blockIdx.x % nseg) * kSoftTileX, t = threadIdx.x;
+  const float *line = in + row * g.W;
+  for (int k = t; k < kSoftTileX + 2 * R; k += kSoftTileX) tile[k] = soft_stage(line, 1, x0 - R + k, g.W, mode);
+  __syncthreads();
+  const int x = x0 + t;
+  if (x < g.W) out[row * g.W + x] = soft_fold(tile + t, 1, x, g.W, mode, R, T);
+}
+
+// along y (AXIS 1) or z (AXIS 2): a block of 32 x 8 threads owns 32 columns and
+// kSoftTileYZ outputs of each; thread (tx, ty) computes outputs ty, ty + 8, ...
+template <int AXIS>
+__global__ void __launch_bounds__(256) k_soft_pass_yz(const float *in, float *out, SoftGeom g, int mode, int R,
+                                                      SoftTaps T) {
+  extern __shared__ float slab[];   // [kSoftTileYZ + 2R][32]
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int n = AXIS == 1 ? g.H : g.D;
+  const int64_t s = AXIS == 1 ? (int64_t)g.W : (int64_t)g.W * g.H;
+  const int x = blockIdx.x * 32 + tx;
+  const int c0 = blockIdx.y * kSoftTileYZ;
+  // the other coordinate: z for the y pass, y for the z pass
+  const int64_t other = AXIS == 1 ? (int64_t)blockIdx.z * g.W * g.H : (int64_t)blockIdx.z * g.W;
+  const float *line = in + other + x;
+  const int rows = kSoftTileYZ + 2 * R;
+  for (int k = ty; k < rows; k += 8) slab[k * 32 + tx] = x < g.W ? soft_stage(line, s, c0 - R + k, n, mode) : 0.0f;
+  __syncthreads();
+  if (x >= g.W) return;
+  for (int m = ty; m < kSoftTileYZ; m += 8) {
+    const int c = c0 + m;
+    if (c >= n) break;
+    out[other + x + (int64_t)c * s] = soft_fold(slab + m * 32 + tx, 32, c, n, mode, R, T);
+  }
+}
+
 // Transposed min / max pass: the output gradient of each window goes to the window's first
 // extreme (the index the forward filter took it from).  g_in must start at zero.
 __global__ void k_soft_minmax_adj(const float *in, const float *g_out, float *g_in, SoftGeom g, int axis, int r,
@@ -334,7 +410,24 @@ SoftTaps gauss_taps_f(double sigma, bool derivative) {
 }
 
 void pass(const SoftRun &R, const float *in, float *out, int axis, int mode, int r, const SoftTaps &T) {
-  KLAUNCH("k_soft_pass", R.st, (k_soft_pass<<<R.blocks(), 256, 0, R.st>>>(in, out, R.g, axis, mode, r, T, R.N)));
+  const int reach = mode == kConv ? T.r : r;
+  const SoftGeom &g = R.g;
+  if (reach > kSoftTileMaxR) {
+    KLAUNCH("k_soft_pass", R.st, (k_soft_pass<<<R.blocks(), 256, 0, R.st>>>(in, out, g, axis, mode, r, T, R.N)));
+    return;
+  }
+  if (axis == 0) {
+    const unsigned blocks = (unsigned)(ceil_div(g.W, kSoftTileX) * (int64_t)g.H * g.D);
+    KLAUNCH("k_soft_pass_x", R.st, (k_soft_pass_x<<<blocks, kSoftTileX, 0, R.st>>>(in, out, g, mode, reach, T)));
+    return;
+  }
+  const size_t smem = (size_t)(kSoftTileYZ + 2 * reach) * 32 * sizeof(float);
+  const int n = axis == 1 ? g.H : g.D, other = axis == 1 ? g.D : g.H;
+  const dim3 grid((unsigned)ceil_div(g.W, 32), (unsigned)ceil_div(n, kSoftTileYZ), (unsigned)other);
+  if (axis == 1)
+    KLAUNCH("k_soft_pass_y", R.st, (k_soft_pass_yz<1><<<grid, dim3(32, 8), smem, R.st>>>(in, out, g, mode, reach, T)));
+  else
+    KLAUNCH("k_soft_pass_z", R.st, (k_soft_pass_yz<2><<<grid, dim3(32, 8), smem, R.st>>>(in, out, g, mode, reach, T)));
 }
 
 // conv of `in` with taps (tx, ty, tz) along x, y, z -> out (t1, t2 as temporaries)
