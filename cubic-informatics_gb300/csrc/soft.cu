@@ -151,6 +151,77 @@ __global__ void __launch_bounds__(256) k_soft_pass_yz(const float *in, float *ou
   }
 }
 
+// The two transposed passes from the same tiles, again with the old operations in the old
+// order: the box mean's gather (kAdjBox; the tile holds g_out, zero outside the line), and
+// the min / max scatter to each window's first extreme (kAdjMin / kAdjMax; the tile holds
+// the filter's input, clamped).  Window positions outside the line are clamped exactly as
+// in k_soft_box_adj / k_soft_minmax_adj.
+enum { kAdjBox = 0, kAdjMin = 1, kAdjMax = 2 };
+
+__device__ __forceinline__ void soft_adj_one(const float *w, int step, int c, int n, int R, int adj, int64_t base,
+                                             int64_t s, const float *g_out, float *g_in) {
+  // w[k * step] is the staged value at line position c - R + k
+  if (adj == kAdjBox) {
+    float acc = 0.0f;
+    for (int t = max(0, c - R); t <= min(n - 1, c + R); t++) acc += w[(t - c + R) * step];
+    if (c == 0)
+      for (int t = 0; t < min(n, R); t++) acc += (float)(R - t) * w[(t - c + R) * step];
+    if (c == n - 1)
+      for (int t = max(0, n - 1 - R + 1); t < n; t++) acc += (float)(t + R - (n - 1)) * w[(t - c + R) * step];
+    g_in[base + (int64_t)c * s] = acc / (float)(2 * R + 1);
+    return;
+  }
+  const float go = g_out[base + (int64_t)c * s];
+  if (go == 0.0f) return;
+  int arg = clampi(c - R, 0, n - 1);
+  float best = w[0];
+  for (int j = -R + 1; j <= R; j++) {
+    const float v = w[(j + R) * step];
+    if (adj == kAdjMax ? v > best : v < best) {
+      best = v;
+      arg = clampi(c + j, 0, n - 1);
+    }
+  }
+  atomicAdd(g_in + base + (int64_t)arg * s, go);
+}
+
+__global__ void __launch_bounds__(kSoftTileX) k_soft_adj_x(const float *src, const float *g_out, float *g_in,
+                                                           SoftGeom g, int adj, int R) {
+  __shared__ float tile[kSoftTileX + 2 * kSoftTileMaxR];
+  const int nseg = (g.W + kSoftTileX - 1) / kSoftTileX;
+  const int64_t row = blockIdx.x / nseg;
+  const int x0 = (int)(blockIdx.x % nseg) * kSoftTileX, t = threadIdx.x;
+  const float *line = src + row * g.W;
+  const int stage_mode = adj == kAdjBox ? kConv : kMin;   // zero outside / clamped
+  for (int k = t; k < kSoftTileX + 2 * R; k += kSoftTileX) tile[k] = soft_stage(line, 1, x0 - R + k, g.W, stage_mode);
+  __syncthreads();
+  const int x = x0 + t;
+  if (x < g.W) soft_adj_one(tile + t, 1, x, g.W, R, adj, row * g.W, 1, g_out, g_in);
+}
+
+template <int AXIS>
+__global__ void __launch_bounds__(256) k_soft_adj_yz(const float *src, const float *g_out, float *g_in, SoftGeom g,
+                                                     int adj, int R) {
+  extern __shared__ float slab[];   // [kSoftTileYZ + 2R][32]
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int n = AXIS == 1 ? g.H : g.D;
+  const int64_t s = AXIS == 1 ? (int64_t)g.W : (int64_t)g.W * g.H;
+  const int x = blockIdx.x * 32 + tx;
+  const int c0 = blockIdx.y * kSoftTileYZ;
+  const int64_t other = AXIS == 1 ? (int64_t)blockIdx.z * g.W * g.H : (int64_t)blockIdx.z * g.W;
+  const float *line = src + other + x;
+  const int stage_mode = adj == kAdjBox ? kConv : kMin;
+  const int rows = kSoftTileYZ + 2 * R;
+  for (int k = ty; k < rows; k += 8) slab[k * 32 + tx] = x < g.W ? soft_stage(line, s, c0 - R + k, n, stage_mode) : 0.0f;
+  __syncthreads();
+  if (x >= g.W) return;
+  for (int m = ty; m < kSoftTileYZ; m += 8) {
+    const int c = c0 + m;
+    if (c >= n) break;
+    soft_adj_one(slab + m * 32 + tx, 32, c, n, R, adj, other + x, s, g_out, g_in);
+  }
+}
+
 // Transposed min / max pass: the output gradient of each window goes to the window's first
 // extreme (the index the forward filter took it from).  g_in must start at zero.
 __global__ void k_soft_minmax_adj(const float *in, const float *g_out, float *g_in, SoftGeom g, int axis, int r,
@@ -430,6 +501,33 @@ void pass(const SoftRun &R, const float *in, float *out, int axis, int mode, int
     KLAUNCH("k_soft_pass_z", R.st, (k_soft_pass_yz<2><<<grid, dim3(32, 8), smem, R.st>>>(in, out, g, mode, reach, T)));
 }
 
+// a transposed pass along `axis`: box gather (src = g_out, into g_in) or min / max scatter
+// (src = the filter's input, g_out into the zeroed g_in)
+void adj_pass(const SoftRun &R, const float *src, const float *g_out, float *g_in, int axis, int adj, int r) {
+  const SoftGeom &g = R.g;
+  const unsigned nb = R.blocks();
+  if (r > kSoftTileMaxR) {
+    if (adj == kAdjBox)
+      KLAUNCH("k_soft_box_adj", R.st, (k_soft_box_adj<<<nb, 256, 0, R.st>>>(src, g_in, g, axis, r, R.N)));
+    else
+      KLAUNCH("k_soft_minmax_adj", R.st, (k_soft_minmax_adj<<<nb, 256, 0, R.st>>>(src, g_out, g_in, g, axis, r,
+                                                                                 adj == kAdjMax, R.N)));
+    return;
+  }
+  if (axis == 0) {
+    const unsigned blocks = (unsigned)(ceil_div(g.W, kSoftTileX) * (int64_t)g.H * g.D);
+    KLAUNCH("k_soft_adj_x", R.st, (k_soft_adj_x<<<blocks, kSoftTileX, 0, R.st>>>(src, g_out, g_in, g, adj, r)));
+    return;
+  }
+  const size_t smem = (size_t)(kSoftTileYZ + 2 * r) * 32 * sizeof(float);
+  const int n = axis == 1 ? g.H : g.D, other = axis == 1 ? g.D : g.H;
+  const dim3 grid((unsigned)ceil_div(g.W, 32), (unsigned)ceil_div(n, kSoftTileYZ), (unsigned)other);
+  if (axis == 1)
+    KLAUNCH("k_soft_adj_y", R.st, (k_soft_adj_yz<1><<<grid, dim3(32, 8), smem, R.st>>>(src, g_out, g_in, g, adj, r)));
+  else
+    KLAUNCH("k_soft_adj_z", R.st, (k_soft_adj_yz<2><<<grid, dim3(32, 8), smem, R.st>>>(src, g_out, g_in, g, adj, r)));
+}
+
 // conv of `in` with taps (tx, ty, tz) along x, y, z -> out (t1, t2 as temporaries)
 void conv3(const SoftRun &R, const float *in, float *out, const SoftTaps &tx, const SoftTaps &ty, const SoftTaps &tz,
            float *t1, float *t2) {
@@ -578,7 +676,7 @@ int soft_backward(const hdog_soft_params *p, const float *vol, const int32_t *po
       for (int a = 2; a >= 0; a--) {
         float *dst = (cur == ping) ? pong : ping;
         if (rr[a] == 0) continue;
-        KLAUNCH("k_soft_box_adj", st, (k_soft_box_adj<<<nb, 256, 0, st>>>(cur, dst, R.g, a, rr[a], R.N)));
+        adj_pass(R, cur, nullptr, dst, a, kAdjBox, rr[a]);
         cur = dst;
       }
       // filter inputs of the forward passes x, y, z: vol, *1, *2
@@ -588,8 +686,7 @@ int soft_backward(const hdog_soft_params *p, const float *vol, const int32_t *po
         float *dst = (cur == ping) ? pong : ping;
         if (dst == g) dst = R.slot(S_GB);
         cudaMemsetAsync(dst, 0, R.N * sizeof(float), st);
-        KLAUNCH("k_soft_minmax_adj", st, (k_soft_minmax_adj<<<nb, 256, 0, st>>>(fin[a], cur, dst, R.g, a, rr[a],
-                                                                               side, R.N)));
+        adj_pass(R, fin[a], cur, dst, a, side == 0 ? kAdjMin : kAdjMax, rr[a]);
         cur = dst;
       }
       KLAUNCH("k_soft_add", st, (k_soft_add<<<nb, 256, 0, st>>>(grad_vol, cur, R.N)));
