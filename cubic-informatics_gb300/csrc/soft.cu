@@ -21,6 +21,12 @@
 // the nearest border repeats each edge value) and the transposed min / max filters (each
 // window's gradient goes to its first extreme, recomputed from the filter's input).
 // Tap radii are (int)(2 sigma + 0.5), held fixed for the derivatives.
+//
+// Every windowed pass (and its transpose) folds each output's window in one fixed order;
+// the passes run from shared-memory tiles that stage a line segment or column slab with the
+// window's reach once (k_soft_pass_x / _yz, k_soft_adj_x / _yz), and fall back to the
+// untiled kernels for reaches above kSoftTileMaxR.  The float32 sigma gradients are
+// sensitive to the last bits of the normalized volume, so the order is kept as it is.
 #include <cmath>
 
 #include "kernels.cuh"
