@@ -133,10 +133,13 @@ __global__ void __launch_bounds__(kSoftTileX) k_soft_pass_x(const float *in, flo
 }
 
 // along y (AXIS 1) or z (AXIS 2): a block of 32 x 8 threads owns 32 columns and
-// kSoftTileYZ outputs of each; thread (tx, ty) computes outputs ty, ty + 8, ...
-template <int AXIS>
+// kSoftTileYZ outputs of each; thread (tx, ty) computes outputs ty, ty + 8, ...  With DOT the
+// outputs are not stored: the block adds sum(output * dotw) over its outputs to *dot_out
+// (double; the same products the separate dot kernel forms).
+template <int AXIS, bool DOT = false>
 __global__ void __launch_bounds__(256) k_soft_pass_yz(const float *in, float *out, SoftGeom g, int mode, int R,
-                                                      SoftTaps T) {
+                                                      SoftTaps T, const float *dotw = nullptr,
+                                                      double *dot_out = nullptr) {
   extern __shared__ float slab[];   // [kSoftTileYZ + 2R][32]
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int n = AXIS == 1 ? g.H : g.D;
@@ -149,11 +152,26 @@ __global__ void __launch_bounds__(256) k_soft_pass_yz(const float *in, float *ou
   const int rows = kSoftTileYZ + 2 * R;
   for (int k = ty; k < rows; k += 8) slab[k * 32 + tx] = x < g.W ? soft_stage(line, s, c0 - R + k, n, mode) : 0.0f;
   __syncthreads();
-  if (x >= g.W) return;
-  for (int m = ty; m < kSoftTileYZ; m += 8) {
-    const int c = c0 + m;
-    if (c >= n) break;
-    out[other + x + (int64_t)c * s] = soft_fold(slab + m * 32 + tx, 32, c, n, mode, R, T);
+  double acc = 0.0;
+  if (x < g.W)
+    for (int m = ty; m < kSoftTileYZ; m += 8) {
+      const int c = c0 + m;
+      if (c >= n) break;
+      const int64_t i = other + x + (int64_t)c * s;
+      const float v = soft_fold(slab + m * 32 + tx, 32, c, n, mode, R, T);
+      if (DOT) acc += (double)dotw[i] * (double)v;
+      else out[i] = v;
+    }
+  if (DOT) {
+    __shared__ double part[8];
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xFFFFFFFFu, acc, o);
+    if (tx == 0) part[ty] = acc;
+    __syncthreads();
+    if (tx == 0 && ty == 0) {
+      double t = 0.0;
+      for (int w = 0; w < 8; w++) t += part[w];
+      atomicAdd(dot_out, t);
+    }
   }
 }
 
@@ -507,6 +525,16 @@ void pass(const SoftRun &R, const float *in, float *out, int axis, int mode, int
     KLAUNCH("k_soft_pass_z", R.st, (k_soft_pass_yz<2><<<grid, dim3(32, 8), smem, R.st>>>(in, out, g, mode, reach, T)));
 }
 
+// the correlation along z with T, summed against w into *acc (double) instead of stored
+void pass_z_dot(const SoftRun &R, const float *in, const SoftTaps &T, const float *w, double *acc) {
+  static_assert(kSoftMaxRadius <= kSoftTileMaxR, "Gaussian taps fit the z tile");
+  const SoftGeom &g = R.g;
+  const size_t smem = (size_t)(kSoftTileYZ + 2 * T.r) * 32 * sizeof(float);
+  const dim3 grid((unsigned)ceil_div(g.W, 32), (unsigned)ceil_div(g.D, kSoftTileYZ), (unsigned)g.H);
+  KLAUNCH("k_soft_pass_z_dot", R.st, (k_soft_pass_yz<2, true><<<grid, dim3(32, 8), smem, R.st>>>(
+                                         in, nullptr, g, kConv, T.r, T, w, acc)));
+}
+
 // a transposed pass along `axis`: box gather (src = g_out, into g_in) or min / max scatter
 // (src = the filter's input, g_out into the zeroed g_in)
 void adj_pass(const SoftRun &R, const float *src, const float *g_out, float *g_in, int axis, int adj, int r) {
@@ -641,12 +669,24 @@ int soft_backward(const hdog_soft_params *p, const float *vol, const int32_t *po
     // acc[0..5]: <gdog, d dog / d sigma_k> without the normalizer term; acc[6]: <gdog, dog>
     cudaMemsetAsync(R.acc, 0, 8 * sizeof(double), st);
     const unsigned db = 152 * 4;
-    for (int k = 0; k < 6; k++) {
-      const int sc = k / 3, ax = k % 3;
-      SoftTaps t[3];
-      for (int a = 0; a < 3; a++) t[a] = gauss_taps_f(s[3 * sc + a], a == ax);
-      conv3(R, R.slot(S_NORM), R.slot(S_T3), t[0], t[1], t[2], R.slot(S_T1), R.slot(S_T2));
-      KLAUNCH("k_soft_dot", st, (k_soft_dot<<<db, 256, 0, st>>>(gdog, R.slot(S_T3), R.N, R.acc + k)));
+    // Per scale: <gdog, C_z C_y C_x norm> with the derivative taps on one axis.  The plain x
+    // pass serves the y and z derivatives, and every z pass folds straight into the dot.
+    float *nm = R.slot(S_NORM), *t1 = R.slot(S_T1), *t2 = R.slot(S_T2);
+    for (int sc = 0; sc < 2; sc++) {
+      SoftTaps pl[3], dv[3];
+      for (int a = 0; a < 3; a++) {
+        pl[a] = gauss_taps_f(s[3 * sc + a], false);
+        dv[a] = gauss_taps_f(s[3 * sc + a], true);
+      }
+      double *acc = R.acc + 3 * sc;
+      pass(R, nm, t1, 0, kConv, 0, pl[0]);
+      pass(R, t1, t2, 1, kConv, 0, pl[1]);
+      pass_z_dot(R, t2, dv[2], gdog, acc + 2);
+      pass(R, t1, t2, 1, kConv, 0, dv[1]);
+      pass_z_dot(R, t2, pl[2], gdog, acc + 1);
+      pass(R, nm, t1, 0, kConv, 0, dv[0]);
+      pass(R, t1, t2, 1, kConv, 0, pl[1]);
+      pass_z_dot(R, t2, pl[2], gdog, acc + 0);
     }
     KLAUNCH("k_soft_dot", st, (k_soft_dot<<<db, 256, 0, st>>>(gdog, R.slot(S_DOG), R.N, R.acc + 6)));
     double h[8];
