@@ -1551,6 +1551,17 @@ extern "C" int hdog_soft_backward(const hdog_soft_params *p, const float *d_volu
   return HDOG_OK;
 }
 
+extern "C" int hdog_soft_backward_kept(const hdog_soft_params *p, const float *d_volume, const int32_t *d_pos,
+                                       int n_pos, const int32_t *d_neg, int n_neg, float grad_loss,
+                                       float *d_grad_volume, float *d_grad_sigma, float *d_grad_thresh,
+                                       void *d_workspace, void *stream) {
+  const int rc = soft_backward(p, d_volume, d_pos, n_pos, d_neg, n_neg, grad_loss, d_grad_volume, d_grad_sigma,
+                               d_grad_thresh, d_workspace, (cudaStream_t)stream, true);
+  if (rc != HDOG_OK) return fail(rc, "hdog_soft_backward_kept: bad argument, parameter or sigma");
+  HDOG_CUDA_TRY(cudaGetLastError());
+  return HDOG_OK;
+}
+
 // ------------------------------------------------------------------ after the records
 extern "C" int hdog_records_to_global(const hdog_record *d_records, int64_t n, const hdog_global_params *p,
                                       hdog_global *d_out, void *stream) {

@@ -117,7 +117,7 @@ int soft_forward(const hdog_soft_params *p, const float *vol, const int32_t *pos
                  int n_neg, float *loss, float *scores, void *work, cudaStream_t st);
 int soft_backward(const hdog_soft_params *p, const float *vol, const int32_t *pos, int n_pos, const int32_t *neg,
                   int n_neg, float grad_loss, float *grad_vol, float *grad_sigma, float *grad_thresh, void *work,
-                  cudaStream_t st);
+                  cudaStream_t st, bool forward_kept = false);
 
 // Zero `bytes` (a multiple of 4) of device memory on stream s with a kernel.
 void zero_async(void *p, size_t bytes, cudaStream_t s);

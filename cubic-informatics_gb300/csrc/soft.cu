@@ -10,8 +10,9 @@
 // by tau, tau^2, tau^3.  Loss = mean score at the positive points - mean score at the
 // negative points.
 //
-// Backward recomputes every intermediate from the input (nothing is kept between the two
-// calls) and runs the adjoints in reverse: the score's derivative scattered through the
+// Backward recomputes every intermediate from the input, or (the _kept entry) takes the
+// forward chain's intermediates from the workspace the forward call filled, which the
+// backward does not overwrite, and runs the adjoints in reverse: the score's derivative scattered through the
 // Hessian stencil into a DoG-shaped gradient; for the sigmas, the derivative-of-Gaussian
 // taps (d t_k / d sigma = t_k (k^2 - sum_j t_j j^2) / sigma^3 for the normalized taps) on
 // one axis and the plain taps on the others, dotted with that gradient, plus the
@@ -22,11 +23,13 @@
 // window's gradient goes to its first extreme, recomputed from the filter's input).
 // Tap radii are (int)(2 sigma + 0.5), held fixed for the derivatives.
 //
-// Every windowed pass (and its transpose) folds each output's window in one fixed order;
-// the passes run from shared-memory tiles that stage a line segment or column slab with the
-// window's reach once (k_soft_pass_x / _yz, k_soft_adj_x / _yz), and fall back to the
-// untiled kernels for reaches above kSoftTileMaxR.  The float32 sigma gradients are
-// sensitive to the last bits of the normalized volume, so the order is kept as it is.
+// The windowed passes (and their transposes) run from shared-memory tiles that stage a line
+// segment or column slab with the window's reach once (k_soft_pass_x / _yz, k_soft_adj_x /
+// _yz, k_soft_ext_yz, k_soft_ext_adj_yz), and fall back to the untiled kernels for reaches
+// above kSoftTileMaxR.  Box means and Gaussians fold each output's window in one fixed order:
+// the float32 sigma gradients are sensitive to the last bits of the normalized volume, so
+// that order is kept.  Min / max windows and their first extremes, which do not round, come
+// from doubling in the tile.
 #include <cmath>
 
 #include "kernels.cuh"
@@ -118,24 +121,107 @@ __device__ __forceinline__ float soft_stage(const float *line, int64_t s, int p,
   return line[(int64_t)clampi(p, 0, n - 1) * s];
 }
 
-// along x: one block per row segment, one output per thread
+// Min / max windows from the staged tile by doubling: after the steps with spans 1, 2, ..., q
+// an entry holds the extreme of the q staged values from it on, where q is the largest power
+// of two <= w = 2R + 1; a window [t, t + 2R] is then the extreme of the entries t and
+// t + w - q (two spans that overlap and cover it).  Min and max do not round, so the values
+// equal the sequential fold's (for inputs without NaN).  With indices, an entry also carries
+// the staged position of its span's first extreme: a later span replaces it only when
+// strictly better, which keeps the first extreme of the union (a tie inside the overlap is
+// already the earlier span's).  Along y and z a block of 32 x 16 threads doubles a slab of
+// kSoftTileYZ + 2R rows (R <= kSoftExtMaxR), kSoftExtPer rows per thread.
+constexpr int kSoftExtMaxR = 32, kSoftExtPer = (kSoftTileYZ + 2 * kSoftExtMaxR) / 16;
+
+__device__ __forceinline__ float soft_ext(float a, float b, bool is_max) { return is_max ? fmaxf(a, b) : fminf(a, b); }
+
+__device__ __forceinline__ void soft_ext_at(float &a, int &ia, float b, int ib, bool is_max) {
+  if (is_max ? b > a : b < a) {
+    a = b;
+    ia = ib;
+  }
+}
+
+__device__ __forceinline__ int soft_span(int R) {   // the largest power of two <= 2R + 1
+  return 1 << (31 - __clz(2 * R + 1));
+}
+
+// Dot products as compensated float32 sums (GB300's FP64 pipe is a small fraction of its
+// FP32 rate): a product a b is split exactly into p + e (p = a b rounded, e = fma(a, b, -p)),
+// added to a running hi + lo by Knuth's TwoSum (the rounding error of hi + p goes to lo), and
+// per warp the pairs combine the same way before one conversion to double; the relative error
+// of a thread's or warp's sum is about 2^-48, against 2^-53 per addition of a double sum.
+__device__ __forceinline__ void soft_two_sum(float &hi, float &lo, float v) {
+  const float s = __fadd_rn(hi, v), bb = __fsub_rn(s, hi);
+  lo = __fadd_rn(lo, __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(v, bb)));
+  hi = s;
+}
+
+__device__ __forceinline__ void soft_dot_add(float &hi, float &lo, float a, float b) {
+  const float p = __fmul_rn(a, b);
+  lo = __fadd_rn(lo, __fmaf_rn(a, b, -p));
+  soft_two_sum(hi, lo, p);
+}
+
+// the warp's (hi, lo) pairs summed into lane 0's, returned as a double there
+__device__ __forceinline__ double soft_warp_dot(float hi, float lo) {
+  for (int o = 16; o > 0; o >>= 1) {
+    const float h2 = __shfl_down_sync(0xFFFFFFFFu, hi, o), l2 = __shfl_down_sync(0xFFFFFFFFu, lo, o);
+    lo = __fadd_rn(lo, l2);
+    soft_two_sum(hi, lo, h2);
+  }
+  return (double)hi + (double)lo;
+}
+
+// along x: a block takes the same segment of kSoftRowsX consecutive rows (so each thread has
+// several loads in flight before the barrier), one output per thread and row
+constexpr int kSoftRowsX = 4;
+
 __global__ void __launch_bounds__(kSoftTileX) k_soft_pass_x(const float *in, float *out, SoftGeom g, int mode, int R,
                                                             SoftTaps T) {
-  __shared__ float tile[kSoftTileX + 2 * kSoftTileMaxR];
+  __shared__ float tile[kSoftRowsX][kSoftTileX + 2 * kSoftTileMaxR];
   const int nseg = (g.W + kSoftTileX - 1) / kSoftTileX;
-  const int64_t row = blockIdx.x / nseg;
+  const int64_t row0 = (int64_t)(blockIdx.x / nseg) * kSoftRowsX;
+  const int nr = (int)min((int64_t)kSoftRowsX, (int64_t)g.H * g.D - row0);
   const int x0 = (int)(blockIdx.x % nseg) * kSoftTileX, t = threadIdx.x;
-  const float *line = in + row * g.W;
-  for (int k = t; k < kSoftTileX + 2 * R; k += kSoftTileX) tile[k] = soft_stage(line, 1, x0 - R + k, g.W, mode);
+  const int L = kSoftTileX + 2 * R;
+  for (int r = 0; r < nr; r++)
+    for (int k = t; k < L; k += kSoftTileX) tile[r][k] = soft_stage(in + (row0 + r) * g.W, 1, x0 - R + k, g.W, mode);
   __syncthreads();
   const int x = x0 + t;
-  if (x < g.W) out[row * g.W + x] = soft_fold(tile + t, 1, x, g.W, mode, R, T);
+  if (mode == kMin || mode == kMax) {
+    const bool is_max = mode == kMax;
+    const int q_end = soft_span(R);
+    for (int q = 1; q < q_end; q *= 2) {
+      const int lim = L - 2 * q + 1;   // entries whose span of 2q stays inside the tile
+      float a[kSoftRowsX][2];
+#pragma unroll
+      for (int r = 0; r < kSoftRowsX; r++)
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+          const int k = t + h * kSoftTileX;
+          a[r][h] = r < nr && k < lim ? soft_ext(tile[r][k], tile[r][k + q], is_max) : 0.0f;
+        }
+      __syncthreads();
+#pragma unroll
+      for (int r = 0; r < kSoftRowsX; r++)
+#pragma unroll
+        for (int h = 0; h < 2; h++)
+          if (r < nr && t + h * kSoftTileX < lim) tile[r][t + h * kSoftTileX] = a[r][h];
+      __syncthreads();
+    }
+    if (x < g.W)
+      for (int r = 0; r < nr; r++)
+        out[(row0 + r) * g.W + x] = soft_ext(tile[r][t], tile[r][t + 2 * R + 1 - q_end], is_max);
+    return;
+  }
+  if (x < g.W)
+    for (int r = 0; r < nr; r++) out[(row0 + r) * g.W + x] = soft_fold(tile[r] + t, 1, x, g.W, mode, R, T);
 }
 
 // along y (AXIS 1) or z (AXIS 2): a block of 32 x 8 threads owns 32 columns and
 // kSoftTileYZ outputs of each; thread (tx, ty) computes outputs ty, ty + 8, ...  With DOT the
 // outputs are not stored: the block adds sum(output * dotw) over its outputs to *dot_out
-// (double; the same products the separate dot kernel forms).
+// (a double; compensated float32 sums up to the warps).
 template <int AXIS, bool DOT = false>
 __global__ void __launch_bounds__(256) k_soft_pass_yz(const float *in, float *out, SoftGeom g, int mode, int R,
                                                       SoftTaps T, const float *dotw = nullptr,
@@ -152,19 +238,19 @@ __global__ void __launch_bounds__(256) k_soft_pass_yz(const float *in, float *ou
   const int rows = kSoftTileYZ + 2 * R;
   for (int k = ty; k < rows; k += 8) slab[k * 32 + tx] = x < g.W ? soft_stage(line, s, c0 - R + k, n, mode) : 0.0f;
   __syncthreads();
-  double acc = 0.0;
+  float hi = 0.0f, lo = 0.0f;
   if (x < g.W)
     for (int m = ty; m < kSoftTileYZ; m += 8) {
       const int c = c0 + m;
       if (c >= n) break;
       const int64_t i = other + x + (int64_t)c * s;
       const float v = soft_fold(slab + m * 32 + tx, 32, c, n, mode, R, T);
-      if (DOT) acc += (double)dotw[i] * (double)v;
+      if (DOT) soft_dot_add(hi, lo, dotw[i], v);
       else out[i] = v;
     }
   if (DOT) {
     __shared__ double part[8];
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xFFFFFFFFu, acc, o);
+    const double acc = soft_warp_dot(hi, lo);
     if (tx == 0) part[ty] = acc;
     __syncthreads();
     if (tx == 0 && ty == 0) {
@@ -172,6 +258,42 @@ __global__ void __launch_bounds__(256) k_soft_pass_yz(const float *in, float *ou
       for (int w = 0; w < 8; w++) t += part[w];
       atomicAdd(dot_out, t);
     }
+  }
+}
+
+// min / max along y (AXIS 1) or z (AXIS 2) by doubling, 32 columns x kSoftTileYZ outputs
+template <int AXIS>
+__global__ void __launch_bounds__(512) k_soft_ext_yz(const float *in, float *out, SoftGeom g, int is_max, int R) {
+  __shared__ float slab[(kSoftTileYZ + 2 * kSoftExtMaxR) * 32];
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int n = AXIS == 1 ? g.H : g.D;
+  const int64_t s = AXIS == 1 ? (int64_t)g.W : (int64_t)g.W * g.H;
+  const int x = blockIdx.x * 32 + tx;
+  const int c0 = blockIdx.y * kSoftTileYZ;
+  const int64_t other = AXIS == 1 ? (int64_t)blockIdx.z * g.W * g.H : (int64_t)blockIdx.z * g.W;
+  const float *line = in + other + x;
+  const int rows = kSoftTileYZ + 2 * R, q_end = soft_span(R);
+  for (int k = ty; k < rows; k += 16) slab[k * 32 + tx] = x < g.W ? soft_stage(line, s, c0 - R + k, n, kMin) : 0.0f;
+  __syncthreads();
+  for (int q = 1; q < q_end; q *= 2) {
+    const int lim = rows - 2 * q + 1;
+    float v[kSoftExtPer];
+#pragma unroll
+    for (int e = 0; e < kSoftExtPer; e++) {
+      const int k = ty + 16 * e;
+      v[e] = k < lim ? soft_ext(slab[k * 32 + tx], slab[(k + q) * 32 + tx], is_max) : 0.0f;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int e = 0; e < kSoftExtPer; e++)
+      if (ty + 16 * e < lim) slab[(ty + 16 * e) * 32 + tx] = v[e];
+    __syncthreads();
+  }
+  if (x >= g.W) return;
+  for (int m = ty; m < kSoftTileYZ; m += 16) {
+    const int c = c0 + m;
+    if (c >= n) break;
+    out[other + x + (int64_t)c * s] = soft_ext(slab[m * 32 + tx], slab[(m + 2 * R + 1 - q_end) * 32 + tx], is_max);
   }
 }
 
@@ -211,16 +333,69 @@ __device__ __forceinline__ void soft_adj_one(const float *w, int step, int c, in
 
 __global__ void __launch_bounds__(kSoftTileX) k_soft_adj_x(const float *src, const float *g_out, float *g_in,
                                                            SoftGeom g, int adj, int R) {
-  __shared__ float tile[kSoftTileX + 2 * kSoftTileMaxR];
+  __shared__ float tile[kSoftRowsX][kSoftTileX + 2 * kSoftTileMaxR];
+  __shared__ int at[kSoftRowsX][kSoftTileX + 2 * kSoftTileMaxR];
   const int nseg = (g.W + kSoftTileX - 1) / kSoftTileX;
-  const int64_t row = blockIdx.x / nseg;
+  const int64_t row0 = (int64_t)(blockIdx.x / nseg) * kSoftRowsX;
+  const int nr = (int)min((int64_t)kSoftRowsX, (int64_t)g.H * g.D - row0);
   const int x0 = (int)(blockIdx.x % nseg) * kSoftTileX, t = threadIdx.x;
-  const float *line = src + row * g.W;
+  const int L = kSoftTileX + 2 * R;
   const int stage_mode = adj == kAdjBox ? kConv : kMin;   // zero outside / clamped
-  for (int k = t; k < kSoftTileX + 2 * R; k += kSoftTileX) tile[k] = soft_stage(line, 1, x0 - R + k, g.W, stage_mode);
+  for (int r = 0; r < nr; r++)
+    for (int k = t; k < L; k += kSoftTileX) {
+      tile[r][k] = soft_stage(src + (row0 + r) * g.W, 1, x0 - R + k, g.W, stage_mode);
+      at[r][k] = k;
+    }
   __syncthreads();
   const int x = x0 + t;
-  if (x < g.W) soft_adj_one(tile + t, 1, x, g.W, R, adj, row * g.W, 1, g_out, g_in);
+  if (adj != kAdjBox) {
+    // first extreme of every window by doubling over (value, staged position) pairs
+    const bool is_max = adj == kAdjMax;
+    const int q_end = soft_span(R);
+    for (int q = 1; q < q_end; q *= 2) {
+      const int lim = L - 2 * q + 1;
+      float a[kSoftRowsX][2];
+      int ia[kSoftRowsX][2];
+#pragma unroll
+      for (int r = 0; r < kSoftRowsX; r++)
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+          const int k = t + h * kSoftTileX;
+          a[r][h] = 0.0f;
+          ia[r][h] = 0;
+          if (r < nr && k < lim) {
+            a[r][h] = tile[r][k];
+            ia[r][h] = at[r][k];
+            soft_ext_at(a[r][h], ia[r][h], tile[r][k + q], at[r][k + q], is_max);
+          }
+        }
+      __syncthreads();
+#pragma unroll
+      for (int r = 0; r < kSoftRowsX; r++)
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+          const int k = t + h * kSoftTileX;
+          if (r < nr && k < lim) {
+            tile[r][k] = a[r][h];
+            at[r][k] = ia[r][h];
+          }
+        }
+      __syncthreads();
+    }
+    if (x < g.W)
+      for (int r = 0; r < nr; r++) {
+        const int64_t row = (row0 + r) * g.W;
+        const float go = g_out[row + x];
+        if (go == 0.0f) continue;
+        float v = tile[r][t];
+        int iv = at[r][t];
+        soft_ext_at(v, iv, tile[r][t + 2 * R + 1 - q_end], at[r][t + 2 * R + 1 - q_end], is_max);
+        atomicAdd(g_in + row + clampi(x0 - R + iv, 0, g.W - 1), go);
+      }
+    return;
+  }
+  if (x < g.W)
+    for (int r = 0; r < nr; r++) soft_adj_one(tile[r] + t, 1, x, g.W, R, adj, (row0 + r) * g.W, 1, g_out, g_in);
 }
 
 template <int AXIS>
@@ -243,6 +418,66 @@ __global__ void __launch_bounds__(256) k_soft_adj_yz(const float *src, const flo
     const int c = c0 + m;
     if (c >= n) break;
     soft_adj_one(slab + m * 32 + tx, 32, c, n, R, adj, other + x, s, g_out, g_in);
+  }
+}
+
+// the transposed min / max along y or z: each window's output gradient to its first extreme,
+// found by doubling over (value, staged position) pairs; g_in must start at zero
+template <int AXIS>
+__global__ void __launch_bounds__(512) k_soft_ext_adj_yz(const float *src, const float *g_out, float *g_in, SoftGeom g,
+                                                         int is_max, int R) {
+  __shared__ float slab[(kSoftTileYZ + 2 * kSoftExtMaxR) * 32];
+  __shared__ int at[(kSoftTileYZ + 2 * kSoftExtMaxR) * 32];
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int n = AXIS == 1 ? g.H : g.D;
+  const int64_t s = AXIS == 1 ? (int64_t)g.W : (int64_t)g.W * g.H;
+  const int x = blockIdx.x * 32 + tx;
+  const int c0 = blockIdx.y * kSoftTileYZ;
+  const int64_t other = AXIS == 1 ? (int64_t)blockIdx.z * g.W * g.H : (int64_t)blockIdx.z * g.W;
+  const float *line = src + other + x;
+  const int rows = kSoftTileYZ + 2 * R, q_end = soft_span(R);
+  for (int k = ty; k < rows; k += 16) {
+    slab[k * 32 + tx] = x < g.W ? soft_stage(line, s, c0 - R + k, n, kMin) : 0.0f;
+    at[k * 32 + tx] = k;
+  }
+  __syncthreads();
+  for (int q = 1; q < q_end; q *= 2) {
+    const int lim = rows - 2 * q + 1;
+    float v[kSoftExtPer];
+    int iv[kSoftExtPer];
+#pragma unroll
+    for (int e = 0; e < kSoftExtPer; e++) {
+      const int k = ty + 16 * e;
+      v[e] = 0.0f;
+      iv[e] = 0;
+      if (k < lim) {
+        v[e] = slab[k * 32 + tx];
+        iv[e] = at[k * 32 + tx];
+        soft_ext_at(v[e], iv[e], slab[(k + q) * 32 + tx], at[(k + q) * 32 + tx], is_max);
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int e = 0; e < kSoftExtPer; e++) {
+      const int k = ty + 16 * e;
+      if (k < lim) {
+        slab[k * 32 + tx] = v[e];
+        at[k * 32 + tx] = iv[e];
+      }
+    }
+    __syncthreads();
+  }
+  if (x >= g.W) return;
+  for (int m = ty; m < kSoftTileYZ; m += 16) {
+    const int c = c0 + m;
+    if (c >= n) break;
+    const float go = g_out[other + x + (int64_t)c * s];
+    if (go == 0.0f) continue;
+    float a = slab[m * 32 + tx];
+    int ia = at[m * 32 + tx];
+    const int m2 = m + 2 * R + 1 - q_end;
+    soft_ext_at(a, ia, slab[m2 * 32 + tx], at[m2 * 32 + tx], is_max);
+    atomicAdd(g_in + other + x + (int64_t)clampi(c0 - R + ia, 0, n - 1) * s, go);
   }
 }
 
@@ -325,13 +560,14 @@ __global__ void k_soft_add(float *a, const float *b, int64_t N) {
   if (i < N) a[i] += b[i];
 }
 
-// sum_i a[i] * b[i] into *out (double; out must start at zero)
+// sum_i a[i] * b[i] into *out (a double, which must start at zero; compensated float32 sums
+// up to the warps)
 __global__ void k_soft_dot(const float *a, const float *b, int64_t N, double *out) {
   __shared__ double part[8];
-  double acc = 0.0;
+  float hi = 0.0f, lo = 0.0f;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x)
-    acc += (double)a[i] * (double)b[i];
-  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xFFFFFFFFu, acc, o);
+    soft_dot_add(hi, lo, a[i], b[i]);
+  const double acc = soft_warp_dot(hi, lo);
   if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = acc;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -512,13 +748,20 @@ void pass(const SoftRun &R, const float *in, float *out, int axis, int mode, int
     return;
   }
   if (axis == 0) {
-    const unsigned blocks = (unsigned)(ceil_div(g.W, kSoftTileX) * (int64_t)g.H * g.D);
+    const unsigned blocks = (unsigned)(ceil_div(g.W, kSoftTileX) * ceil_div((int64_t)g.H * g.D, kSoftRowsX));
     KLAUNCH("k_soft_pass_x", R.st, (k_soft_pass_x<<<blocks, kSoftTileX, 0, R.st>>>(in, out, g, mode, reach, T)));
     return;
   }
   const size_t smem = (size_t)(kSoftTileYZ + 2 * reach) * 32 * sizeof(float);
   const int n = axis == 1 ? g.H : g.D, other = axis == 1 ? g.D : g.H;
   const dim3 grid((unsigned)ceil_div(g.W, 32), (unsigned)ceil_div(n, kSoftTileYZ), (unsigned)other);
+  if ((mode == kMin || mode == kMax) && reach <= kSoftExtMaxR) {
+    if (axis == 1)
+      KLAUNCH("k_soft_ext_y", R.st, (k_soft_ext_yz<1><<<grid, dim3(32, 16), 0, R.st>>>(in, out, g, mode == kMax, reach)));
+    else
+      KLAUNCH("k_soft_ext_z", R.st, (k_soft_ext_yz<2><<<grid, dim3(32, 16), 0, R.st>>>(in, out, g, mode == kMax, reach)));
+    return;
+  }
   if (axis == 1)
     KLAUNCH("k_soft_pass_y", R.st, (k_soft_pass_yz<1><<<grid, dim3(32, 8), smem, R.st>>>(in, out, g, mode, reach, T)));
   else
@@ -549,12 +792,22 @@ void adj_pass(const SoftRun &R, const float *src, const float *g_out, float *g_i
     return;
   }
   if (axis == 0) {
-    const unsigned blocks = (unsigned)(ceil_div(g.W, kSoftTileX) * (int64_t)g.H * g.D);
+    const unsigned blocks = (unsigned)(ceil_div(g.W, kSoftTileX) * ceil_div((int64_t)g.H * g.D, kSoftRowsX));
     KLAUNCH("k_soft_adj_x", R.st, (k_soft_adj_x<<<blocks, kSoftTileX, 0, R.st>>>(src, g_out, g_in, g, adj, r)));
     return;
   }
-  const size_t smem = (size_t)(kSoftTileYZ + 2 * r) * 32 * sizeof(float);
   const int n = axis == 1 ? g.H : g.D, other = axis == 1 ? g.D : g.H;
+  if (adj != kAdjBox && r <= kSoftExtMaxR) {
+    const dim3 grid((unsigned)ceil_div(g.W, 32), (unsigned)ceil_div(n, kSoftTileYZ), (unsigned)other);
+    if (axis == 1)
+      KLAUNCH("k_soft_ext_adj_y", R.st, (k_soft_ext_adj_yz<1><<<grid, dim3(32, 16), 0, R.st>>>(src, g_out, g_in, g,
+                                                                                              adj == kAdjMax, r)));
+    else
+      KLAUNCH("k_soft_ext_adj_z", R.st, (k_soft_ext_adj_yz<2><<<grid, dim3(32, 16), 0, R.st>>>(src, g_out, g_in, g,
+                                                                                              adj == kAdjMax, r)));
+    return;
+  }
+  const size_t smem = (size_t)(kSoftTileYZ + 2 * r) * 32 * sizeof(float);
   const dim3 grid((unsigned)ceil_div(g.W, 32), (unsigned)ceil_div(n, kSoftTileYZ), (unsigned)other);
   if (axis == 1)
     KLAUNCH("k_soft_adj_y", R.st, (k_soft_adj_yz<1><<<grid, dim3(32, 8), smem, R.st>>>(src, g_out, g_in, g, adj, r)));
@@ -645,7 +898,7 @@ int soft_forward(const hdog_soft_params *p, const float *vol, const int32_t *pos
 
 int soft_backward(const hdog_soft_params *p, const float *vol, const int32_t *pos, int n_pos, const int32_t *neg,
                   int n_neg, float grad_loss, float *grad_vol, float *grad_sigma, float *grad_thresh, void *work,
-                  cudaStream_t st) {
+                  cudaStream_t st, bool forward_kept) {
   const int rc = check_params(p, vol, pos, n_pos, neg, n_neg, work);
   if (rc != HDOG_OK) return rc;
   SoftRun R{*p, SoftGeom{p->width, p->height, p->depth}, (int64_t)p->width * p->height * p->depth, st,
@@ -653,7 +906,9 @@ int soft_backward(const hdog_soft_params *p, const float *vol, const int32_t *po
   R.acc = static_cast<double *>(work);
   R.w = reinterpret_cast<float *>(R.acc + 16);
   const unsigned nb = R.blocks();
-  forward_chain(R, vol);
+  // The backward reads the forward chain's slots (S_MN1 .. S_DOG) and writes only the others,
+  // so a workspace that soft_forward filled for the same inputs still holds them.
+  if (!forward_kept) forward_chain(R, vol);
   float *gdog = R.slot(S_GDOG);
   cudaMemsetAsync(gdog, 0, R.N * sizeof(float), st);
   double *gb = R.acc + 8;   // threshold gradients

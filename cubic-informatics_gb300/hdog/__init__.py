@@ -156,6 +156,8 @@ _SIGNATURES = {
                                          _P, _P, _P, _P]),
     "hdog_soft_backward": (ctypes.c_int, [ctypes.POINTER(hdog_soft_params), _P, _P, ctypes.c_int, _P, ctypes.c_int,
                                           ctypes.c_float, _P, _P, _P, _P, _P]),
+    "hdog_soft_backward_kept": (ctypes.c_int, [ctypes.POINTER(hdog_soft_params), _P, _P, ctypes.c_int, _P,
+                                               ctypes.c_int, ctypes.c_float, _P, _P, _P, _P, _P]),
     "hdog_memcpy": (ctypes.c_int, [_P, _P, ctypes.c_size_t, _P]),
     "hdog_stream_sync": (ctypes.c_int, [_P]),
     "hdog_device_alloc": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.c_size_t]),

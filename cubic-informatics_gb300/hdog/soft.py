@@ -7,6 +7,11 @@ sample points.  Torch only holds the tensors and the graph; every stage runs in 
                                radius_norm_z=5, min_intensity=50.0, tau=1e-3)
     loss.backward()      # volume.grad, sigma.grad, b.grad
 
+By default the forward's workspace (17 volume-sized float32 buffers) stays alive until the
+backward, which then takes the forward chain's intermediates from it instead of recomputing
+them (same results); keep_intermediates=False frees it after the forward and the backward
+recomputes.
+
 volume: (D, H, W) float32 CUDA tensor; sigma: 6 values (x1, y1, z1, x2, y2, z2; the small
 then the large scale); thresh: 3 offsets (b0, b1, b2) of the relaxed tests xx < b0,
 xx yy - xy^2 > b1, det < b2 (zero: the reference's mask test), optional; pos / neg: (n, 3)
@@ -42,7 +47,7 @@ def _check_inputs(vol, pos, neg):
 
 class SoftLoss(torch.autograd.Function):
     @staticmethod
-    def forward(ctx, vol, sigma, thresh, pos, neg, cfg):
+    def forward(ctx, vol, sigma, thresh, pos, neg, cfg, keep):
         _check_inputs(vol, pos, neg)
         p = _params(vol, sigma, thresh, cfg)
         ws = torch.empty(lib().hdog_soft_workspace_bytes(ctypes.byref(p)), dtype=torch.uint8, device=vol.device)
@@ -52,6 +57,8 @@ class SoftLoss(torch.autograd.Function):
                                       _ptr(loss), None, _ptr(ws), stream))
         ctx.save_for_backward(vol, sigma, thresh, pos, neg)
         ctx.cfg = cfg
+        # the saved tensors' version check already refuses a volume changed in place since
+        ctx.kept = ws if keep else None
         return loss[0]
 
     @staticmethod
@@ -62,24 +69,30 @@ class SoftLoss(torch.autograd.Function):
         gv = torch.zeros_like(vol) if want_vol else None
         gs = torch.zeros(6, dtype=torch.float32, device=vol.device) if want_sigma else None
         gb = torch.zeros(3, dtype=torch.float32, device=vol.device) if want_thresh else None
-        ws = torch.empty(lib().hdog_soft_workspace_bytes(ctypes.byref(p)), dtype=torch.uint8, device=vol.device)
         stream = ctypes.c_void_p(torch.cuda.current_stream(vol.device).cuda_stream)
-        check(lib().hdog_soft_backward(ctypes.byref(p), _ptr(vol), _ptr(pos), pos.shape[0], _ptr(neg), neg.shape[0],
-                                       float(grad), _ptr(gv), _ptr(gs), _ptr(gb), _ptr(ws), stream))
+        if ctx.kept is not None:
+            ws = ctx.kept
+            fn = lib().hdog_soft_backward_kept
+        else:
+            ws = torch.empty(lib().hdog_soft_workspace_bytes(ctypes.byref(p)), dtype=torch.uint8, device=vol.device)
+            fn = lib().hdog_soft_backward
+        check(fn(ctypes.byref(p), _ptr(vol), _ptr(pos), pos.shape[0], _ptr(neg), neg.shape[0], float(grad), _ptr(gv),
+                 _ptr(gs), _ptr(gb), _ptr(ws), stream))
         if gs is not None:
             gs = gs.to(device=sigma.device, dtype=sigma.dtype).reshape(sigma.shape)
         if gb is not None:
             gb = gb.to(device=thresh.device, dtype=thresh.dtype).reshape(thresh.shape)
-        return gv, gs, gb, None, None, None
+        return gv, gs, gb, None, None, None, None
 
 
 def soft_loss(vol, sigma, pos, neg, thresh=None, radius_norm_xy=20, radius_norm_z=5, min_intensity=50.0, tau=1e-3,
-              gamma=1.0):
+              gamma=1.0, keep_intermediates=True):
     """Mean relaxed mask score at pos minus that at neg (see the module docstring)."""
     if thresh is None:
         thresh = torch.zeros(3, dtype=torch.float32)
     pos, neg = pos.contiguous(), neg.contiguous()
-    return SoftLoss.apply(vol, sigma, thresh, pos, neg, (radius_norm_xy, radius_norm_z, min_intensity, tau, gamma))
+    return SoftLoss.apply(vol, sigma, thresh, pos, neg, (radius_norm_xy, radius_norm_z, min_intensity, tau, gamma),
+                          bool(keep_intermediates))
 
 
 def fit(vol, pos, neg, sigma0, thresh0=(0.0, 0.0, 0.0), steps=20, lr=0.05, lr_thresh=None, fit_thresholds=True,

@@ -308,8 +308,8 @@ int hdog_classifier_features(const hdog_record *d_records, int64_t n, const hdog
    sigmoid((b0 - xx) / tau) * sigmoid((xx yy - xy^2 - b1) / tau^2) * sigmoid((b2 - det) / tau^3)
    with thresholds b (zero: the reference's test).  Loss = mean score at the positive points -
    mean score at the negative points.  Points are int32 (z, y, x) triples.  Backward
-   recomputes the forward from the input (the workspace holds nothing between calls) and
-   returns d loss / d volume, d loss / d sigma and d loss / d thresholds (any may be NULL);
+   recomputes the forward from the input and returns d loss / d volume, d loss / d sigma and
+   d loss / d thresholds (any may be NULL);
    tap radii (int)(2 sigma + 0.5) are held fixed for the derivatives.  Sigmas up to 15.7
    (radius 31).  The workspace is device memory of hdog_soft_workspace_bytes bytes. */
 typedef struct hdog_soft_params {
@@ -328,6 +328,14 @@ int hdog_soft_forward(const hdog_soft_params *p, const float *d_volume, const in
 int hdog_soft_backward(const hdog_soft_params *p, const float *d_volume, const int32_t *d_pos, int n_pos,
                        const int32_t *d_neg, int n_neg, float grad_loss, float *d_grad_volume,
                        float *d_grad_sigma, float *d_grad_thresh, void *d_workspace, void *stream);
+/* hdog_soft_backward that takes the forward chain's intermediates (min / max and box-mean
+   volumes, normalized volume, DoG) from d_workspace instead of recomputing them: the
+   workspace must be the one an hdog_soft_forward call filled with the same parameters and
+   volume, with nothing else written to it since (backward calls leave those parts intact, so
+   several may follow one forward).  Same results as hdog_soft_backward. */
+int hdog_soft_backward_kept(const hdog_soft_params *p, const float *d_volume, const int32_t *d_pos, int n_pos,
+                            const int32_t *d_neg, int n_neg, float grad_loss, float *d_grad_volume,
+                            float *d_grad_sigma, float *d_grad_thresh, void *d_workspace, void *stream);
 
 /* ---- context options ---- */
 enum {

@@ -119,6 +119,31 @@ def test_gpu_forward_and_adjoint_match_reference(reference):
 
 
 @pytest.mark.gpu
+def test_gpu_backward_from_the_kept_forward_equals_the_recomputed_one(reference):
+    """The backward that takes the forward's intermediates from its workspace (the default)
+    against the one that recomputes them, and two backward calls after one forward: the
+    same gradients up to the order of the double and float atomic sums (a last-bit effect)."""
+    import hdog
+    vol, pos, neg, tau, b = reference[:5]
+    p, n = torch.tensor(pos, device="cuda"), torch.tensor(neg, device="cuda")
+
+    def grads(keep, calls=1):
+        v = torch.tensor(vol, dtype=torch.float32, device="cuda", requires_grad=True)
+        s = torch.tensor(SIGMA, dtype=torch.float32, requires_grad=True)
+        bt = torch.tensor(b, dtype=torch.float32, requires_grad=True)
+        loss = hdog.soft.soft_loss(v, s, p, n, thresh=bt, radius_norm_xy=RXY, radius_norm_z=RZ,
+                                   min_intensity=MIN_INT, tau=tau, keep_intermediates=keep)
+        for k in range(calls):
+            loss.backward(retain_graph=k + 1 < calls)
+        return v.grad.cpu().numpy() / calls, s.grad.numpy() / calls, bt.grad.numpy() / calls
+
+    kept, again, recomputed = grads(True), grads(True, calls=2), grads(False)
+    for g in (again, recomputed):
+        for a, r in zip(kept, g):
+            assert np.allclose(a, r, rtol=1e-6, atol=1e-6 * np.abs(r).max()), (np.abs(a - r).max(), np.abs(r).max())
+
+
+@pytest.mark.gpu
 def test_gpu_sigma_fit_improves_the_loss(reference):
     import hdog
     vol, pos, neg, tau = reference[:4]
