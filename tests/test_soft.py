@@ -119,6 +119,46 @@ def test_gpu_forward_and_adjoint_match_reference(reference):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("rxy,rz", [(20, 5), (40, 3)])
+def test_gpu_adjoint_with_wide_normalization_windows(rxy, rz):
+    """The case above with the workload's normalization reach (20, 5) and with a reach of 40
+    (wider than the lines; the x tiles up to 64, the y / z min / max kernels up to 32, the
+    y / z tiles above), against the FP64 reference gradient.  The sigma gradients are held to
+    2e-4 relative here: the float32 box means sum 41 values per axis, and the sigma gradients,
+    which go through second differences of the DoG and sigmoids scaled by 1/tau^3, move by
+    about 1e-4 for a last-bit change of the normalized volume (measured: 1.22e-4 on sigma_y1
+    at reach 20; min / max do not round, so this is the float32 rounding of the box means and
+    Gaussians); the loss, threshold and input gradients keep the bounds above."""
+    import hdog
+    vol, pos, neg = case()
+    with torch.no_grad():
+        h = sr.hessian(sr.dog(sr.normalize(torch.tensor(vol), rxy, rz, MIN_INT),
+                              [torch.tensor(v, dtype=torch.float64) for v in SIGMA]))
+        tau = float(torch.stack([e[pos[:, 0], pos[:, 1], pos[:, 2]].abs() for e in h]).median())
+    b = thresholds(tau)
+    I = torch.tensor(vol, dtype=torch.float64, requires_grad=True)
+    sig = torch.tensor(SIGMA, dtype=torch.float64, requires_grad=True)
+    bt = torch.tensor(b, dtype=torch.float64, requires_grad=True)
+    L = sr.loss(I, list(sig), torch.tensor(pos, dtype=torch.long), torch.tensor(neg, dtype=torch.long), rxy, rz,
+                MIN_INT, tau, b=list(bt))
+    L.backward()
+    v = torch.tensor(vol, dtype=torch.float32, device="cuda", requires_grad=True)
+    s = torch.tensor(SIGMA, dtype=torch.float32, requires_grad=True)
+    b32 = torch.tensor(b, dtype=torch.float32, requires_grad=True)
+    loss = hdog.soft.soft_loss(v, s, torch.tensor(pos, device="cuda"), torch.tensor(neg, device="cuda"), thresh=b32,
+                               radius_norm_xy=rxy, radius_norm_z=rz, min_intensity=MIN_INT, tau=tau)
+    loss.backward()
+    assert abs(float(loss.detach()) - float(L.detach())) <= 1e-5 * abs(float(L.detach()))
+    gs = sig.grad.numpy()
+    assert np.all(np.abs(s.grad.numpy() - gs) <= 2e-4 * np.abs(gs) + 1e-9), (s.grad.numpy(), gs)
+    gb = bt.grad.numpy()
+    assert np.all(np.abs(b32.grad.numpy() - gb) <= 1e-4 * np.abs(gb)), (b32.grad.numpy(), gb)
+    gI = I.grad.numpy()
+    err = np.abs(v.grad.cpu().numpy().astype(np.float64) - gI)
+    assert err.max() <= 1e-4 * np.abs(gI).max(), (float(err.max()), float(np.abs(gI).max()))
+
+
+@pytest.mark.gpu
 def test_gpu_backward_from_the_kept_forward_equals_the_recomputed_one(reference):
     """The backward that takes the forward's intermediates from its workspace (the default)
     against the one that recomputes them, and two backward calls after one forward: the
