@@ -219,13 +219,16 @@ __global__ void __launch_bounds__(kSoftTileX) k_soft_pass_x(const float *in, flo
 }
 
 // along y (AXIS 1) or z (AXIS 2): a block of 32 x 8 threads owns 32 columns and
-// kSoftTileYZ outputs of each; thread (tx, ty) computes outputs ty, ty + 8, ...  With DOT the
-// outputs are not stored: the block adds sum(output * dotw) over its outputs to *dot_out
-// (a double; compensated float32 sums up to the warps).
-template <int AXIS, bool DOT = false>
+// kSoftTileYZ outputs of each; thread (tx, ty) computes outputs ty, ty + 8, ...  The epilogue
+// stores the outputs (kEpiStore); or stores scale * (aux - output), the DoG difference
+// (kEpiDiff); or stores nothing and adds sum(output * aux) over the block's outputs to
+// *dot_out (kEpiDot; a double, from compensated float32 sums up to the warps).
+enum { kEpiStore = 0, kEpiDot = 1, kEpiDiff = 2 };
+
+template <int AXIS, int EPI = kEpiStore>
 __global__ void __launch_bounds__(256) k_soft_pass_yz(const float *in, float *out, SoftGeom g, int mode, int R,
-                                                      SoftTaps T, const float *dotw = nullptr,
-                                                      double *dot_out = nullptr) {
+                                                      SoftTaps T, const float *aux = nullptr,
+                                                      double *dot_out = nullptr, float scale = 0.0f) {
   extern __shared__ float slab[];   // [kSoftTileYZ + 2R][32]
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int n = AXIS == 1 ? g.H : g.D;
@@ -245,10 +248,11 @@ __global__ void __launch_bounds__(256) k_soft_pass_yz(const float *in, float *ou
       if (c >= n) break;
       const int64_t i = other + x + (int64_t)c * s;
       const float v = soft_fold(slab + m * 32 + tx, 32, c, n, mode, R, T);
-      if (DOT) soft_dot_add(hi, lo, dotw[i], v);
+      if (EPI == kEpiDot) soft_dot_add(hi, lo, aux[i], v);
+      else if (EPI == kEpiDiff) out[i] = scale * (aux[i] - v);
       else out[i] = v;
     }
-  if (DOT) {
+  if (EPI == kEpiDot) {
     __shared__ double part[8];
     const double acc = soft_warp_dot(hi, lo);
     if (tx == 0) part[ty] = acc;
@@ -550,11 +554,6 @@ __global__ void k_soft_norm_adj(const float *I, const float *e, const float *d, 
 }
 
 // out = scale * (a - b)
-__global__ void k_soft_diff(const float *a, const float *b, float *out, float scale, int64_t N) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < N) out[i] = scale * (a[i] - b[i]);
-}
-
 __global__ void k_soft_add(float *a, const float *b, int64_t N) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < N) a[i] += b[i];
@@ -774,8 +773,21 @@ void pass_z_dot(const SoftRun &R, const float *in, const SoftTaps &T, const floa
   const SoftGeom &g = R.g;
   const size_t smem = (size_t)(kSoftTileYZ + 2 * T.r) * 32 * sizeof(float);
   const dim3 grid((unsigned)ceil_div(g.W, 32), (unsigned)ceil_div(g.D, kSoftTileYZ), (unsigned)g.H);
-  KLAUNCH("k_soft_pass_z_dot", R.st, (k_soft_pass_yz<2, true><<<grid, dim3(32, 8), smem, R.st>>>(
+  KLAUNCH("k_soft_pass_z_dot", R.st, (k_soft_pass_yz<2, kEpiDot><<<grid, dim3(32, 8), smem, R.st>>>(
                                          in, nullptr, g, kConv, T.r, T, w, acc)));
+}
+
+// the separable Gaussian (x, y, then z) with the DoG difference folded into the z pass:
+// out = scale * (sub - in * G), the same operations as a separate difference kernel
+void conv3_diff(const SoftRun &R, const float *in, float *out, const SoftTaps &tx, const SoftTaps &ty,
+                const SoftTaps &tz, float *t1, float *t2, const float *sub, float scale) {
+  pass(R, in, t1, 0, kConv, 0, tx);
+  pass(R, t1, t2, 1, kConv, 0, ty);
+  const SoftGeom &g = R.g;
+  const size_t smem = (size_t)(kSoftTileYZ + 2 * tz.r) * 32 * sizeof(float);
+  const dim3 grid((unsigned)ceil_div(g.W, 32), (unsigned)ceil_div(g.D, kSoftTileYZ), (unsigned)g.H);
+  KLAUNCH("k_soft_pass_z_diff", R.st, (k_soft_pass_yz<2, kEpiDiff><<<grid, dim3(32, 8), smem, R.st>>>(
+                                          t2, out, g, kConv, tz.r, tz, sub, nullptr, scale)));
 }
 
 // a transposed pass along `axis`: box gather (src = g_out, into g_in) or min / max scatter
@@ -847,11 +859,9 @@ void forward_chain(const SoftRun &R, const float *vol) {
   const float *s = p.sigma;
   conv3(R, R.slot(S_NORM), R.slot(S_T3), gauss_taps_f(s[0], false), gauss_taps_f(s[1], false), gauss_taps_f(s[2], false),
         R.slot(S_T1), R.slot(S_T2));
-  conv3(R, R.slot(S_NORM), R.slot(S_GA), gauss_taps_f(s[3], false), gauss_taps_f(s[4], false), gauss_taps_f(s[5], false),
-        R.slot(S_T1), R.slot(S_T2));
   const float nrm = (float)pow((double)s[0] * s[1] * s[2], (double)p.gamma);
-  KLAUNCH("k_soft_diff", R.st, (k_soft_diff<<<R.blocks(), 256, 0, R.st>>>(R.slot(S_T3), R.slot(S_GA), R.slot(S_DOG),
-                                                                        nrm, R.N)));
+  conv3_diff(R, R.slot(S_NORM), R.slot(S_DOG), gauss_taps_f(s[3], false), gauss_taps_f(s[4], false),
+             gauss_taps_f(s[5], false), R.slot(S_T1), R.slot(S_T2), R.slot(S_T3), nrm);
 }
 
 SoftThresh thresh_of(const hdog_soft_params &p) {
@@ -960,16 +970,19 @@ int soft_backward(const hdog_soft_params *p, const float *vol, const int32_t *po
     // g_norm = normalizer (G1 - G2)^T gdog = normalizer (G1 gdog - G2 gdog)
     conv3(R, gdog, R.slot(S_T3), gauss_taps_f(s[0], false), gauss_taps_f(s[1], false), gauss_taps_f(s[2], false),
           R.slot(S_T1), R.slot(S_T2));
-    conv3(R, gdog, R.slot(S_GA), gauss_taps_f(s[3], false), gauss_taps_f(s[4], false), gauss_taps_f(s[5], false),
-          R.slot(S_T1), R.slot(S_T2));
-    KLAUNCH("k_soft_diff", st, (k_soft_diff<<<nb, 256, 0, st>>>(R.slot(S_T3), R.slot(S_GA), R.slot(S_GB), nrm, R.N)));
+    conv3_diff(R, gdog, R.slot(S_GB), gauss_taps_f(s[3], false), gauss_taps_f(s[4], false), gauss_taps_f(s[5], false),
+               R.slot(S_T1), R.slot(S_T2), R.slot(S_T3), nrm);
     // quotient rule: direct term into grad_vol, g_e -> S_T1, g_d -> S_T2
     KLAUNCH("k_soft_norm_adj", st, (k_soft_norm_adj<<<nb, 256, 0, st>>>(vol, R.slot(S_E), R.slot(S_D), R.slot(S_GB),
                                                                        grad_vol, R.slot(S_T1), R.slot(S_T2),
                                                                        p->min_intensity, R.N)));
     const int rr[3] = {p->radius_norm_xy, p->radius_norm_xy, p->radius_norm_z};
     // min side then max side: box means transposed z -> y -> x, then the min / max filters
-    // transposed z -> y -> x, each scattering into a zeroed buffer
+    // transposed z -> y -> x, each scattering into a zeroed buffer but the last, which
+    // scatters straight into the input gradient (holding the quotient rule's direct term)
+    int last = -1;   // the axis of the last min / max pass: the lowest one with a window
+    for (int a = 2; a >= 0; a--)
+      if (rr[a] != 0) last = a;
     for (int side = 0; side < 2; side++) {
       float *g = R.slot(side == 0 ? S_T1 : S_T2);
       float *ping = R.slot(S_GA), *pong = R.slot(S_GC);
@@ -984,13 +997,16 @@ int soft_backward(const hdog_soft_params *p, const float *vol, const int32_t *po
       const float *fin[3] = {vol, R.slot(side == 0 ? S_MN1 : S_MX1), R.slot(side == 0 ? S_MN2 : S_MX2)};
       for (int a = 2; a >= 0; a--) {
         if (rr[a] == 0) continue;
-        float *dst = (cur == ping) ? pong : ping;
-        if (dst == g) dst = R.slot(S_GB);
-        cudaMemsetAsync(dst, 0, R.N * sizeof(float), st);
+        float *dst = grad_vol;
+        if (a != last) {
+          dst = (cur == ping) ? pong : ping;
+          if (dst == g) dst = R.slot(S_GB);
+          cudaMemsetAsync(dst, 0, R.N * sizeof(float), st);
+        }
         adj_pass(R, fin[a], cur, dst, a, side == 0 ? kAdjMin : kAdjMax, rr[a]);
         cur = dst;
       }
-      KLAUNCH("k_soft_add", st, (k_soft_add<<<nb, 256, 0, st>>>(grad_vol, cur, R.N)));
+      if (last < 0) KLAUNCH("k_soft_add", st, (k_soft_add<<<nb, 256, 0, st>>>(grad_vol, cur, R.N)));
     }
   }
   HDOG_CUDA_TRY(cudaGetLastError());
