@@ -167,3 +167,50 @@ def test_context_bytes_scale_with_substacks():
     n = 2560 * 2160 * 32
     assert 30 * n < a.value < 70 * n
     assert 3.9 * a.value < b.value < 4.1 * a.value
+
+
+def soft_params(**kw):
+    v = dict(width=44, height=40, depth=14, radius_norm_xy=4, radius_norm_z=2, min_intensity=50.0,
+             sigma=[1.2, 1.3, 1.1, 1.9, 2.1, 1.7], gamma=1.0, tau=1e-3, thresh=[0.0, 0.0, 0.0])
+    v.update(kw)
+    return hdog.hdog_soft_params(v["width"], v["height"], v["depth"], v["radius_norm_xy"], v["radius_norm_z"],
+                                 v["min_intensity"], (ctypes.c_float * 6)(*v["sigma"]), v["gamma"], v["tau"],
+                                 (ctypes.c_float * 3)(*v["thresh"]))
+
+
+@pytest.mark.parametrize("what,kw,ptrs,code", [
+    ("no volume", {}, dict(vol=None), hdog.HDOG_ERR_ARG),
+    ("no workspace", {}, dict(work=None), hdog.HDOG_ERR_ARG),
+    ("negative point count", {}, dict(n_pos=-1), hdog.HDOG_ERR_ARG),
+    ("points without a pointer", {}, dict(pos=None), hdog.HDOG_ERR_ARG),
+    ("empty frame", dict(width=0), {}, hdog.HDOG_ERR_PARAM),
+    ("tau not positive", dict(tau=0.0), {}, hdog.HDOG_ERR_PARAM),
+    ("negative normalization radius", dict(radius_norm_z=-1), {}, hdog.HDOG_ERR_PARAM),
+    ("sigma with taps past radius 31", dict(sigma=[1.2, 1.3, 1.1, 1.9, 2.1, 15.8]), {}, hdog.HDOG_ERR_SHAPE),
+    ("sigma not positive", dict(sigma=[1.2, 0.0, 1.1, 1.9, 2.1, 1.7]), {}, hdog.HDOG_ERR_SHAPE),
+])
+def test_soft_entry_points_check_their_arguments_on_the_host(what, kw, ptrs, code):
+    """The differentiable chain's three entry points refuse bad arguments before any device
+    work (the pointers below are never dereferenced: every case fails its checks first)."""
+    L = hdog.lib()
+    p = soft_params(**kw)
+    fake = ctypes.c_void_p(4096)
+    a = dict(vol=fake, pos=fake, n_pos=3, neg=fake, n_neg=2, work=fake)
+    a.update(ptrs)
+    out = ctypes.c_void_p(8192)
+    rc = L.hdog_soft_forward(ctypes.byref(p), a["vol"], a["pos"], a["n_pos"], a["neg"], a["n_neg"], out, None,
+                             a["work"], None)
+    assert rc == code, (what, rc)
+    assert b"hdog_soft_forward" in L.hdog_last_error()
+    for name in ("hdog_soft_backward", "hdog_soft_backward_kept"):
+        rc = getattr(L, name)(ctypes.byref(p), a["vol"], a["pos"], a["n_pos"], a["neg"], a["n_neg"], 1.0, None, None,
+                              None, a["work"], None)
+        assert rc == code, (what, name, rc)
+        assert name.encode() in L.hdog_last_error()
+
+
+def test_soft_forward_needs_a_loss_pointer():
+    L = hdog.lib()
+    p = soft_params()
+    fake = ctypes.c_void_p(4096)
+    assert L.hdog_soft_forward(ctypes.byref(p), fake, fake, 1, fake, 1, None, None, fake, None) == hdog.HDOG_ERR_ARG
