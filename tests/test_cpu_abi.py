@@ -214,3 +214,22 @@ def test_soft_forward_needs_a_loss_pointer():
     p = soft_params()
     fake = ctypes.c_void_p(4096)
     assert L.hdog_soft_forward(ctypes.byref(p), fake, fake, 1, fake, 1, None, None, fake, None) == hdog.HDOG_ERR_ARG
+
+
+def test_graph_entry_points_check_their_arguments_on_the_host():
+    """The batched graph form's entry points refuse missing arguments before any device work;
+    destroying a null graph is a no-op."""
+    L = hdog.lib()
+    out = ctypes.c_void_p()
+    assert L.hdog_graph_create(None, 1, None, 0, None, None) == hdog.HDOG_ERR_ARG
+    assert L.hdog_graph_create(None, 1, None, 0, None, ctypes.byref(out)) == hdog.HDOG_ERR_ARG
+    assert out.value is None
+    ctx = (ctypes.c_void_p * 1)()
+    assert L.hdog_graph_create(ctx, 0, None, 0, None, ctypes.byref(out)) == hdog.HDOG_ERR_ARG
+    assert L.hdog_graph_create(ctx, 1, None, 2, None, ctypes.byref(out)) == hdog.HDOG_ERR_ARG
+    assert L.hdog_graph_create(ctx, 1, None, 0, None, ctypes.byref(out)) == hdog.HDOG_ERR_ARG   # null context
+    assert b"hdog_graph_create" in L.hdog_last_error()
+    n = ctypes.c_int64()
+    assert L.hdog_graph_run(None, None, 0, ctypes.byref(n), None, None) == hdog.HDOG_ERR_ARG
+    assert L.hdog_graph_last_records(None, None, 0, ctypes.byref(n)) == hdog.HDOG_ERR_ARG
+    assert L.hdog_graph_destroy(None) == hdog.HDOG_OK
